@@ -1,0 +1,160 @@
+/*
+ * wtomo3d-gb300: GB300-native forward-modelling hot path of wtomo3d.
+ *
+ * C ABI of libwtomo3d_gpu.so.  Every entry point takes plain pointers and
+ * sizes and returns an int status (0 = success) unless stated otherwise.
+ * Complex values are interleaved (re, im) pairs: `double _Complex` /
+ * `float _Complex` in C, COMPLEX(C_DOUBLE_COMPLEX)/COMPLEX(C_FLOAT_COMPLEX)
+ * in Fortran.
+ *
+ * Grid ordering follows the reference: node g = iz + nz*(ix-1) + nx*nz*(iy-1)
+ * (1-based, z fastest; srgraphs.f:689,696), dofs 3g-2..3g = (u, v, w).
+ * Model arrays are (nz, nx, ny) column-major float arrays (modelio.f90:104-111
+ * layout after MODELIO_H52WT_MODEL).
+ */
+#ifndef WTOMO3D_GPU_H
+#define WTOMO3D_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define WT3D_OK                0
+#define WT3D_ERR_ARG           1   /* invalid argument                        */
+#define WT3D_ERR_CUDA          2   /* CUDA runtime error                      */
+#define WT3D_ERR_NOMEM         3   /* device or host allocation failed        */
+#define WT3D_ERR_STATE         4   /* call out of order (no model, no factor) */
+#define WT3D_ERR_PATTERN       5   /* CSR pattern is not a 27-point grid graph */
+#define WT3D_ERR_NOCONV        6   /* refinement did not reach the tolerance  */
+#define WT3D_ERR_NOGPU         7   /* no CUDA device                          */
+
+/* ---- precisions --------------------------------------------------------- */
+#define WT3D_PREC_MIXED        0   /* complex64 fronts + FP64 refinement      */
+#define WT3D_PREC_FP64         1   /* complex128 fronts (the FP64 GPU oracle)  */
+
+/* Grid and boundary description.  Replaces the INIT_/MODEL_/PML_MODULE
+ * globals read by ASMBLE (modules.F90:1-76) and the ini keys of
+ * readini.f90:46-86,216.  pmld <= 0 selects the reference default 10*dx;
+ * pmlr <= 0 selects 1e-3. */
+typedef struct wt3d_grid {
+    int    nx, ny, nz;
+    double dx;          /* dx = dy = dz (readini.f90:55-59)                 */
+    double pmld;        /* PML width in metres                              */
+    double pmlr;        /* PML reflection coefficient                       */
+    int    fst;         /* free surface on top (model:fst, default true)    */
+    int    usemin;      /* Min-cell free surface (optional:usemin)          */
+} wt3d_grid;
+
+/* ---- drop-in boundary of the reference ---------------------------------
+ * Replaces strumpack_serial_finter (strumpack_finter.c:9-121; Fortran
+ * interface interface.f90:295-309).  Same symbol, signature, job protocol and
+ * error convention:
+ *   job  1 : initialise and analyse the 1-based CSR pattern (values unused)
+ *   job  2 : (re)set values and factor
+ *   job  3 : solve one right-hand side: sol = A^-1 rhs
+ *   job -1 : destroy
+ * *ierr = 0 on success, 1 on error (with a message on stdout), as the
+ * reference.  irptr/jcptr are read, never modified.  The pattern must be the
+ * 27-point, 3-dof grid graph built by srel3d + SPARSE_ADJ2CRS; the grid is
+ * recovered from it.  Factorisation is complex64 with FP64 iterative
+ * refinement; the solution is returned in complex64 as the reference does.
+ * Not re-entrant (one global instance, like the reference). */
+void strumpack_serial_finter(int *job, int *nrows, int *nnz,
+                             int *irptr, int *jcptr, float _Complex *a,
+                             float _Complex *rhs, float _Complex *sol,
+                             int *ierr);
+
+/* ---- pattern and assembly ----------------------------------------------
+ * wt3d_pattern replaces srel3d_getsize + srel3d + SPARSE_ADJ2CRS
+ * (srgraphs.f:626-734, sparse.f:13-49).  n = 3*nx*ny*nz, nnz =
+ * 9(3nx-2)(3ny-2)(3nz-2).  base = 0 or 1.  Host arrays irptr[n+1], jcptr[nnz]. */
+long long wt3d_pattern_nnz(int nx, int ny, int nz);
+int wt3d_pattern(int nx, int ny, int nz, int base, int *irptr, int *jcptr);
+
+/* wt3d_assemble replaces ASMBLE (asmble.f90:1-636; interface.f90:4-12) with
+ * the model set up as modelio.f90:78-92 does.  Host arrays in and out; the
+ * work runs on the current CUDA device.  a[nnz] receives complex128 values in
+ * the CSR order of wt3d_pattern.  omega = 2*pi*f (+ i/tau) as elwave.f90:151,164. */
+int wt3d_assemble(const wt3d_grid *g, const float *vp, const float *vs, const float *rho,
+                  double omega_re, double omega_im, double _Complex *a);
+
+/* Device-pointer variant: d_vp/d_vs/d_rho device floats, d_irptr the 0-based
+ * row pointer on the device (n+1 ints), d_a device complex128[nnz].
+ * stream is a cudaStream_t (NULL = default stream).  Asynchronous. */
+int wt3d_assemble_device(const wt3d_grid *g, const float *d_vp, const float *d_vs,
+                         const float *d_rho, double omega_re, double omega_im,
+                         const int *d_irptr, void *d_a, void *stream);
+
+/* ---- handle-based solver (re-entrant siblings of the job protocol) ------ */
+typedef struct wt3d_solver wt3d_solver;
+
+/* Analyse: nested-dissection ordering and symbolic factorisation of the grid
+ * graph on the host; allocates the front storage on the device. */
+int wt3d_solver_create(wt3d_solver **h, const wt3d_grid *g, int precision);
+int wt3d_solver_destroy(wt3d_solver *h);
+
+/* Model (host arrays, (nz,nx,ny) floats). */
+int wt3d_set_model(wt3d_solver *h, const float *vp, const float *vs, const float *rho);
+
+/* Assemble A(omega) on the device and factor it (precision from create). */
+int wt3d_factor(wt3d_solver *h, double omega_re, double omega_im);
+
+/* Set caller-assembled operator values (complex64, host, CSR order of
+ * wt3d_pattern) and factor them; the job-2 path of strumpack_serial_finter
+ * (strumpack_finter.c:68-92). */
+int wt3d_set_values_c64(wt3d_solver *h, const float _Complex *a);
+int wt3d_factor_values(wt3d_solver *h);
+
+/* Solve A X = B for nrhs right-hand sides (host arrays, column k of B at
+ * B + k*n, complex128).  Mixed precision refines in FP64 until every column
+ * has ||b - A x|| / ||b|| <= tol or maxit refinement steps are done.
+ * relres[nrhs] (may be NULL) receives the final relative residuals,
+ * *iters (may be NULL) the refinement steps taken.  Returns WT3D_ERR_NOCONV
+ * (with X filled) if the tolerance was not reached. */
+int wt3d_solve(wt3d_solver *h, int nrhs, const double _Complex *B, double _Complex *X,
+               double tol, int maxit, double *relres, int *iters);
+
+/* Conjugate-transpose solve A^H X = B reusing the resident factors. */
+int wt3d_solve_adjoint(wt3d_solver *h, int nrhs, const double _Complex *B, double _Complex *X,
+                       double tol, int maxit, double *relres, int *iters);
+
+/* Device-pointer solve: d_B, d_X device complex128, column-major n x nrhs. */
+int wt3d_solve_device(wt3d_solver *h, int nrhs, const void *d_B, void *d_X,
+                      double tol, int maxit, double *relres, int *iters, int adjoint);
+
+/* y = A x with the assembled complex128 operator (host arrays), for checks. */
+int wt3d_apply(wt3d_solver *h, int nrhs, const double _Complex *X, double _Complex *Y);
+
+/* Statistics of the last factorisation. */
+typedef struct wt3d_stats {
+    long long n, nnz;              /* unknowns, operator nonzeros             */
+    long long nfronts;             /* fronts in the elimination tree          */
+    long long factor_entries;      /* complex entries stored in the factors   */
+    double    factor_flops;        /* real-flop count, sum of 8(p^3/3+p^2 b+p b^2) */
+    double    factor_bytes;        /* bytes held by the factors on the device */
+    double    device_bytes;        /* total device bytes held by the handle   */
+    double    t_analyse_ms, t_assemble_ms, t_factor_ms, t_solve_ms; /* last calls */
+    int       perturbed_pivots;    /* pivots replaced by the static threshold */
+    int       levels;              /* depth of the elimination tree + 1       */
+} wt3d_stats;
+int wt3d_get_stats(const wt3d_solver *h, wt3d_stats *st);
+
+/* Host-only view of the analysis (nested dissection + symbolic
+ * factorisation; no GPU needed).  info[8] = {fronts, factor entries, levels,
+ * max pivots, max border, border entries, update buffer 0, update buffer 1};
+ * *flops = sum of 8(p^3/3 + p^2 b + p b^2).  leaf_nodes <= 0 selects 64. */
+int wt3d_analyse_info(int nx, int ny, int nz, int leaf_nodes, long long *info, double *flops);
+/* Export the elimination structure: perm[n] (new dof -> natural dof), per
+ * front p, b, first pivot, parent, depth, and the concatenated border dofs
+ * (new indices) and their positions in the parent front (rel). */
+int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *perm, int *fp, int *fb, int *ffirst,
+                        int *fparent, int *flevel, int *border, int *rel);
+
+/* Last error message of the calling thread (static storage). */
+const char *wt3d_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

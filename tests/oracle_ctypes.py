@@ -1,0 +1,77 @@
+"""ctypes binding of the CPU oracle (oracle/wt3d_oracle.c).
+
+Test infrastructure only: the checker the CUDA path is compared against.
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+class OGrid(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int), ("dx", ctypes.c_double),
+                ("pmld", ctypes.c_double), ("pmlr", ctypes.c_double), ("fst", ctypes.c_int),
+                ("usemin", ctypes.c_int)]
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Oracle:
+    def __init__(self):
+        from wtomo3d_gb300 import build
+        path = build.build_oracle()
+        L = ctypes.CDLL(path)
+        vp = ctypes.c_void_p
+        L.ora_srel3d_getsize.argtypes = [ctypes.c_int] * 3 + [ctypes.POINTER(ctypes.c_longlong)] * 2
+        L.ora_pattern.argtypes = [ctypes.c_int] * 3 + [vp, vp]
+        for f in (L.ora_assemble_c128, L.ora_assemble_c64):
+            f.argtypes = [ctypes.POINTER(OGrid), vp, vp, vp, ctypes.c_double, ctypes.c_double, vp, vp]
+        L.ora_node_blocks_c128.argtypes = [ctypes.POINTER(OGrid), vp, vp, vp, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp]
+        L.ora_spmv_c128.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp]
+        self.L = L
+
+    @staticmethod
+    def grid(g):
+        pmld = g.pmld if g.pmld > 0 else 10.0 * g.dx
+        pmlr = g.pmlr if g.pmlr > 0 else 1e-3
+        return OGrid(g.nx, g.ny, g.nz, g.dx, pmld, pmlr, g.fst, g.usemin)
+
+    def getsize(self, nx, ny, nz):
+        nv, ne = ctypes.c_longlong(), ctypes.c_longlong()
+        self.L.ora_srel3d_getsize(nx, ny, nz, ctypes.byref(nv), ctypes.byref(ne))
+        return nv.value, ne.value
+
+    def pattern(self, nx, ny, nz):
+        n, ne = self.getsize(nx, ny, nz)
+        ir = np.zeros(n + 1, np.int32)
+        jc = np.zeros(2 * ne + n, np.int32)
+        rc = self.L.ora_pattern(nx, ny, nz, _p(ir), _p(jc))
+        assert rc == 0
+        return ir, jc
+
+    def assemble(self, g, vp, vs, rho, omega, irptr, precision="c128"):
+        og = self.grid(g)
+        vp, vs, rho = [np.ascontiguousarray(np.asarray(x, np.float32).reshape(-1, order="F")) for x in (vp, vs, rho)]
+        dt = np.complex128 if precision == "c128" else np.complex64
+        a = np.zeros(irptr[-1] - 1, dt)
+        f = self.L.ora_assemble_c128 if precision == "c128" else self.L.ora_assemble_c64
+        om = complex(omega)
+        ierr = f(ctypes.byref(og), _p(vp), _p(vs), _p(rho), om.real, om.imag, _p(irptr), _p(a))
+        return a, ierr
+
+    def node_blocks(self, g, vp, vs, rho, omega, iz, ix, iy):
+        og = self.grid(g)
+        vp, vs, rho = [np.ascontiguousarray(np.asarray(x, np.float32).reshape(-1, order="F")) for x in (vp, vs, rho)]
+        blk = np.zeros(27 * 9, np.complex128)
+        act = np.zeros(27, np.int32)
+        om = complex(omega)
+        ierr = self.L.ora_node_blocks_c128(ctypes.byref(og), _p(vp), _p(vs), _p(rho), om.real, om.imag,
+                                           iz, ix, iy, _p(blk), _p(act))
+        return blk.reshape(27, 3, 3), act, ierr

@@ -1,0 +1,75 @@
+"""CPU tests of the C ABI: the library loads, exports every symbol the
+public header declares, and fails loudly (no CPU fallback) without a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import wtomo3d_gb300 as wt
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "wtomo3d_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_ ]*?[\s\*]+([A-Za-z_][A-Za-z0-9_]*)\s*\(", src, flags=re.M)
+    return sorted(set(n for n in names if n not in ("if", "while", "return")))
+
+
+def test_header_symbols_exported():
+    names = header_functions()
+    assert "strumpack_serial_finter" in names and "wt3d_solve" in names
+    L = wt.lib()
+    for n in names:
+        assert hasattr(L, n), "missing export: " + n
+
+
+def test_pattern_nnz_closed_form():
+    for dims in [(2, 2, 2), (40, 40, 40), (96, 96, 64), (128, 128, 96)]:
+        nx, ny, nz = dims
+        assert wt.lib().wt3d_pattern_nnz(nx, ny, nz) == 9 * (3 * nx - 2) * (3 * ny - 2) * (3 * nz - 2)
+    assert wt.lib().wt3d_pattern_nnz(40, 40, 40) == 14787288
+    assert wt.lib().wt3d_pattern_nnz(96, 96, 64) == 139871160
+    assert wt.lib().wt3d_pattern_nnz(128, 128, 96) == 375608376
+
+
+def _has_gpu():
+    import torch
+    return torch.cuda.is_available()
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-GPU error path")
+def test_no_gpu_fails_loudly():
+    g = wt.Grid(4, 4, 4, 10.0)
+    with pytest.raises(wt.WT3DError) as e:
+        wt.Solver(g)
+    assert e.value.code == wt.WT3D_ERR_NOGPU
+    with pytest.raises(wt.WT3DError):
+        wt.pattern(4, 4, 4)
+
+
+def test_job_protocol_order_errors():
+    """Out-of-order jobs report ierr = 1 like strumpack_finter.c:71-76,95-99."""
+    n, nnz = 24, 24 * 24
+    ir = np.zeros(n + 1, np.int32)
+    jc = np.zeros(nnz, np.int32)
+    a = np.zeros(nnz, np.complex64)
+    b = np.zeros(n, np.complex64)
+    x = np.zeros(n, np.complex64)
+    assert wt.strumpack_serial_finter(2, n, nnz, ir, jc, a, b, x) == 1
+    assert wt.strumpack_serial_finter(3, n, nnz, ir, jc, a, b, x) == 1
+    assert wt.strumpack_serial_finter(-1, n, nnz, ir, jc, a, b, x) == 0
+
+
+def test_job1_rejects_non_grid_pattern():
+    # a 1-based tridiagonal pattern is not the 27-point grid graph
+    n = 24
+    rows = [[j for j in (i - 1, i, i + 1) if 0 <= j < n] for i in range(n)]
+    ir = np.cumsum([1] + [len(r) for r in rows]).astype(np.int32)
+    jc = (np.concatenate(rows) + 1).astype(np.int32)
+    a = np.ones(len(jc), np.complex64)
+    b = np.zeros(n, np.complex64)
+    assert wt.strumpack_serial_finter(1, n, len(jc), ir, jc, a, b, b.copy()) == 1

@@ -1,0 +1,147 @@
+"""GPU multifrontal solver: parity with SuperLU (complex128) on operators the
+oracle assembles, the mixed-precision refinement reaching its tolerance, the
+FP64 path, the adjoint solve, many right-hand sides, and the
+strumpack_serial_finter job protocol."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+import wtomo3d_gb300 as wt
+from wtomo3d_gb300 import Grid, model
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_matrix(oracle, g, vp, vs, rho, om):
+    ir, jc = oracle.pattern(g.nx, g.ny, g.nz)
+    a, ierr = oracle.assemble(g, vp, vs, rho, om, ir)
+    assert ierr == 0
+    return sp.csr_matrix((a, jc - 1, ir - 1), shape=(g.n, g.n)), ir, jc, a
+
+
+def rand_rhs(n, k, seed=0):
+    r = np.random.default_rng(seed)
+    return r.standard_normal((n, k)) + 1j * r.standard_normal((n, k))
+
+
+@pytest.fixture(scope="module")
+def small_case(oracle):
+    g = Grid(14, 12, 13, 20.0, pmld=3 * 20.0, fst=1)
+    vp, vs, rho = model.layered_random(g.nx, g.ny, g.nz, g.dx, seed=1)
+    om = 2 * np.pi * 1.5
+    A, ir, jc, a = oracle_matrix(oracle, g, vp, vs, rho, om)
+    lu = spla.splu(A.tocsc())
+    return g, vp, vs, rho, om, A, lu
+
+
+@pytest.mark.parametrize("prec", [wt.PREC_MIXED, wt.PREC_FP64])
+def test_solve_matches_superlu(small_case, prec):
+    g, vp, vs, rho, om, A, lu = small_case
+    B = rand_rhs(g.n, 3)
+    with wt.Solver(g, prec) as s:
+        s.set_model(vp, vs, rho)
+        s.factor(om)
+        X = s.solve(B, tol=1e-10, maxit=30)
+        st = s.stats()
+    Xr = lu.solve(B)
+    err = np.linalg.norm(X - Xr) / np.linalg.norm(Xr)
+    res = np.linalg.norm(B - A @ X, axis=0) / np.linalg.norm(B, axis=0)
+    assert res.max() <= 1e-10, res
+    assert err <= 1e-8, err
+    assert st["perturbed_pivots"] == 0
+    if prec == wt.PREC_FP64:
+        assert err <= 1e-10
+
+
+def test_mixed_refinement_converges_in_few_steps(small_case):
+    g, vp, vs, rho, om, A, lu = small_case
+    B = rand_rhs(g.n, 8, seed=3)
+    with wt.Solver(g) as s:
+        s.set_model(vp, vs, rho)
+        s.factor(om)
+        X = s.solve(B, tol=1e-8, maxit=10)
+        assert s.last_iters <= 6
+        assert s.last_relres.max() <= 1e-8
+
+
+def test_many_rhs_batches(small_case):
+    g, vp, vs, rho, om, A, lu = small_case
+    B = rand_rhs(g.n, 70, seed=4)   # two passes of 64 + 6
+    with wt.Solver(g) as s:
+        s.set_model(vp, vs, rho)
+        s.factor(om)
+        X = s.solve(B, tol=1e-9)
+    Xr = lu.solve(B)
+    assert np.linalg.norm(X - Xr) / np.linalg.norm(Xr) <= 1e-7
+
+
+def test_adjoint_solve(small_case):
+    g, vp, vs, rho, om, A, lu = small_case
+    B = rand_rhs(g.n, 2, seed=5)
+    with wt.Solver(g) as s:
+        s.set_model(vp, vs, rho)
+        s.factor(om)
+        X = s.solve_adjoint(B, tol=1e-10, maxit=30)
+    AH = A.conj().T.tocsr()
+    res = np.linalg.norm(B - AH @ X, axis=0) / np.linalg.norm(B, axis=0)
+    assert res.max() <= 1e-10
+    Xr = spla.splu(AH.tocsc()).solve(B)
+    assert np.linalg.norm(X - Xr) / np.linalg.norm(Xr) <= 1e-8
+
+
+def test_apply_matches_oracle_operator(small_case):
+    g, vp, vs, rho, om, A, lu = small_case
+    X = rand_rhs(g.n, 2, seed=6)
+    with wt.Solver(g) as s:
+        s.set_model(vp, vs, rho)
+        s.factor(om)
+        Y = s.apply(X)
+    Yr = A @ X
+    assert np.abs(Y - Yr).max() <= 1e-11 * np.abs(Yr).max()
+
+
+def test_config1_point_force_small(oracle):
+    """Config 1 physics at reduced size: homogeneous, PML on all faces, vertical
+    point force at the centre node; mixed precision vs SuperLU."""
+    g = Grid(20, 20, 20, 25.0, pmld=5 * 25.0, fst=0)
+    vp, vs, rho = model.homogeneous(20, 20, 20)
+    A, ir, jc, a = oracle_matrix(oracle, g, vp, vs, rho, 2 * np.pi)
+    c = (g.nx - 1) * g.dx / 2
+    b = model.point_force(g.nx, g.ny, g.nz, g.dx, c, c, c, comp=2)
+    with wt.Solver(g) as s:
+        s.set_model(vp, vs, rho)
+        s.factor(2 * np.pi)
+        x = s.solve(b, tol=1e-10)
+    xr = spla.spsolve(A.tocsc(), b)
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) <= 1e-8
+
+
+def test_strumpack_job_protocol(oracle):
+    """Replays elwave.f90:141-190 (job 1, then 2 and 3 per frequency, then -1)
+    with complex64 operators assembled by the oracle in the reference's own
+    precision; irptr/jcptr are left unchanged."""
+    g = Grid(10, 9, 11, 20.0, pmld=3 * 20.0, fst=1)
+    vp, vs, rho = model.layered_random(g.nx, g.ny, g.nz, g.dx, seed=2)
+    ir, jc = oracle.pattern(g.nx, g.ny, g.nz)
+    ir0, jc0 = ir.copy(), jc.copy()
+    n, nnz = g.n, len(jc)
+    dummy = np.zeros(n, np.complex64)
+    a0 = np.zeros(nnz, np.complex64)
+    assert wt.strumpack_serial_finter(1, n, nnz, ir, jc, a0, dummy, dummy.copy()) == 0
+    assert wt.strumpack_serial_finter(1, n, nnz, ir, jc, a0, dummy, dummy.copy()) == 1   # already initialised
+    rng = np.random.default_rng(9)
+    for f in (0.5, 2.0):
+        a64, ierr = oracle.assemble(g, vp, vs, rho, 2 * np.pi * f, ir, "c64")
+        assert ierr == 0
+        assert wt.strumpack_serial_finter(2, n, nnz, ir, jc, a64, dummy, dummy.copy()) == 0
+        rhs = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+        sol = np.zeros(n, np.complex64)
+        assert wt.strumpack_serial_finter(3, n, nnz, ir, jc, a64, rhs, sol) == 0
+        A = sp.csr_matrix((a64.astype(np.complex128), jc - 1, ir - 1), shape=(n, n))
+        xr = spla.spsolve(A.tocsc(), rhs.astype(np.complex128))
+        err = np.linalg.norm(sol - xr) / np.linalg.norm(xr)
+        assert err <= 1e-6, err     # complex64 output, FP64-refined
+    assert wt.strumpack_serial_finter(-1, n, nnz, ir, jc, a0, dummy, dummy.copy()) == 0
+    np.testing.assert_array_equal(ir, ir0)
+    np.testing.assert_array_equal(jc, jc0)

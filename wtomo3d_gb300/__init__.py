@@ -1,0 +1,232 @@
+"""wtomo3d-gb300: GB300-native frequency-domain elastic forward modelling.
+
+Python mirror of the C ABI in include/wtomo3d_gpu.h.  The compute runs in
+libwtomo3d_gpu.so (hand-written CUDA for sm_103a); this module only marshals
+host arrays through ctypes.  There is no CPU fallback: if the library or a
+GPU is missing, every call raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libwtomo3d_gpu.so")
+
+WT3D_OK = 0
+WT3D_ERR_ARG = 1
+WT3D_ERR_CUDA = 2
+WT3D_ERR_NOMEM = 3
+WT3D_ERR_STATE = 4
+WT3D_ERR_PATTERN = 5
+WT3D_ERR_NOCONV = 6
+WT3D_ERR_NOGPU = 7
+
+PREC_MIXED = 0
+PREC_FP64 = 1
+
+
+class WT3DError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("wtomo3d error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Grid(ctypes.Structure):
+    """wt3d_grid: grid and boundary description (dx = dy = dz)."""
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("dx", ctypes.c_double), ("pmld", ctypes.c_double), ("pmlr", ctypes.c_double),
+                ("fst", ctypes.c_int), ("usemin", ctypes.c_int)]
+
+    def __init__(self, nx, ny, nz, dx, pmld=0.0, pmlr=0.0, fst=True, usemin=True):
+        super().__init__(nx, ny, nz, float(dx), float(pmld), float(pmlr), int(bool(fst)), int(bool(usemin)))
+
+    @property
+    def nnodes(self):
+        return self.nx * self.ny * self.nz
+
+    @property
+    def n(self):
+        return 3 * self.nnodes
+
+    @property
+    def nnz(self):
+        return 9 * (3 * self.nx - 2) * (3 * self.ny - 2) * (3 * self.nz - 2)
+
+    def pml(self):
+        """(pmld, pmlf, ipml) as readini.f90:81-84 computes them (in double)."""
+        pmld = self.pmld if self.pmld > 0 else 10.0 * self.dx
+        pmlr = self.pmlr if self.pmlr > 0 else 1e-3
+        ipml = int(pmld / self.dx) + 1
+        pmlf = 3.0 * np.log(1.0 / pmlr) / (2.0 * pmld ** 3)
+        return pmld, pmlf, ipml
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_longlong), ("nnz", ctypes.c_longlong), ("nfronts", ctypes.c_longlong),
+                ("factor_entries", ctypes.c_longlong), ("factor_flops", ctypes.c_double),
+                ("factor_bytes", ctypes.c_double), ("device_bytes", ctypes.c_double),
+                ("t_analyse_ms", ctypes.c_double), ("t_assemble_ms", ctypes.c_double),
+                ("t_factor_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double),
+                ("perturbed_pivots", ctypes.c_int), ("levels", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    """Load libwtomo3d_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libwtomo3d_gpu.so is not built: run `python -c \"import __graft_entry__ as g; "
+                               "g.build()\"` (no CPU fallback exists)")
+        L = ctypes.CDLL(LIB_PATH)
+        vp = ctypes.c_void_p
+        L.wt3d_last_error.restype = ctypes.c_char_p
+        L.wt3d_pattern_nnz.restype = ctypes.c_longlong
+        L.wt3d_pattern_nnz.argtypes = [ctypes.c_int] * 3
+        L.wt3d_pattern.argtypes = [ctypes.c_int] * 4 + [vp, vp]
+        L.wt3d_assemble.argtypes = [ctypes.POINTER(Grid), vp, vp, vp, ctypes.c_double, ctypes.c_double, vp]
+        L.wt3d_solver_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(Grid), ctypes.c_int]
+        L.wt3d_solver_destroy.argtypes = [vp]
+        L.wt3d_set_model.argtypes = [vp, vp, vp, vp]
+        L.wt3d_factor.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+        L.wt3d_set_values_c64.argtypes = [vp, vp]
+        L.wt3d_factor_values.argtypes = [vp]
+        for f in (L.wt3d_solve, L.wt3d_solve_adjoint):
+            f.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_double, ctypes.c_int, vp, vp]
+        L.wt3d_solve_device.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_double, ctypes.c_int, vp, vp,
+                                        ctypes.c_int]
+        L.wt3d_apply.argtypes = [vp, ctypes.c_int, vp, vp]
+        L.wt3d_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.strumpack_serial_finter.argtypes = [ip, ip, ip, vp, vp, vp, vp, vp, ip]
+        L.strumpack_serial_finter.restype = None
+        _lib = L
+    return _lib
+
+
+def _check(rc, allow=()):
+    if rc != WT3D_OK and rc not in allow:
+        raise WT3DError(rc, lib().wt3d_last_error().decode())
+    return rc
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _f32(a, n):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, order="F"))
+    if a.size != n:
+        raise ValueError("model array has %d entries, expected %d" % (a.size, n))
+    return a
+
+
+def pattern(nx, ny, nz, base=1):
+    """CSR pattern of the 27-point 3-dof grid graph (srel3d + SPARSE_ADJ2CRS)."""
+    n = 3 * nx * ny * nz
+    nnz = lib().wt3d_pattern_nnz(nx, ny, nz)
+    irptr = np.empty(n + 1, np.int32)
+    jcptr = np.empty(nnz, np.int32)
+    _check(lib().wt3d_pattern(nx, ny, nz, base, _ptr(irptr), _ptr(jcptr)))
+    return irptr, jcptr
+
+
+def assemble(grid, vp, vs, rho, omega):
+    """Complex128 CSR values of A(omega) in the order of pattern() (ASMBLE)."""
+    n = grid.nnodes
+    vp, vs, rho = _f32(vp, n), _f32(vs, n), _f32(rho, n)
+    a = np.empty(grid.nnz, np.complex128)
+    om = complex(omega)
+    _check(lib().wt3d_assemble(ctypes.byref(grid), _ptr(vp), _ptr(vs), _ptr(rho), om.real, om.imag, _ptr(a)))
+    return a
+
+
+class Solver:
+    """Handle-based multifrontal solver on one GPU (wt3d_solver_*)."""
+
+    def __init__(self, grid, precision=PREC_MIXED):
+        self.grid = grid
+        self.precision = precision
+        self._h = ctypes.c_void_p()
+        _check(lib().wt3d_solver_create(ctypes.byref(self._h), ctypes.byref(grid), precision))
+
+    def close(self):
+        if self._h:
+            lib().wt3d_solver_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_model(self, vp, vs, rho):
+        n = self.grid.nnodes
+        self._model = (_f32(vp, n), _f32(vs, n), _f32(rho, n))
+        _check(lib().wt3d_set_model(self._h, *[_ptr(a) for a in self._model]))
+
+    def factor(self, omega):
+        om = complex(omega)
+        _check(lib().wt3d_factor(self._h, om.real, om.imag))
+
+    def set_values(self, a_c64):
+        a = np.ascontiguousarray(a_c64, dtype=np.complex64)
+        _check(lib().wt3d_set_values_c64(self._h, _ptr(a)))
+        _check(lib().wt3d_factor_values(self._h))
+
+    def _solve(self, fn, B, tol, maxit, allow_noconv):
+        B = np.asarray(B, dtype=np.complex128)
+        one = B.ndim == 1
+        Bf = np.asfortranarray(B.reshape(self.grid.n, -1))
+        nrhs = Bf.shape[1]
+        X = np.empty_like(Bf, order="F")
+        relres = np.zeros(nrhs)
+        iters = ctypes.c_int(0)
+        rc = fn(self._h, nrhs, _ptr(Bf), _ptr(X), tol, maxit, _ptr(relres), ctypes.byref(iters))
+        _check(rc, allow=(WT3D_ERR_NOCONV,) if allow_noconv else ())
+        self.last_relres, self.last_iters = relres, iters.value
+        return X[:, 0] if one else X
+
+    def solve(self, B, tol=1e-8, maxit=20, allow_noconv=False):
+        """X = A^-1 B with FP64 refinement to ||b - A x|| / ||b|| <= tol."""
+        return self._solve(lib().wt3d_solve, B, tol, maxit, allow_noconv)
+
+    def solve_adjoint(self, B, tol=1e-8, maxit=20, allow_noconv=False):
+        """X = A^-H B reusing the resident factors."""
+        return self._solve(lib().wt3d_solve_adjoint, B, tol, maxit, allow_noconv)
+
+    def apply(self, X):
+        X = np.asarray(X, dtype=np.complex128)
+        one = X.ndim == 1
+        Xf = np.asfortranarray(X.reshape(self.grid.n, -1))
+        Y = np.empty_like(Xf, order="F")
+        _check(lib().wt3d_apply(self._h, Xf.shape[1], _ptr(Xf), _ptr(Y)))
+        return Y[:, 0] if one else Y
+
+    def stats(self):
+        s = Stats()
+        _check(lib().wt3d_get_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+
+def strumpack_serial_finter(job, nrows, nnz, irptr, jcptr, a, rhs, sol):
+    """Call the drop-in job-protocol entry point exactly as the Fortran driver
+    does (by reference, 1-based CSR, complex64).  Returns ierr."""
+    c = ctypes.c_int
+    ierr = c(0)
+    lib().strumpack_serial_finter(ctypes.byref(c(job)), ctypes.byref(c(nrows)), ctypes.byref(c(nnz)),
+                                  _ptr(irptr), _ptr(jcptr), _ptr(a), _ptr(rhs), _ptr(sol), ctypes.byref(ierr))
+    return ierr.value

@@ -1,0 +1,631 @@
+// C ABI of libwtomo3d_gpu: the drop-in strumpack_serial_finter job protocol,
+// the handle-based wt3d_* solver, and the FP64 iterative refinement that wraps
+// the complex64 multifrontal factorisation.
+#include "engine.cuh"
+#include "wtomo3d_gpu.h"
+#include <chrono>
+#include <complex>
+#include <cstring>
+#include <mutex>
+
+namespace wt3d {
+
+static thread_local std::string g_err;
+void set_error(const std::string &msg) { g_err = msg; }
+
+// ---------------------------------------------------------------------------
+// FP64 refinement kernels (natural ordering, row-major n x MAXRHS complex128)
+// ---------------------------------------------------------------------------
+__global__ void k_cm_to_rm(long long n, int m, const double2 *__restrict__ cm, double2 *__restrict__ rm)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int j = 0; j < m; j++) rm[i * MAXRHS + j] = cm[(long long)j * n + i];
+}
+
+__global__ void k_rm_to_cm(long long n, int m, const double2 *__restrict__ rm, double2 *__restrict__ cm)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int j = 0; j < m; j++) cm[(long long)j * n + i] = rm[i * MAXRHS + j];
+}
+
+// R = B - op(A) X (op = A or A^H), per-column squared norms of R into nr and of B into nb.
+__global__ void __launch_bounds__(256) k_residual(long long n, int m, const int *__restrict__ irptr,
+                                                  const int *__restrict__ jcptr, const double2 *__restrict__ a,
+                                                  const int *__restrict__ tpos, const double2 *__restrict__ X,
+                                                  const double2 *__restrict__ B, double2 *__restrict__ R,
+                                                  double *__restrict__ nr, double *__restrict__ nb, int adjoint)
+{
+    const int lane = threadIdx.x & 31;
+    const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    double sr0 = 0, sr1 = 0, sb0 = 0, sb1 = 0;
+    const int j0 = lane, j1 = lane + 32;
+    for (long long i = w0; i < n; i += nw) {
+        double2 acc0 = make_double2(0, 0), acc1 = make_double2(0, 0);
+        for (int k = irptr[i]; k < irptr[i + 1]; k++) {
+            double2 av;
+            if (adjoint) { av = a[tpos[k]]; av.y = -av.y; }
+            else av = a[k];
+            const double2 *xr = X + (long long)jcptr[k] * MAXRHS;
+            if (j0 < m) {
+                double2 x = xr[j0];
+                acc0.x += av.x * x.x - av.y * x.y;
+                acc0.y += av.x * x.y + av.y * x.x;
+            }
+            if (j1 < m) {
+                double2 x = xr[j1];
+                acc1.x += av.x * x.x - av.y * x.y;
+                acc1.y += av.x * x.y + av.y * x.x;
+            }
+        }
+        if (j0 < m) {
+            double2 b = B[i * MAXRHS + j0];
+            double2 r = make_double2(b.x - acc0.x, b.y - acc0.y);
+            R[i * MAXRHS + j0] = r;
+            sr0 += r.x * r.x + r.y * r.y;
+            sb0 += b.x * b.x + b.y * b.y;
+        }
+        if (j1 < m) {
+            double2 b = B[i * MAXRHS + j1];
+            double2 r = make_double2(b.x - acc1.x, b.y - acc1.y);
+            R[i * MAXRHS + j1] = r;
+            sr1 += r.x * r.x + r.y * r.y;
+            sb1 += b.x * b.x + b.y * b.y;
+        }
+    }
+    if (j0 < m) { atomicAdd(&nr[j0], sr0); atomicAdd(&nb[j0], sb0); }
+    if (j1 < m) { atomicAdd(&nr[j1], sr1); atomicAdd(&nb[j1], sb1); }
+}
+
+template <class T>
+__global__ void k_gather_new(long long n, int m, const int *__restrict__ perm, const double2 *__restrict__ R,
+                             cx<T> *__restrict__ Xs)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n * m) return;
+    long long i = q / m;
+    int j = (int)(q % m);
+    double2 v = R[(long long)perm[i] * MAXRHS + j];
+    Xs[i * MAXRHS + j] = cx<T>((T)v.x, (T)v.y);
+}
+
+template <class T>
+__global__ void k_scatter_add_nat(long long n, int m, const int *__restrict__ perm, const cx<T> *__restrict__ Xs,
+                                  double2 *__restrict__ Xn)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n * m) return;
+    long long i = q / m;
+    int j = (int)(q % m);
+    cx<T> v = Xs[i * MAXRHS + j];
+    double2 *d = Xn + (long long)perm[i] * MAXRHS + j;
+    d->x += (double)v.re;
+    d->y += (double)v.im;
+}
+
+__global__ void k_c64_to_c128(long long n, const float2 *__restrict__ s, double2 *__restrict__ d)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = make_double2(s[i].x, s[i].y);
+}
+
+}  // namespace wt3d
+
+using namespace wt3d;
+
+struct wt3d_solver {
+    wt3d_grid grid{};
+    int prec = WT3D_PREC_MIXED;
+    Symbolic sym;
+    long long n = 0, nnz = 0;
+    DevVec<int> irptr, jcptr, tpos, perm;
+    DevVec<double2> a;
+    DevVec<double2> da, mu;
+    DevVec<double> ro;
+    DevVec<float> vp, vs, rho;
+    DevVec<double2> Bn, Xn, Rn, T1;
+    DevVec<double> norms;
+    std::unique_ptr<Engine<float>> e32;
+    std::unique_ptr<Engine<double>> e64;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool have_model = false, have_values = false, have_factor = false;
+    wt3d_stats stats{};
+    ~wt3d_solver()
+    {
+        if (st) cudaStreamSynchronize(st);
+        e32.reset();
+        e64.reset();
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+namespace {
+
+double ms_between(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+int check_grid(const wt3d_grid *g)
+{
+    if (!g || g->nx < 2 || g->ny < 2 || g->nz < 2 || !(g->dx > 0)) {
+        set_error("invalid grid: need nx, ny, nz >= 2 and dx > 0");
+        return WT3D_ERR_ARG;
+    }
+    long long nnz = wt3d_pattern_nnz(g->nx, g->ny, g->nz);
+    if (nnz >= (1LL << 31)) {
+        set_error("grid too large: nnz >= 2^31");
+        return WT3D_ERR_ARG;
+    }
+    return WT3D_OK;
+}
+
+int have_gpu()
+{
+    int nd = 0;
+    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) {
+        set_error("no CUDA device available");
+        return WT3D_ERR_NOGPU;
+    }
+    return WT3D_OK;
+}
+
+// Refinement driver over m <= MAXRHS columns held in h->Bn; result in h->Xn.
+template <class T>
+int refine(wt3d_solver *h, Engine<T> &E, int m, bool adjoint, double tol, int maxit, double *relres, int *iters)
+{
+    cudaStream_t st = h->st;
+    const long long n = h->n;
+    Schedule<T> *sc = E.solve_schedule(m, adjoint);
+    if (!sc) return WT3D_ERR_NOMEM;
+    WT_CUDA(cudaMemsetAsync(h->Xn.p, 0, sizeof(double2) * n * MAXRHS, st));
+    // start from R = B
+    WT_CUDA(cudaMemcpyAsync(h->Rn.p, h->Bn.p, sizeof(double2) * n * MAXRHS, cudaMemcpyDeviceToDevice, st));
+    std::vector<double> hn(2 * MAXRHS);
+    int it = 0, rc = WT3D_OK;
+    const int th = 256;
+    const unsigned nb = (unsigned)ceil_div(n * m, th);
+    for (;;) {
+        k_gather_new<T><<<nb, th, 0, st>>>(n, m, h->perm.p, h->Rn.p, E.X.p);
+        rc = E.run(*sc, st);
+        if (rc) return rc;
+        k_scatter_add_nat<T><<<nb, th, 0, st>>>(n, m, h->perm.p, E.X.p, h->Xn.p);
+        WT_CUDA(cudaMemsetAsync(h->norms.p, 0, sizeof(double) * 2 * MAXRHS, st));
+        k_residual<<<152 * 8, 256, 0, st>>>(n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, h->Xn.p, h->Bn.p,
+                                            h->Rn.p, h->norms.p, h->norms.p + MAXRHS, adjoint ? 1 : 0);
+        WT_CUDA(cudaGetLastError());
+        WT_CUDA(cudaMemcpyAsync(hn.data(), h->norms.p, sizeof(double) * 2 * MAXRHS, cudaMemcpyDeviceToHost, st));
+        WT_CUDA(cudaStreamSynchronize(st));
+        double worst = 0;
+        for (int j = 0; j < m; j++) {
+            double r = hn[MAXRHS + j] > 0 ? sqrt(hn[j] / hn[MAXRHS + j]) : sqrt(hn[j]);
+            if (relres) relres[j] = r;
+            worst = std::max(worst, r);
+        }
+        if (!(worst == worst)) { rc = WT3D_ERR_NOCONV; break; }   // NaN
+        if (worst <= tol) break;
+        if (it >= maxit) { rc = WT3D_ERR_NOCONV; break; }
+        it++;
+    }
+    if (iters) *iters = it;
+    if (rc == WT3D_ERR_NOCONV) set_error("iterative refinement did not reach the requested tolerance");
+    return rc;
+}
+
+int solve_dev_cm(wt3d_solver *h, int nrhs, const double2 *d_B, double2 *d_X, double tol, int maxit, double *relres,
+                 int *iters, bool adjoint)
+{
+    if (!h->have_factor) { set_error("solve before factor"); return WT3D_ERR_STATE; }
+    const long long n = h->n;
+    int worst_rc = WT3D_OK, maxits = 0;
+    cudaEventRecord(h->ev0, h->st);
+    for (int c0 = 0; c0 < nrhs; c0 += MAXRHS) {
+        int m = std::min(MAXRHS, nrhs - c0);
+        k_cm_to_rm<<<ceil_div(n, 256), 256, 0, h->st>>>(n, m, d_B + (long long)c0 * n, h->Bn.p);
+        int its = 0, rc;
+        if (h->e32) rc = refine<float>(h, *h->e32, m, adjoint, tol, maxit, relres ? relres + c0 : nullptr, &its);
+        else rc = refine<double>(h, *h->e64, m, adjoint, tol, maxit, relres ? relres + c0 : nullptr, &its);
+        if (rc && rc != WT3D_ERR_NOCONV) return rc;
+        if (rc) worst_rc = rc;
+        maxits = std::max(maxits, its);
+        k_rm_to_cm<<<ceil_div(n, 256), 256, 0, h->st>>>(n, m, h->Xn.p, d_X + (long long)c0 * n);
+    }
+    cudaEventRecord(h->ev1, h->st);
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    h->stats.t_solve_ms = ms_between(h->ev0, h->ev1);
+    if (iters) *iters = maxits;
+    return worst_rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *wt3d_last_error(void) { return g_err.c_str(); }
+
+long long wt3d_pattern_nnz(int nx, int ny, int nz)
+{
+    return 9LL * (3LL * nx - 2) * (3LL * ny - 2) * (3LL * nz - 2);
+}
+
+int wt3d_pattern(int nx, int ny, int nz, int base, int *irptr, int *jcptr)
+{
+    if (nx < 2 || ny < 2 || nz < 2 || (base != 0 && base != 1) || !irptr || !jcptr) {
+        set_error("wt3d_pattern: invalid arguments");
+        return WT3D_ERR_ARG;
+    }
+    int rc = have_gpu();
+    if (rc) return rc;
+    long long nnz = wt3d_pattern_nnz(nx, ny, nz);
+    long long n = 3LL * nx * ny * nz;
+    int *di = nullptr, *dj = nullptr;
+    WT_CUDA(cudaMalloc(&di, sizeof(int) * (n + 1)));
+    if (cudaMalloc(&dj, sizeof(int) * nnz) != cudaSuccess) { cudaFree(di); set_error("cudaMalloc"); return WT3D_ERR_NOMEM; }
+    rc = device_pattern(nx, ny, nz, base, di, dj, 0);
+    if (!rc && (cudaMemcpy(irptr, di, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost) != cudaSuccess ||
+                cudaMemcpy(jcptr, dj, sizeof(int) * nnz, cudaMemcpyDeviceToHost) != cudaSuccess)) {
+        set_error("wt3d_pattern: copy back failed");
+        rc = WT3D_ERR_CUDA;
+    }
+    cudaFree(di);
+    cudaFree(dj);
+    return rc;
+}
+
+int wt3d_assemble_device(const wt3d_grid *g, const float *d_vp, const float *d_vs, const float *d_rho,
+                         double omega_re, double omega_im, const int *d_irptr, void *d_a, void *stream)
+{
+    int rc = check_grid(g);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    long long nn = (long long)g->nx * g->ny * g->nz;
+    void *da = nullptr, *mu = nullptr;
+    double *ro = nullptr;
+    WT_CUDA(cudaMallocAsync(&da, sizeof(double2) * nn, st));
+    WT_CUDA(cudaMallocAsync(&mu, sizeof(double2) * nn, st));
+    WT_CUDA(cudaMallocAsync(&ro, sizeof(double) * nn, st));
+    rc = device_lame(nn, d_vp, d_vs, d_rho, da, mu, ro, st);
+    if (!rc) rc = device_assemble(*g, da, mu, ro, omega_re, omega_im, d_irptr, d_a, st);
+    cudaFreeAsync(da, st);
+    cudaFreeAsync(mu, st);
+    cudaFreeAsync(ro, st);
+    return rc;
+}
+
+int wt3d_assemble(const wt3d_grid *g, const float *vp, const float *vs, const float *rho, double omega_re,
+                  double omega_im, double _Complex *a)
+{
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if ((rc = have_gpu())) return rc;
+    if (!vp || !vs || !rho || !a) { set_error("wt3d_assemble: null pointer"); return WT3D_ERR_ARG; }
+    long long nn = (long long)g->nx * g->ny * g->nz, n = 3 * nn, nnz = wt3d_pattern_nnz(g->nx, g->ny, g->nz);
+    DevVec<float> dvp, dvs, drho;
+    DevVec<int> di, dj;
+    DevVec<double2> da;
+    if ((rc = dvp.alloc(nn)) || (rc = dvs.alloc(nn)) || (rc = drho.alloc(nn)) || (rc = di.alloc(n + 1)) ||
+        (rc = dj.alloc(nnz)) || (rc = da.alloc(nnz)))
+        return rc;
+    WT_CUDA(cudaMemcpy(dvp.p, vp, sizeof(float) * nn, cudaMemcpyHostToDevice));
+    WT_CUDA(cudaMemcpy(dvs.p, vs, sizeof(float) * nn, cudaMemcpyHostToDevice));
+    WT_CUDA(cudaMemcpy(drho.p, rho, sizeof(float) * nn, cudaMemcpyHostToDevice));
+    if ((rc = device_pattern(g->nx, g->ny, g->nz, 0, di.p, dj.p, 0))) return rc;
+    if ((rc = wt3d_assemble_device(g, dvp.p, dvs.p, drho.p, omega_re, omega_im, di.p, da.p, nullptr))) return rc;
+    WT_CUDA(cudaMemcpy(a, da.p, sizeof(double2) * nnz, cudaMemcpyDeviceToHost));
+    return WT3D_OK;
+}
+
+// -------------------------------------------------------------------------
+int wt3d_solver_create(wt3d_solver **out, const wt3d_grid *g, int precision)
+{
+    if (!out) { set_error("null handle pointer"); return WT3D_ERR_ARG; }
+    *out = nullptr;
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (precision != WT3D_PREC_MIXED && precision != WT3D_PREC_FP64) { set_error("bad precision"); return WT3D_ERR_ARG; }
+    if ((rc = have_gpu())) return rc;
+    auto t0 = std::chrono::steady_clock::now();
+    std::unique_ptr<wt3d_solver> h(new wt3d_solver());
+    h->grid = *g;
+    h->prec = precision;
+    if ((rc = symbolic_grid(g->nx, g->ny, g->nz, 64, h->sym))) return rc;
+    h->n = h->sym.n;
+    h->nnz = wt3d_pattern_nnz(g->nx, g->ny, g->nz);
+    WT_CUDA(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    WT_CUDA(cudaEventCreate(&h->ev0));
+    WT_CUDA(cudaEventCreate(&h->ev1));
+    if ((rc = h->irptr.alloc(h->n + 1)) || (rc = h->jcptr.alloc(h->nnz)) || (rc = h->a.alloc(h->nnz))) return rc;
+    if ((rc = device_pattern(g->nx, g->ny, g->nz, 0, h->irptr.p, h->jcptr.p, h->st))) return rc;
+    std::vector<int> hir(h->n + 1), hjc(h->nnz);
+    WT_CUDA(cudaMemcpyAsync(hir.data(), h->irptr.p, sizeof(int) * (h->n + 1), cudaMemcpyDeviceToHost, h->st));
+    WT_CUDA(cudaMemcpyAsync(hjc.data(), h->jcptr.p, sizeof(int) * h->nnz, cudaMemcpyDeviceToHost, h->st));
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    std::vector<long long> map;
+    if ((rc = scatter_map(h->sym, hir, hjc, map))) return rc;
+    {
+        // transposed positions for the adjoint residual
+        std::vector<int> tp(h->nnz), cur(hir.begin(), hir.end() - 1);
+        for (long long r = 0; r < h->n; r++)
+            for (long long k = hir[r]; k < hir[r + 1]; k++) tp[k] = cur[hjc[k]]++;
+        if ((rc = h->tpos.upload(tp))) return rc;
+    }
+    if ((rc = h->perm.upload(h->sym.perm))) return rc;
+    if ((rc = h->Bn.alloc((size_t)h->n * MAXRHS)) || (rc = h->Xn.alloc((size_t)h->n * MAXRHS)) ||
+        (rc = h->Rn.alloc((size_t)h->n * MAXRHS)) || (rc = h->norms.alloc(2 * MAXRHS)))
+        return rc;
+    if (precision == WT3D_PREC_MIXED) {
+        h->e32.reset(new Engine<float>());
+        rc = h->e32->init(h->sym, map);
+    } else {
+        h->e64.reset(new Engine<double>());
+        rc = h->e64->init(h->sym, map);
+    }
+    if (rc) return rc;
+    auto t1 = std::chrono::steady_clock::now();
+    h->stats.n = h->n;
+    h->stats.nnz = h->nnz;
+    h->stats.nfronts = (long long)h->sym.fronts.size();
+    h->stats.factor_entries = h->sym.fac_total;
+    h->stats.factor_flops = h->sym.flops;
+    h->stats.factor_bytes = (double)h->sym.fac_total * (precision == WT3D_PREC_MIXED ? 8.0 : 16.0);
+    h->stats.levels = (int)h->sym.levels.size();
+    h->stats.t_analyse_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    *out = h.release();
+    return WT3D_OK;
+}
+
+int wt3d_solver_destroy(wt3d_solver *h)
+{
+    delete h;
+    return WT3D_OK;
+}
+
+int wt3d_set_model(wt3d_solver *h, const float *vp, const float *vs, const float *rho)
+{
+    if (!h || !vp || !vs || !rho) { set_error("wt3d_set_model: null pointer"); return WT3D_ERR_ARG; }
+    long long nn = h->n / 3;
+    int rc;
+    if (!h->vp.p) {
+        if ((rc = h->vp.alloc(nn)) || (rc = h->vs.alloc(nn)) || (rc = h->rho.alloc(nn)) || (rc = h->da.alloc(nn)) ||
+            (rc = h->mu.alloc(nn)) || (rc = h->ro.alloc(nn)))
+            return rc;
+    }
+    WT_CUDA(cudaMemcpyAsync(h->vp.p, vp, sizeof(float) * nn, cudaMemcpyHostToDevice, h->st));
+    WT_CUDA(cudaMemcpyAsync(h->vs.p, vs, sizeof(float) * nn, cudaMemcpyHostToDevice, h->st));
+    WT_CUDA(cudaMemcpyAsync(h->rho.p, rho, sizeof(float) * nn, cudaMemcpyHostToDevice, h->st));
+    if ((rc = device_lame(nn, h->vp.p, h->vs.p, h->rho.p, h->da.p, h->mu.p, h->ro.p, h->st))) return rc;
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    h->have_model = true;
+    return WT3D_OK;
+}
+
+static int factor_values(wt3d_solver *h)
+{
+    int np = 0, rc;
+    cudaEventRecord(h->ev0, h->st);
+    if (h->e32) rc = h->e32->factor(h->a.p, h->nnz, h->st, &np);
+    else rc = h->e64->factor(h->a.p, h->nnz, h->st, &np);
+    if (rc) return rc;
+    cudaEventRecord(h->ev1, h->st);
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    h->stats.t_factor_ms = ms_between(h->ev0, h->ev1);
+    h->stats.perturbed_pivots = np;
+    h->stats.device_bytes = (double)(h->e32 ? h->e32->device_bytes() : h->e64->device_bytes()) +
+                            (double)h->nnz * (16 + 4 + 4) + (double)h->n * MAXRHS * 16 * 3;
+    h->have_factor = true;
+    return WT3D_OK;
+}
+
+int wt3d_factor(wt3d_solver *h, double omega_re, double omega_im)
+{
+    if (!h) { set_error("null handle"); return WT3D_ERR_ARG; }
+    if (!h->have_model) { set_error("wt3d_factor: no model set"); return WT3D_ERR_STATE; }
+    h->have_factor = false;
+    cudaEventRecord(h->ev0, h->st);
+    int rc = device_assemble(h->grid, h->da.p, h->mu.p, h->ro.p, omega_re, omega_im, h->irptr.p, h->a.p, h->st);
+    if (rc) return rc;
+    cudaEventRecord(h->ev1, h->st);
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    h->stats.t_assemble_ms = ms_between(h->ev0, h->ev1);
+    h->have_values = true;
+    return factor_values(h);
+}
+
+int wt3d_set_values_c64(wt3d_solver *h, const float _Complex *a)
+{
+    if (!h || !a) { set_error("null pointer"); return WT3D_ERR_ARG; }
+    DevVec<float2> tmp;
+    int rc = tmp.alloc(h->nnz);
+    if (rc) return rc;
+    WT_CUDA(cudaMemcpyAsync(tmp.p, a, sizeof(float2) * h->nnz, cudaMemcpyHostToDevice, h->st));
+    k_c64_to_c128<<<ceil_div(h->nnz, 256), 256, 0, h->st>>>(h->nnz, tmp.p, h->a.p);
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    h->have_values = true;
+    h->have_factor = false;
+    return WT3D_OK;
+}
+
+int wt3d_factor_values(wt3d_solver *h)
+{
+    if (!h || !h->have_values) { set_error("no operator values"); return WT3D_ERR_STATE; }
+    return factor_values(h);
+}
+
+int wt3d_solve_device(wt3d_solver *h, int nrhs, const void *d_B, void *d_X, double tol, int maxit, double *relres,
+                      int *iters, int adjoint)
+{
+    if (!h || nrhs < 1 || !d_B || !d_X) { set_error("wt3d_solve_device: bad arguments"); return WT3D_ERR_ARG; }
+    return solve_dev_cm(h, nrhs, (const double2 *)d_B, (double2 *)d_X, tol, maxit, relres, iters, adjoint != 0);
+}
+
+static int solve_host(wt3d_solver *h, int nrhs, const double _Complex *B, double _Complex *X, double tol, int maxit,
+                      double *relres, int *iters, bool adjoint)
+{
+    if (!h || nrhs < 1 || !B || !X) { set_error("wt3d_solve: bad arguments"); return WT3D_ERR_ARG; }
+    if (!h->have_factor) { set_error("solve before factor"); return WT3D_ERR_STATE; }
+    DevVec<double2> dB, dX;
+    int rc;
+    if ((rc = dB.alloc((size_t)h->n * nrhs)) || (rc = dX.alloc((size_t)h->n * nrhs))) return rc;
+    WT_CUDA(cudaMemcpyAsync(dB.p, B, sizeof(double2) * h->n * nrhs, cudaMemcpyHostToDevice, h->st));
+    rc = solve_dev_cm(h, nrhs, dB.p, dX.p, tol, maxit, relres, iters, adjoint);
+    if (rc && rc != WT3D_ERR_NOCONV) return rc;
+    WT_CUDA(cudaMemcpy(X, dX.p, sizeof(double2) * h->n * nrhs, cudaMemcpyDeviceToHost));
+    return rc;
+}
+
+int wt3d_solve(wt3d_solver *h, int nrhs, const double _Complex *B, double _Complex *X, double tol, int maxit,
+               double *relres, int *iters)
+{
+    return solve_host(h, nrhs, B, X, tol, maxit, relres, iters, false);
+}
+
+int wt3d_solve_adjoint(wt3d_solver *h, int nrhs, const double _Complex *B, double _Complex *X, double tol, int maxit,
+                       double *relres, int *iters)
+{
+    return solve_host(h, nrhs, B, X, tol, maxit, relres, iters, true);
+}
+
+int wt3d_apply(wt3d_solver *h, int nrhs, const double _Complex *X, double _Complex *Y)
+{
+    if (!h || nrhs < 1 || !X || !Y) { set_error("wt3d_apply: bad arguments"); return WT3D_ERR_ARG; }
+    if (!h->have_values) { set_error("no operator"); return WT3D_ERR_STATE; }
+    const long long n = h->n;
+    DevVec<double2> dX;
+    int rc = dX.alloc((size_t)n * nrhs);
+    if (rc) return rc;
+    WT_CUDA(cudaMemcpyAsync(dX.p, X, sizeof(double2) * n * nrhs, cudaMemcpyHostToDevice, h->st));
+    for (int c0 = 0; c0 < nrhs; c0 += MAXRHS) {
+        int m = std::min(MAXRHS, nrhs - c0);
+        k_cm_to_rm<<<ceil_div(n, 256), 256, 0, h->st>>>(n, m, dX.p + (long long)c0 * n, h->Xn.p);
+        WT_CUDA(cudaMemsetAsync(h->Bn.p, 0, sizeof(double2) * n * MAXRHS, h->st));
+        WT_CUDA(cudaMemsetAsync(h->norms.p, 0, sizeof(double) * 2 * MAXRHS, h->st));
+        // R = 0 - A X
+        k_residual<<<152 * 8, 256, 0, h->st>>>(n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, h->Xn.p, h->Bn.p,
+                                               h->Rn.p, h->norms.p, h->norms.p + MAXRHS, 0);
+        k_rm_to_cm<<<ceil_div(n, 256), 256, 0, h->st>>>(n, m, h->Rn.p, dX.p + (long long)c0 * n);
+    }
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    std::vector<std::complex<double>> tmp((size_t)n * nrhs);
+    WT_CUDA(cudaMemcpy(tmp.data(), dX.p, sizeof(double2) * n * nrhs, cudaMemcpyDeviceToHost));
+    std::complex<double> *Yc = reinterpret_cast<std::complex<double> *>(Y);
+    for (size_t i = 0; i < tmp.size(); i++) Yc[i] = -tmp[i];
+    return WT3D_OK;
+}
+
+int wt3d_get_stats(const wt3d_solver *h, wt3d_stats *st)
+{
+    if (!h || !st) return WT3D_ERR_ARG;
+    *st = h->stats;
+    return WT3D_OK;
+}
+
+// -------------------------------------------------------------------------
+// strumpack_serial_finter drop-in (strumpack_finter.c:9-121)
+// -------------------------------------------------------------------------
+static wt3d_solver *g_sp = nullptr;
+static bool g_sp_factored = false;
+static std::mutex g_sp_mu;
+
+void strumpack_serial_finter(int *job, int *nrows, int *nnz, int *irptr, int *jcptr, float _Complex *a,
+                             float _Complex *rhs, float _Complex *sol, int *ierr)
+{
+    const char *fcnm = "strumpack_serial_finter";
+    std::lock_guard<std::mutex> lock(g_sp_mu);
+    *ierr = 0;
+    if (*job == 1) {
+        if (g_sp) { printf("%s: Error already initialized!\n", fcnm); *ierr = 1; return; }
+        int nx, ny, nz;
+        if (detect_grid(*nrows, *nnz, irptr, jcptr, nx, ny, nz) != WT3D_OK) {
+            printf("%s: Error reordering matrix!\n", fcnm);
+            set_error("CSR pattern is not the 27-point 3-dof grid graph");
+            *ierr = 1;
+            return;
+        }
+        wt3d_grid g{nx, ny, nz, 1.0, 0.0, 0.0, 1, 1};
+        if (wt3d_solver_create(&g_sp, &g, WT3D_PREC_MIXED) != WT3D_OK) {
+            printf("%s: Error reordering matrix! (%s)\n", fcnm, g_err.c_str());
+            g_sp = nullptr;
+            *ierr = 1;
+        }
+        g_sp_factored = false;
+    } else if (*job == 2) {
+        g_sp_factored = false;
+        if (!g_sp) { printf("%s: Error not initialized!\n", fcnm); *ierr = 1; return; }
+        if (wt3d_set_values_c64(g_sp, a) != WT3D_OK || wt3d_factor_values(g_sp) != WT3D_OK) {
+            printf("%s: Error factoring matrix! (%s)\n", fcnm, g_err.c_str());
+            *ierr = 1;
+            return;
+        }
+        g_sp_factored = true;
+    } else if (*job == 3) {
+        if (!g_sp || !g_sp_factored) { printf("%s: Error matrix not factorized!\n", fcnm); *ierr = 1; return; }
+        const long long n = g_sp->n;
+        std::vector<std::complex<double>> b(n), x(n);
+        const std::complex<float> *r = reinterpret_cast<const std::complex<float> *>(rhs);
+        for (long long i = 0; i < n; i++) b[i] = std::complex<double>(r[i]);
+        double rr = 0;
+        int rc = wt3d_solve(g_sp, 1, reinterpret_cast<double _Complex *>(b.data()),
+                            reinterpret_cast<double _Complex *>(x.data()), 1e-10, 20, &rr, nullptr);
+        if (rc != WT3D_OK && rc != WT3D_ERR_NOCONV) {
+            printf("%s: Error in solution phase1\n", fcnm);
+            *ierr = 1;
+            return;
+        }
+        std::complex<float> *s = reinterpret_cast<std::complex<float> *>(sol);
+        for (long long i = 0; i < n; i++) s[i] = std::complex<float>(x[i]);
+    } else if (*job == -1) {
+        if (g_sp) wt3d_solver_destroy(g_sp);
+        g_sp = nullptr;
+        g_sp_factored = false;
+    }
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// host-only inspection of the analysis (no GPU needed)
+// ---------------------------------------------------------------------------
+extern "C" int wt3d_analyse_info(int nx, int ny, int nz, int leaf_nodes, long long *info, double *flops)
+{
+    Symbolic S;
+    int rc = symbolic_grid(nx, ny, nz, leaf_nodes > 0 ? leaf_nodes : 64, S);
+    if (rc) return rc;
+    if (info) {
+        info[0] = (long long)S.fronts.size();
+        info[1] = S.fac_total;
+        info[2] = (long long)S.levels.size();
+        info[3] = S.max_p;
+        info[4] = S.max_b;
+        info[5] = (long long)S.border.size();
+        info[6] = S.upd_size[0];
+        info[7] = S.upd_size[1];
+    }
+    if (flops) *flops = S.flops;
+    return WT3D_OK;
+}
+
+extern "C" int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *perm, int *fp, int *fb, int *ffirst,
+                                   int *fparent, int *flevel, int *border, int *rel)
+{
+    Symbolic S;
+    int rc = symbolic_grid(nx, ny, nz, leaf_nodes > 0 ? leaf_nodes : 64, S);
+    if (rc) return rc;
+    std::copy(S.perm.begin(), S.perm.end(), perm);
+    for (size_t f = 0; f < S.fronts.size(); f++) {
+        fp[f] = S.fronts[f].p;
+        fb[f] = S.fronts[f].b;
+        ffirst[f] = S.fronts[f].first;
+        fparent[f] = S.fronts[f].parent;
+        flevel[f] = S.fronts[f].level;
+    }
+    std::copy(S.border.begin(), S.border.end(), border);
+    std::copy(S.rel.begin(), S.rel.end(), rel);
+    return WT3D_OK;
+}

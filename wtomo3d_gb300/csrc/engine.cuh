@@ -1,0 +1,446 @@
+// Multifrontal engine: device storage of the fronts, the static launch
+// schedule of the factorisation and of the solves, and their execution.
+#pragma once
+#include "internal.h"
+#include "mf_kernels.cuh"
+#include <functional>
+#include <map>
+#include <memory>
+
+namespace wt3d {
+
+template <class T>
+struct DevVec {
+    T *p = nullptr;
+    size_t n = 0;
+    int alloc(size_t count)
+    {
+        free();
+        if (count == 0) return WT3D_OK;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            set_error(std::string("cudaMalloc(") + std::to_string(count * sizeof(T)) + " B): " + cudaGetErrorString(e));
+            return WT3D_ERR_NOMEM;
+        }
+        n = count;
+        return WT3D_OK;
+    }
+    int upload(const std::vector<T> &v)
+    {
+        int rc = alloc(v.size());
+        if (rc) return rc;
+        if (!v.empty() && cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) {
+            set_error("upload failed");
+            return WT3D_ERR_CUDA;
+        }
+        return WT3D_OK;
+    }
+    void free()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DevVec() { free(); }
+    DevVec() = default;
+    DevVec(const DevVec &) = delete;
+    DevVec &operator=(const DevVec &) = delete;
+};
+
+using Launch = std::function<void(cudaStream_t)>;
+
+// A list of launches plus the task arrays they read.
+template <class T>
+struct Schedule {
+    std::vector<Launch> launches;
+    DevVec<PanelTask> panel;
+    DevVec<RowTask> row;
+    DevVec<ColTask> col;
+    DevVec<GemmTask<T>> gemm;
+    DevVec<EATask> ea;
+    cudaGraphExec_t graph = nullptr;
+    ~Schedule()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+    }
+};
+
+template <class T>
+class Engine {
+public:
+    const Symbolic *S = nullptr;
+    DevVec<cx<T>> fac, upd0, upd1, X;
+    DevVec<int> ipiv, border;
+    DevVec<int> rel;
+    DevVec<FrontDev> fr;
+    DevVec<long long> map;
+    DevVec<int> npert;
+    DevVec<unsigned long long> maxabs;
+    std::unique_ptr<Schedule<T>> fsched;
+    std::map<int, std::unique_ptr<Schedule<T>>> ssched[2];   // [adjoint][m]
+    double pivot_rel = 1e-7;
+    bool use_graphs = true;
+
+    size_t device_bytes() const
+    {
+        return fac.n * sizeof(cx<T>) + (upd0.n + upd1.n + X.n) * sizeof(cx<T>) + (ipiv.n + border.n + rel.n) * 4 +
+               fr.n * sizeof(FrontDev) + map.n * 8;
+    }
+
+    int init(const Symbolic &sym, const std::vector<long long> &hmap)
+    {
+        S = &sym;
+        int rc;
+        if ((rc = fac.alloc(sym.fac_total))) return rc;
+        if ((rc = upd0.alloc(std::max<long long>(sym.upd_size[0], 1)))) return rc;
+        if ((rc = upd1.alloc(std::max<long long>(sym.upd_size[1], 1)))) return rc;
+        if ((rc = X.alloc((size_t)sym.n * MAXRHS))) return rc;
+        if ((rc = ipiv.alloc(sym.n))) return rc;
+        if ((rc = border.upload(sym.border))) return rc;
+        if ((rc = rel.upload(sym.rel))) return rc;
+        if ((rc = map.upload(hmap))) return rc;
+        if ((rc = npert.alloc(1))) return rc;
+        if ((rc = maxabs.alloc(1))) return rc;
+        std::vector<FrontDev> h(sym.fronts.size());
+        for (size_t f = 0; f < h.size(); f++) {
+            const Front &F = sym.fronts[f];
+            h[f].fac = F.fac_off;
+            h[f].upd = F.upd_off;
+            h[f].border = F.border_off;
+            h[f].p = F.p;
+            h[f].b = F.b;
+            h[f].first = F.first;
+            h[f].parity = F.level & 1;
+        }
+        if ((rc = fr.upload(h))) return rc;
+        static bool attr_done = false;
+        if (!attr_done) {
+            size_t sp = sizeof(cx<T>) * KB * (KB + 1);
+            cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp);
+            cudaFuncSetAttribute(k_trsm_row<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (TRW + 1))));
+            cudaFuncSetAttribute(k_trsm_col<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1))));
+            cudaFuncSetAttribute(k_diag_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1))));
+            attr_done = true;
+        }
+        return build_factor_schedule();
+    }
+
+    // ---------------------------------------------------------------------
+    static void add_gemm(std::vector<GemmTask<T>> &v, long long &tiles, const cx<T> *A, int lda, const cx<T> *B,
+                         int ldb, cx<T> *C, int ldc, int M, int N, int K, const int *brow = nullptr,
+                         const int *crow = nullptr, int conjA = 0)
+    {
+        if (M <= 0 || N <= 0 || K <= 0) return;
+        GemmTask<T> g;
+        g.A = A; g.B = B; g.C = C; g.brow = brow; g.crow = crow;
+        g.lda = lda; g.ldb = ldb; g.ldc = ldc; g.M = M; g.N = N; g.K = K;
+        g.tiles_n = (N + GBN - 1) / GBN;
+        g.tile0 = tiles;
+        g.conjA = conjA;
+        tiles += (long long)((M + GBM - 1) / GBM) * g.tiles_n;
+        v.push_back(g);
+    }
+
+    // Appends a gemm launch over tasks [b, e) with local tile numbering.
+    static void push_gemm_launch(Schedule<T> &sc, std::vector<GemmTask<T>> &all, size_t b, long long tiles)
+    {
+        if (all.size() == b) return;
+        // rebase tile0 to the launch
+        long long t0 = all[b].tile0;
+        for (size_t i = b; i < all.size(); i++) all[i].tile0 -= t0;
+        int nt = (int)(all.size() - b);
+        long long ntiles = tiles - t0;
+        Schedule<T> *psc = &sc;
+        sc.launches.push_back([psc, b, nt, ntiles](cudaStream_t st) {
+            k_gemm<T><<<(unsigned)ntiles, 256, 0, st>>>(psc->gemm.p + b, nt);
+        });
+    }
+
+    int build_factor_schedule()
+    {
+        auto sc = std::make_unique<Schedule<T>>();
+        std::vector<PanelTask> hp;
+        std::vector<RowTask> hr;
+        std::vector<ColTask> hc;
+        std::vector<GemmTask<T>> hg;
+        std::vector<EATask> he;
+        Schedule<T> *psc = sc.get();
+        const Symbolic &sym = *S;
+        cx<T> *F = fac.p;
+        cx<T> *U[2] = {upd0.p, upd1.p};
+        const long long nnz = (long long)map.n;
+        // zero the factor pool, scatter the operator
+        {
+            cx<T> *fp = F; size_t bytes = fac.n * sizeof(cx<T>);
+            long long *mp = map.p;
+            Engine<T> *self = this;
+            sc->launches.push_back([fp, bytes](cudaStream_t st) { cudaMemsetAsync(fp, 0, bytes, st); });
+            sc->launches.push_back([self, mp, nnz, fp](cudaStream_t st) {
+                k_scatter<T><<<ceil_div(nnz, 256), 256, 0, st>>>(nnz, mp, self->a_dev, fp);
+            });
+        }
+        const int nlev = (int)sym.levels.size();
+        for (int L = nlev - 1; L >= 0; L--) {
+            const std::vector<int> &fl = sym.levels[L];
+            // zero this level's update region
+            long long usz = 0;
+            for (int f : fl) usz += (long long)sym.fronts[f].b * sym.fronts[f].b;
+            if (usz > 0) {
+                cx<T> *up = U[L & 1];
+                size_t bytes = usz * sizeof(cx<T>);
+                sc->launches.push_back([up, bytes](cudaStream_t st) { cudaMemsetAsync(up, 0, bytes, st); });
+            }
+            // extend-add, one child slot at a time (siblings overlap in the parent)
+            for (int slot = 0; slot < 2; slot++) {
+                size_t b0 = he.size();
+                long long rows = 0;
+                for (int f : fl) {
+                    const Front &P = sym.fronts[f];
+                    if (P.nchild <= slot) continue;
+                    int c = P.child[slot];
+                    if (sym.fronts[c].b == 0) continue;
+                    he.push_back(EATask{c, f, rows});
+                    rows += sym.fronts[c].b;
+                }
+                if (he.size() > b0) {
+                    int nt = (int)(he.size() - b0);
+                    sc->launches.push_back([psc, this, b0, nt, rows](cudaStream_t st) {
+                        k_extend_add<T><<<ceil_div(rows * 32, 256), 256, 0, st>>>(
+                            psc->ea.p + b0, nt, rows, fr.p, rel.p, fac.p, upd0.p, upd1.p);
+                    });
+                }
+            }
+            // blocked partial LU, level-synchronous over fronts
+            int maxp = 0;
+            for (int f : fl) maxp = std::max(maxp, sym.fronts[f].p);
+            for (int k = 0; k < maxp; k += KB) {
+                size_t p0 = hp.size(), r0 = hr.size(), c0 = hc.size(), g0 = hg.size();
+                long long tiles = 0;
+                for (int f : fl) {
+                    const Front &Fr = sym.fronts[f];
+                    if (Fr.p <= k) continue;
+                    const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k), k2 = k + kb;
+                    hp.push_back(PanelTask{f, k});
+                    for (int c = k2; c < nf; c += TRW) hr.push_back(RowTask{f, k, c});
+                    for (int r = k2; r < Fr.p; r += TCR) hc.push_back(ColTask{f, k, r, 0});
+                    for (int r = 0; r < Fr.b; r += TCR) hc.push_back(ColTask{f, k, r, 1});
+                    cx<T> *Pb = F + Fr.fac_off;
+                    cx<T> *Lo = Pb + (long long)Fr.p * nf;
+                    add_gemm(hg, tiles, Pb + (long long)k2 * nf + k, nf, Pb + (long long)k * nf + k2, nf,
+                             Pb + (long long)k2 * nf + k2, nf, Fr.p - k2, nf - k2, kb);
+                    add_gemm(hg, tiles, Lo + k, Fr.p, Pb + (long long)k * nf + k2, nf, Lo + k2, Fr.p, Fr.b,
+                             Fr.p - k2, kb);
+                }
+                int np = (int)(hp.size() - p0), nr = (int)(hr.size() - r0), ncl = (int)(hc.size() - c0);
+                size_t smp = sizeof(cx<T>) * KB * (KB + 1);
+                size_t smr = sizeof(cx<T>) * (KB * (KB + 1) + KB * (TRW + 1));
+                size_t smc = sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1));
+                sc->launches.push_back([psc, this, p0, np, smp](cudaStream_t st) {
+                    k_panel<T><<<np, 256, smp, st>>>(psc->panel.p + p0, fr.p, fac.p, ipiv.p, maxabs.p, pivot_rel, npert.p);
+                });
+                if (nr)
+                    sc->launches.push_back([psc, this, r0, nr, smr](cudaStream_t st) {
+                        k_trsm_row<T><<<nr, TRW, smr, st>>>(psc->row.p + r0, fr.p, fac.p, ipiv.p);
+                    });
+                if (ncl)
+                    sc->launches.push_back([psc, this, c0, ncl, smc](cudaStream_t st) {
+                        k_trsm_col<T><<<ncl, TCR, smc, st>>>(psc->col.p + c0, fr.p, fac.p);
+                    });
+                push_gemm_launch(*sc, hg, g0, tiles);
+            }
+            // Schur complement F22 -= L21 U12 (K = p)
+            {
+                size_t g0 = hg.size();
+                long long tiles = 0;
+                for (int f : fl) {
+                    const Front &Fr = sym.fronts[f];
+                    if (Fr.b == 0) continue;
+                    const int nf = Fr.nf();
+                    cx<T> *Pb = F + Fr.fac_off;
+                    cx<T> *Lo = Pb + (long long)Fr.p * nf;
+                    add_gemm(hg, tiles, Lo, Fr.p, Pb + Fr.p, nf, U[L & 1] + Fr.upd_off, Fr.b, Fr.b, Fr.b, Fr.p);
+                }
+                push_gemm_launch(*sc, hg, g0, tiles);
+            }
+        }
+        int rc;
+        if ((rc = sc->panel.upload(hp))) return rc;
+        if ((rc = sc->row.upload(hr))) return rc;
+        if ((rc = sc->col.upload(hc))) return rc;
+        if ((rc = sc->gemm.upload(hg))) return rc;
+        if ((rc = sc->ea.upload(he))) return rc;
+        fsched = std::move(sc);
+        return WT3D_OK;
+    }
+
+    // Solve schedule for m right-hand sides in X (new ordering, row-major n x MAXRHS).
+    Schedule<T> *solve_schedule(int m, bool adjoint)
+    {
+        auto it = ssched[adjoint].find(m);
+        if (it != ssched[adjoint].end()) return it->second.get();
+        auto sc = std::make_unique<Schedule<T>>();
+        Schedule<T> *psc = sc.get();
+        std::vector<PanelTask> hp;
+        std::vector<GemmTask<T>> hg;
+        const Symbolic &sym = *S;
+        cx<T> *F = fac.p;
+        cx<T> *Xp = X.p;
+        const int ldx = MAXRHS;
+        const int nlev = (int)sym.levels.size();
+        size_t smd = sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1));
+        auto diag_launch = [&](size_t p0, int mode) {
+            int np = (int)(hp.size() - p0);
+            if (!np) return;
+            sc->launches.push_back([psc, this, p0, np, smd, m, mode, Xp, ldx](cudaStream_t st) {
+                k_diag_solve<T><<<np, MAXRHS, smd, st>>>(psc->panel.p + p0, fr.p, fac.p, ipiv.p, Xp, ldx, m, mode);
+            });
+        };
+        // ---- forward sweep: leaves to root ----
+        for (int L = nlev - 1; L >= 0; L--) {
+            const std::vector<int> &fl = sym.levels[L];
+            int maxp = 0;
+            for (int f : fl) maxp = std::max(maxp, sym.fronts[f].p);
+            for (int k = 0; k < maxp; k += KB) {
+                size_t p0 = hp.size(), g0 = hg.size();
+                long long tiles = 0;
+                for (int f : fl) {
+                    const Front &Fr = sym.fronts[f];
+                    if (Fr.p <= k) continue;
+                    const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k), k2 = k + kb;
+                    hp.push_back(PanelTask{f, k});
+                    cx<T> *Pb = F + Fr.fac_off;
+                    cx<T> *Y = Xp + (long long)Fr.first * ldx;
+                    if (!adjoint)   // Y[k2:p] -= L[k2:p, k:k2] Y[k:k2]
+                        add_gemm(hg, tiles, Pb + (long long)k2 * nf + k, nf, Y + (long long)k * ldx, ldx,
+                                 Y + (long long)k2 * ldx, ldx, Fr.p - k2, m, kb);
+                    else            // Y[k2:p] -= U[k:k2, k2:p]^H Y[k:k2]
+                        add_gemm(hg, tiles, Pb + (long long)k * nf + k2, nf, Y + (long long)k * ldx, ldx,
+                                 Y + (long long)k2 * ldx, ldx, Fr.p - k2, m, kb, nullptr, nullptr, 1);
+                }
+                diag_launch(p0, adjoint ? 2 : 0);
+                push_gemm_launch(*sc, hg, g0, tiles);
+            }
+            // border update  X[border] -= L21 Y   (adjoint: U12^H Y)
+            size_t g0 = hg.size();
+            long long tiles = 0;
+            for (int f : fl) {
+                const Front &Fr = sym.fronts[f];
+                if (Fr.b == 0) continue;
+                const int nf = Fr.nf();
+                cx<T> *Pb = F + Fr.fac_off;
+                cx<T> *Lo = Pb + (long long)Fr.p * nf;
+                cx<T> *Y = Xp + (long long)Fr.first * ldx;
+                const int *crow = border.p + Fr.border_off;
+                if (!adjoint) add_gemm(hg, tiles, Lo, Fr.p, Y, ldx, Xp, ldx, Fr.b, m, Fr.p, nullptr, crow, 0);
+                else add_gemm(hg, tiles, Pb + Fr.p, nf, Y, ldx, Xp, ldx, Fr.b, m, Fr.p, nullptr, crow, 1);
+            }
+            push_gemm_launch(*sc, hg, g0, tiles);
+        }
+        // ---- backward sweep: root to leaves ----
+        for (int L = 0; L < nlev; L++) {
+            const std::vector<int> &fl = sym.levels[L];
+            size_t g0 = hg.size();
+            long long tiles = 0;
+            int maxsteps = 0;
+            for (int f : fl) {
+                const Front &Fr = sym.fronts[f];
+                maxsteps = std::max(maxsteps, (Fr.p + KB - 1) / KB);
+                if (Fr.b == 0) continue;
+                const int nf = Fr.nf();
+                cx<T> *Pb = F + Fr.fac_off;
+                cx<T> *Lo = Pb + (long long)Fr.p * nf;
+                cx<T> *Y = Xp + (long long)Fr.first * ldx;
+                const int *brow = border.p + Fr.border_off;
+                if (!adjoint)   // Y -= U12 X[border]
+                    add_gemm(hg, tiles, Pb + Fr.p, nf, Xp, ldx, Y, ldx, Fr.p, m, Fr.b, brow, nullptr, 0);
+                else            // Y -= L21^H X[border]
+                    add_gemm(hg, tiles, Lo, Fr.p, Xp, ldx, Y, ldx, Fr.p, m, Fr.b, brow, nullptr, 1);
+            }
+            push_gemm_launch(*sc, hg, g0, tiles);
+            for (int s = maxsteps - 1; s >= 0; s--) {
+                const int k = s * KB;
+                size_t p0 = hp.size(), g1 = hg.size();
+                long long t1 = 0;
+                for (int f : fl) {
+                    const Front &Fr = sym.fronts[f];
+                    if (Fr.p <= k) continue;
+                    const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k), k2 = k + kb;
+                    cx<T> *Pb = F + Fr.fac_off;
+                    cx<T> *Y = Xp + (long long)Fr.first * ldx;
+                    hp.push_back(PanelTask{f, k});
+                    if (adjoint)   // Y[k:k2] -= L[k2:p, k:k2]^H Y[k2:p]   (before the diagonal solve)
+                        add_gemm(hg, t1, Pb + (long long)k2 * nf + k, nf, Y + (long long)k2 * ldx, ldx,
+                                 Y + (long long)k * ldx, ldx, kb, m, Fr.p - k2, nullptr, nullptr, 1);
+                }
+                if (!adjoint) {
+                    diag_launch(p0, 1);
+                    // Y[0:k] -= U[0:k, k:k2] Y[k:k2]
+                    for (int f : fl) {
+                        const Front &Fr = sym.fronts[f];
+                        if (Fr.p <= k || k == 0) continue;
+                        const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k);
+                        cx<T> *Pb = F + Fr.fac_off;
+                        cx<T> *Y = Xp + (long long)Fr.first * ldx;
+                        add_gemm(hg, t1, Pb + k, nf, Y + (long long)k * ldx, ldx, Y, ldx, k, m, kb);
+                    }
+                    push_gemm_launch(*sc, hg, g1, t1);
+                } else {
+                    push_gemm_launch(*sc, hg, g1, t1);
+                    diag_launch(p0, 3);
+                }
+            }
+        }
+        if (sc->panel.upload(hp) || sc->gemm.upload(hg)) return nullptr;
+        Schedule<T> *ret = sc.get();
+        ssched[adjoint][m] = std::move(sc);
+        return ret;
+    }
+
+    const double2 *a_dev = nullptr;   // complex128 operator values (set before factor)
+
+    int run(Schedule<T> &sc, cudaStream_t st)
+    {
+        if (use_graphs) {
+            if (!sc.graph) {
+                cudaGraph_t g;
+                WT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                for (auto &l : sc.launches) l(st);
+                WT_CUDA(cudaStreamEndCapture(st, &g));
+                cudaError_t e = cudaGraphInstantiate(&sc.graph, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+                    sc.graph = nullptr;
+                    return WT3D_ERR_CUDA;
+                }
+            }
+            WT_CUDA(cudaGraphLaunch(sc.graph, st));
+        } else {
+            for (auto &l : sc.launches) l(st);
+        }
+        WT_CUDA(cudaGetLastError());
+        return WT3D_OK;
+    }
+
+    int factor(const double2 *d_a, long long nnz, cudaStream_t st, int *h_npert)
+    {
+        if (d_a != a_dev && fsched->graph) { cudaGraphExecDestroy(fsched->graph); fsched->graph = nullptr; }
+        a_dev = d_a;
+        WT_CUDA(cudaMemsetAsync(maxabs.p, 0, sizeof(unsigned long long), st));
+        k_maxabs<<<1216, 256, 0, st>>>(nnz, d_a, maxabs.p);
+        WT_CUDA(cudaMemsetAsync(npert.p, 0, sizeof(int), st));
+        int rc = run(*fsched, st);
+        if (rc) return rc;
+        if (h_npert) {
+            WT_CUDA(cudaMemcpyAsync(h_npert, npert.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        }
+        return WT3D_OK;
+    }
+
+};
+
+}  // namespace wt3d

@@ -1,0 +1,470 @@
+// Multifrontal numeric kernels (templated on the real type T: float for the
+// complex64 mixed-precision path, double for the complex128 oracle path).
+//
+// Front layout (row-major): the pivot rows P = F[0:p, 0:nf] (p x nf) are
+// followed by the lower-left border block Lo = F[p:nf, 0:p] (b x p) in the
+// factor pool; the Schur/update block F22 (b x b) lives in one of two
+// level-parity update buffers.  Factorisation is right-looking blocked LU on
+// the first p columns with KB-wide panels and partial pivoting restricted to
+// the diagonal KB x KB tile; row interchanges are LINPACK style (applied to
+// the columns right of the panel only), so the forward solve applies them
+// block by block.
+#pragma once
+#include "common.cuh"
+
+namespace wt3d {
+
+constexpr int KB = 64;        // panel width
+constexpr int MAXRHS = 64;    // right-hand sides per solve pass
+
+struct FrontDev {
+    long long fac;     // P block offset in the factor pool (complex elements)
+    long long upd;     // F22 offset in its parity buffer
+    long long border;  // offset into the border index array
+    int p, b, first, parity;
+};
+
+struct PanelTask { int f, k; };
+struct RowTask { int f, k, c0; };
+struct ColTask { int f, k, r0, which; };
+struct EATask { int child, parent; long long row0; };
+
+template <class T>
+struct GemmTask {
+    const cx<T> *A;
+    const cx<T> *B;
+    cx<T> *C;
+    const int *brow;   // optional row gather for B
+    const int *crow;   // optional row scatter for C (atomic)
+    int lda, ldb, ldc, M, N, K;
+    int tiles_n;
+    long long tile0;
+    int conjA;         // use conj(A^T): A is read as its conjugate transpose
+};
+
+template <class T>
+__device__ __forceinline__ void atomic_sub(cx<T> *p, cx<T> v)
+{
+    atomicAdd(&p->re, -v.re);
+    atomicAdd(&p->im, -v.im);
+}
+
+template <class Task>
+__device__ __forceinline__ int find_task(const Task *tasks, int ntasks, long long key)
+{
+    int lo = 0, hi = ntasks - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].tile0 <= key) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// original entries -> fronts
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_scatter(long long nnz, const long long *__restrict__ map, const double2 *__restrict__ a,
+                          cx<T> *__restrict__ fac)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnz) return;
+    double2 v = a[k];
+    fac[map[k]] = cx<T>((T)v.x, (T)v.y);
+}
+
+__global__ void k_maxabs(long long n, const double2 *__restrict__ a, unsigned long long *out)
+{
+    double m = 0;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        double2 v = a[k];
+        m = fmax(m, v.x * v.x + v.y * v.y);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// ---------------------------------------------------------------------------
+// extend-add: child update matrix into the parent front (one warp per row)
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_extend_add(const EATask *__restrict__ tasks, int ntasks, long long nrows,
+                             const FrontDev *__restrict__ fr, const int *__restrict__ rel, cx<T> *__restrict__ fac,
+                             cx<T> *__restrict__ upd0, cx<T> *__restrict__ upd1)
+{
+    long long gr = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (gr >= nrows) return;
+    int lo = 0, hi = ntasks - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].row0 <= gr) lo = mid;
+        else hi = mid - 1;
+    }
+    const EATask t = tasks[lo];
+    const FrontDev C = fr[t.child], P = fr[t.parent];
+    const int i = (int)(gr - t.row0);
+    const int *rl = rel + C.border;   // rel shares the border indexing
+    const cx<T> *src = (C.parity ? upd1 : upd0) + C.upd + (long long)i * C.b;
+    const int R = rl[i];
+    const int nfP = P.p + P.b;
+    cx<T> *pf = fac + P.fac;
+    cx<T> *p22 = (P.parity ? upd1 : upd0) + P.upd;
+    for (int j = lane; j < C.b; j += 32) {
+        const int Cc = rl[j];
+        cx<T> v = src[j];
+        cx<T> *dst;
+        if (R < P.p) dst = pf + (long long)R * nfP + Cc;
+        else if (Cc < P.p) dst = pf + (long long)P.p * nfP + (long long)(R - P.p) * P.p + Cc;
+        else dst = p22 + (long long)(R - P.p) * P.b + (Cc - P.p);
+        *dst = *dst + v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// panel: LU of the KB x KB diagonal tile with partial pivoting inside the tile
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
+                                               cx<T> *__restrict__ fac, int *__restrict__ ipiv,
+                                               const unsigned long long *__restrict__ amax2, double pivot_rel,
+                                               int *__restrict__ npert)
+{
+    // static-pivot threshold: pivot_rel * max |a_ij| of the assembled operator
+    const T thresh = (T)(pivot_rel * sqrt(__longlong_as_double((long long)*amax2)));
+    extern __shared__ __align__(16) unsigned char smraw[];
+    cx<T> *S = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1)
+    __shared__ int s_piv;
+    const PanelTask t = tasks[blockIdx.x];
+    const FrontDev F = fr[t.f];
+    const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
+    const int LD = KB + 1;
+    cx<T> *D = fac + F.fac + (long long)k * nf + k;
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < kb * kb; idx += blockDim.x) {
+        int i = idx / kb, j = idx % kb;
+        S[i * LD + j] = D[(long long)i * nf + j];
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; j++) {
+        if (tid < 32) {
+            T best = -1; int bi = j;
+            for (int i = j + tid; i < kb; i += 32) {
+                T v = cabs2(S[i * LD + j]);
+                if (v > best) { best = v; bi = i; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                T ov = __shfl_xor_sync(0xffffffffu, best, o);
+                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+            }
+            if (tid == 0) s_piv = bi;
+        }
+        __syncthreads();
+        const int pv = s_piv;
+        if (pv != j)
+            for (int c = tid; c < kb; c += blockDim.x) {
+                cx<T> a = S[j * LD + c];
+                S[j * LD + c] = S[pv * LD + c];
+                S[pv * LD + c] = a;
+            }
+        __syncthreads();
+        if (tid == 0) {
+            ipiv[F.first + k + j] = k + pv;
+            cx<T> d = S[j * LD + j];
+            T m2 = cabs2(d);
+            if (!(m2 >= thresh * thresh)) {   // also catches NaN
+                T m = sqrt(m2);
+                S[j * LD + j] = (m > 0 && m == m) ? d * (thresh / m) : cx<T>(thresh);
+                atomicAdd(npert, 1);
+            }
+        }
+        __syncthreads();
+        const cx<T> d = S[j * LD + j];
+        const cx<T> inv = cdiv(cx<T>(1), d);
+        for (int i = j + 1 + tid; i < kb; i += blockDim.x) S[i * LD + j] = S[i * LD + j] * inv;
+        __syncthreads();
+        const int rem = kb - j - 1;
+        for (int idx = tid; idx < rem * rem; idx += blockDim.x) {
+            int i = j + 1 + idx / rem, c = j + 1 + idx % rem;
+            S[i * LD + c] = S[i * LD + c] - S[i * LD + j] * S[j * LD + c];
+        }
+        __syncthreads();
+    }
+    for (int idx = tid; idx < kb * kb; idx += blockDim.x) {
+        int i = idx / kb, j = idx % kb;
+        D[(long long)i * nf + j] = S[i * LD + j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// row band right of the panel: swap rows, then L_D^{-1} (unit lower)
+// ---------------------------------------------------------------------------
+constexpr int TRW = 128;   // columns per CTA
+template <class T>
+__global__ void __launch_bounds__(TRW) k_trsm_row(const RowTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
+                                                  cx<T> *__restrict__ fac, const int *__restrict__ ipiv)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    cx<T> *L = reinterpret_cast<cx<T> *>(smraw);          // KB x (KB+1)
+    cx<T> *Bt = L + KB * (KB + 1);                       // KB x (TRW+1)
+    __shared__ int idx[KB];
+    const RowTask t = tasks[blockIdx.x];
+    const FrontDev F = fr[t.f];
+    const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
+    const int c0 = t.c0, nc = min(TRW, nf - c0);
+    const int tid = threadIdx.x;
+    cx<T> *base = fac + F.fac + (long long)k * nf;
+    for (int q = tid; q < kb * kb; q += blockDim.x) {
+        int i = q / kb, j = q % kb;
+        L[i * (KB + 1) + j] = base[(long long)i * nf + k + j];
+    }
+    if (tid == 0) {
+        for (int i = 0; i < kb; i++) idx[i] = i;
+        for (int j = 0; j < kb; j++) {
+            int pv = ipiv[F.first + k + j] - k;
+            int a = idx[j]; idx[j] = idx[pv]; idx[pv] = a;
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < kb * nc; q += blockDim.x) {
+        int i = q / nc, c = q % nc;
+        Bt[i * (TRW + 1) + c] = base[(long long)idx[i] * nf + c0 + c];
+    }
+    __syncthreads();
+    if (tid < nc) {
+        for (int i = 1; i < kb; i++) {
+            cx<T> s = Bt[i * (TRW + 1) + tid];
+            for (int l = 0; l < i; l++) s = s - L[i * (KB + 1) + l] * Bt[l * (TRW + 1) + tid];
+            Bt[i * (TRW + 1) + tid] = s;
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < kb * nc; q += blockDim.x) {
+        int i = q / nc, c = q % nc;
+        base[(long long)i * nf + c0 + c] = Bt[i * (TRW + 1) + c];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// column band below the panel: X <- X U_D^{-1}
+// ---------------------------------------------------------------------------
+constexpr int TCR = 128;   // rows per CTA
+template <class T>
+__global__ void __launch_bounds__(TCR) k_trsm_col(const ColTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
+                                                  cx<T> *__restrict__ fac)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    cx<T> *U = reinterpret_cast<cx<T> *>(smraw);          // KB x (KB+1)
+    cx<T> *Xs = U + KB * (KB + 1);                        // TCR x (KB+1)
+    __shared__ cx<T> invd[KB];
+    const ColTask t = tasks[blockIdx.x];
+    const FrontDev F = fr[t.f];
+    const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
+    const int tid = threadIdx.x;
+    const cx<T> *D = fac + F.fac + (long long)k * nf + k;
+    for (int q = tid; q < kb * kb; q += blockDim.x) {
+        int i = q / kb, j = q % kb;
+        U[i * (KB + 1) + j] = D[(long long)i * nf + j];
+    }
+    cx<T> *xb;
+    long long ld;
+    int nr;
+    if (t.which == 0) {
+        xb = fac + F.fac + (long long)t.r0 * nf + k;
+        ld = nf;
+        nr = min(TCR, F.p - t.r0);
+    } else {
+        xb = fac + F.fac + (long long)F.p * nf + (long long)t.r0 * F.p + k;
+        ld = F.p;
+        nr = min(TCR, F.b - t.r0);
+    }
+    for (int q = tid; q < nr * kb; q += blockDim.x) {
+        int r = q / kb, j = q % kb;
+        Xs[r * (KB + 1) + j] = xb[(long long)r * ld + j];
+    }
+    __syncthreads();
+    for (int j = tid; j < kb; j += blockDim.x) invd[j] = cdiv(cx<T>(1), U[j * (KB + 1) + j]);
+    __syncthreads();
+    if (tid < nr) {
+        cx<T> *x = Xs + tid * (KB + 1);
+        for (int j = 0; j < kb; j++) {
+            cx<T> s = x[j];
+            for (int l = 0; l < j; l++) s = s - x[l] * U[l * (KB + 1) + j];
+            x[j] = s * invd[j];
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < nr * kb; q += blockDim.x) {
+        int r = q / kb, j = q % kb;
+        xb[(long long)r * ld + j] = Xs[r * (KB + 1) + j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// SIMT complex GEMM  C -= op(A) * B  (64x64 tiles, 4x4 per thread)
+// ---------------------------------------------------------------------------
+constexpr int GBM = 64, GBN = 64, GBK = 16;
+template <class T>
+__global__ void __launch_bounds__(256) k_gemm(const GemmTask<T> *__restrict__ tasks, int ntasks)
+{
+    __shared__ cx<T> As[GBK][GBM + 1];
+    __shared__ cx<T> Bs[GBK][GBN];
+    const int ti = find_task(tasks, ntasks, (long long)blockIdx.x);
+    const GemmTask<T> t = tasks[ti];
+    const long long lt = (long long)blockIdx.x - t.tile0;
+    const int m0 = (int)(lt / t.tiles_n) * GBM, n0 = (int)(lt % t.tiles_n) * GBN;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    cx<T> acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = cx<T>(0);
+    for (int k0 = 0; k0 < t.K; k0 += GBK) {
+        if (!t.conjA) {
+#pragma unroll
+            for (int q = 0; q < (GBM * GBK) / 256; q++) {
+                int idx = tid + q * 256;
+                int i = idx / GBK, kk = idx % GBK;
+                int r = m0 + i, c = k0 + kk;
+                As[kk][i] = (r < t.M && c < t.K) ? t.A[(long long)r * t.lda + c] : cx<T>(0);
+            }
+        } else {
+            // op(A)[r][c] = conj(A[c][r])
+#pragma unroll
+            for (int q = 0; q < (GBM * GBK) / 256; q++) {
+                int idx = tid + q * 256;
+                int kk = idx / GBM, i = idx % GBM;
+                int r = m0 + i, c = k0 + kk;
+                As[kk][i] = (r < t.M && c < t.K) ? conj(t.A[(long long)c * t.lda + r]) : cx<T>(0);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < (GBK * GBN) / 256; q++) {
+            int idx = tid + q * 256;
+            int kk = idx / GBN, j = idx % GBN;
+            int r = k0 + kk, c = n0 + j;
+            cx<T> v(0);
+            if (r < t.K && c < t.N) {
+                long long row = t.brow ? (long long)t.brow[r] : (long long)r;
+                v = t.B[row * t.ldb + c];
+            }
+            Bs[kk][j] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < GBK; kk++) {
+            cx<T> a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    acc[i][j].re = fma(a[i].re, b[j].re, fma(-a[i].im, b[j].im, acc[i][j].re));
+                    acc[i][j].im = fma(a[i].re, b[j].im, fma(a[i].im, b[j].re, acc[i][j].im));
+                }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        int r = m0 + ty + 16 * i;
+        if (r >= t.M) continue;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            int c = n0 + tx + 16 * j;
+            if (c >= t.N) continue;
+            if (t.crow) {
+                atomic_sub(t.C + (long long)t.crow[r] * t.ldc + c, acc[i][j]);
+            } else {
+                cx<T> *p = t.C + (long long)r * t.ldc + c;
+                *p = *p - acc[i][j];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// solve: diagonal-tile triangular solves on the RHS block of a front
+// mode 0: forward  (swaps + unit lower L_D)
+// mode 1: backward (upper U_D)
+// mode 2: adjoint forward  (U_D^H, lower, non-unit)
+// mode 3: adjoint backward (L_D^H, unit upper, then reverse swaps)
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(MAXRHS) k_diag_solve(const PanelTask *__restrict__ tasks,
+                                                       const FrontDev *__restrict__ fr,
+                                                       const cx<T> *__restrict__ fac, const int *__restrict__ ipiv,
+                                                       cx<T> *__restrict__ X, int ldx, int m, int mode)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    cx<T> *Ds = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1)
+    cx<T> *Ys = Ds + KB * (KB + 1);                 // KB x (MAXRHS+1)
+    __shared__ int idx[KB];
+    const PanelTask t = tasks[blockIdx.x];
+    const FrontDev F = fr[t.f];
+    const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
+    const int tid = threadIdx.x;
+    const cx<T> *D = fac + F.fac + (long long)k * nf + k;
+    for (int q = tid; q < kb * kb; q += blockDim.x) {
+        int i = q / kb, j = q % kb;
+        Ds[i * (KB + 1) + j] = D[(long long)i * nf + j];
+    }
+    if (tid == 0) {
+        for (int i = 0; i < kb; i++) idx[i] = i;
+        if (mode == 0 || mode == 3)
+            for (int j = 0; j < kb; j++) {
+                int pv = ipiv[F.first + k + j] - k;
+                int a = idx[j]; idx[j] = idx[pv]; idx[pv] = a;
+            }
+    }
+    __syncthreads();
+    cx<T> *Y = X + (long long)(F.first + k) * ldx;
+    const int LY = MAXRHS + 1;
+    for (int q = tid; q < kb * m; q += blockDim.x) {
+        int i = q / m, c = q % m;
+        Ys[i * LY + c] = Y[(long long)(mode == 0 ? idx[i] : i) * ldx + c];
+    }
+    __syncthreads();
+    if (tid < m) {
+        const int c = tid;
+        if (mode == 0) {
+            for (int i = 1; i < kb; i++) {
+                cx<T> s = Ys[i * LY + c];
+                for (int l = 0; l < i; l++) s = s - Ds[i * (KB + 1) + l] * Ys[l * LY + c];
+                Ys[i * LY + c] = s;
+            }
+        } else if (mode == 1) {
+            for (int i = kb - 1; i >= 0; i--) {
+                cx<T> s = Ys[i * LY + c];
+                for (int l = i + 1; l < kb; l++) s = s - Ds[i * (KB + 1) + l] * Ys[l * LY + c];
+                Ys[i * LY + c] = cdiv(s, Ds[i * (KB + 1) + i]);
+            }
+        } else if (mode == 2) {
+            // U_D^H y = s : lower triangular with conj(U[l][i])
+            for (int i = 0; i < kb; i++) {
+                cx<T> s = Ys[i * LY + c];
+                for (int l = 0; l < i; l++) s = s - conj(Ds[l * (KB + 1) + i]) * Ys[l * LY + c];
+                Ys[i * LY + c] = cdiv(s, conj(Ds[i * (KB + 1) + i]));
+            }
+        } else {
+            // L_D^H y = s : unit upper with conj(L[l][i])
+            for (int i = kb - 1; i >= 0; i--) {
+                cx<T> s = Ys[i * LY + c];
+                for (int l = i + 1; l < kb; l++) s = s - conj(Ds[l * (KB + 1) + i]) * Ys[l * LY + c];
+                Ys[i * LY + c] = s;
+            }
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < kb * m; q += blockDim.x) {
+        int i = q / m, c = q % m;
+        Y[(long long)(mode == 3 ? idx[i] : i) * ldx + c] = Ys[i * LY + c];
+    }
+}
+
+}  // namespace wt3d
