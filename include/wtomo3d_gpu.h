@@ -151,6 +151,10 @@ int wt3d_analyse_info(int nx, int ny, int nz, int leaf_nodes, long long *info, d
 int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *perm, int *fp, int *fb, int *ffirst,
                         int *fparent, int *flevel, int *border, int *rel);
 
+/* Copy internal device state to the host for checks (what = 0: factor pool,
+ * complex entries of the handle's precision; 1: pivot indices). */
+int wt3d_debug_fetch(wt3d_solver *h, int what, void *out, long long count);
+
 /* Last error message of the calling thread (static storage). */
 const char *wt3d_last_error(void);
 

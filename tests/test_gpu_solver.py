@@ -20,9 +20,25 @@ def oracle_matrix(oracle, g, vp, vs, rho, om):
     return sp.csr_matrix((a, jc - 1, ir - 1), shape=(g.n, g.n)), ir, jc, a
 
 
-def rand_rhs(n, k, seed=0):
+def rand_rhs(n, k, seed=0, g=None):
+    """k physical right-hand sides: point forces (random node, component and
+    complex amplitude) at seeded positions away from the Dirichlet faces.
+    (A random dense vector is not a meaningful load for this operator:
+    |A||x|/|b| reaches 1e10 and even SuperLU stops near 1e-6 relative
+    residual.)"""
     r = np.random.default_rng(seed)
-    return r.standard_normal((n, k)) + 1j * r.standard_normal((n, k))
+    nn = n // 3
+    nz, nx, ny = (g.nz, g.nx, g.ny) if g is not None else (None, None, None)
+    B = np.zeros((n, k), complex)
+    for j in range(k):
+        for _ in range(3):
+            if g is not None:
+                iz, ix, iy = r.integers(0, nz - 1), r.integers(1, nx - 1), r.integers(1, ny - 1)
+                node = iz + nz * (ix + nx * iy)
+            else:
+                node = r.integers(0, nn)
+            B[3 * node + r.integers(0, 3), j] += r.standard_normal() + 1j * r.standard_normal()
+    return B
 
 
 @pytest.fixture(scope="module")
@@ -35,50 +51,54 @@ def small_case(oracle):
     return g, vp, vs, rho, om, A, lu
 
 
-@pytest.mark.parametrize("prec", [wt.PREC_MIXED, wt.PREC_FP64])
-def test_solve_matches_superlu(small_case, prec):
+def test_mixed_vs_fp64_vs_superlu(small_case):
+    """Mixed precision and the FP64 GPU factorisation agree to 1e-8 relative;
+    both reach relative residual 1e-10 on the complex128 operator; SuperLU
+    (complex128) agrees to its own accuracy."""
     g, vp, vs, rho, om, A, lu = small_case
-    B = rand_rhs(g.n, 3)
-    with wt.Solver(g, prec) as s:
-        s.set_model(vp, vs, rho)
-        s.factor(om)
-        X = s.solve(B, tol=1e-10, maxit=30)
-        st = s.stats()
+    B = rand_rhs(g.n, 3, g=g)
+    out = {}
+    for prec in (wt.PREC_MIXED, wt.PREC_FP64):
+        with wt.Solver(g, prec) as s:
+            s.set_model(vp, vs, rho)
+            s.factor(om)
+            out[prec] = s.solve(B, tol=1e-10, maxit=30)
+            assert s.stats()["perturbed_pivots"] == 0
+        res = np.linalg.norm(B - A @ out[prec], axis=0) / np.linalg.norm(B, axis=0)
+        assert res.max() <= 1e-10, res
+    Xm, X64 = out[wt.PREC_MIXED], out[wt.PREC_FP64]
+    assert np.linalg.norm(Xm - X64) / np.linalg.norm(X64) <= 1e-8
     Xr = lu.solve(B)
-    err = np.linalg.norm(X - Xr) / np.linalg.norm(Xr)
-    res = np.linalg.norm(B - A @ X, axis=0) / np.linalg.norm(B, axis=0)
-    assert res.max() <= 1e-10, res
-    assert err <= 1e-8, err
-    assert st["perturbed_pivots"] == 0
-    if prec == wt.PREC_FP64:
-        assert err <= 1e-10
+    assert np.linalg.norm(X64 - Xr) / np.linalg.norm(Xr) <= 1e-6
 
 
 def test_mixed_refinement_converges_in_few_steps(small_case):
     g, vp, vs, rho, om, A, lu = small_case
-    B = rand_rhs(g.n, 8, seed=3)
+    B = rand_rhs(g.n, 8, seed=3, g=g)
     with wt.Solver(g) as s:
         s.set_model(vp, vs, rho)
         s.factor(om)
         X = s.solve(B, tol=1e-8, maxit=10)
-        assert s.last_iters <= 6
+        assert s.last_iters <= 5
         assert s.last_relres.max() <= 1e-8
 
 
 def test_many_rhs_batches(small_case):
     g, vp, vs, rho, om, A, lu = small_case
-    B = rand_rhs(g.n, 70, seed=4)   # two passes of 64 + 6
+    B = rand_rhs(g.n, 70, seed=4, g=g)   # two passes of 64 + 6
     with wt.Solver(g) as s:
         s.set_model(vp, vs, rho)
         s.factor(om)
         X = s.solve(B, tol=1e-9)
+    res = np.linalg.norm(B - A @ X, axis=0) / np.linalg.norm(B, axis=0)
+    assert res.max() <= 1e-9
     Xr = lu.solve(B)
-    assert np.linalg.norm(X - Xr) / np.linalg.norm(Xr) <= 1e-7
+    assert np.linalg.norm(X - Xr) / np.linalg.norm(Xr) <= 1e-5
 
 
 def test_adjoint_solve(small_case):
     g, vp, vs, rho, om, A, lu = small_case
-    B = rand_rhs(g.n, 2, seed=5)
+    B = rand_rhs(g.n, 2, seed=5, g=g)
     with wt.Solver(g) as s:
         s.set_model(vp, vs, rho)
         s.factor(om)
@@ -87,7 +107,7 @@ def test_adjoint_solve(small_case):
     res = np.linalg.norm(B - AH @ X, axis=0) / np.linalg.norm(B, axis=0)
     assert res.max() <= 1e-10
     Xr = spla.splu(AH.tocsc()).solve(B)
-    assert np.linalg.norm(X - Xr) / np.linalg.norm(Xr) <= 1e-8
+    assert np.linalg.norm(X - Xr) / np.linalg.norm(Xr) <= 1e-5
 
 
 def test_apply_matches_oracle_operator(small_case):
@@ -113,8 +133,9 @@ def test_config1_point_force_small(oracle):
         s.set_model(vp, vs, rho)
         s.factor(2 * np.pi)
         x = s.solve(b, tol=1e-10)
+    assert np.linalg.norm(b - A @ x) / np.linalg.norm(b) <= 1e-10
     xr = spla.spsolve(A.tocsc(), b)
-    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) <= 1e-8
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) <= 1e-5
 
 
 def test_strumpack_job_protocol(oracle):
@@ -135,7 +156,7 @@ def test_strumpack_job_protocol(oracle):
         a64, ierr = oracle.assemble(g, vp, vs, rho, 2 * np.pi * f, ir, "c64")
         assert ierr == 0
         assert wt.strumpack_serial_finter(2, n, nnz, ir, jc, a64, dummy, dummy.copy()) == 0
-        rhs = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+        rhs = rand_rhs(n, 1, seed=int(f * 10), g=g)[:, 0].astype(np.complex64)
         sol = np.zeros(n, np.complex64)
         assert wt.strumpack_serial_finter(3, n, nnz, ir, jc, a64, rhs, sol) == 0
         A = sp.csr_matrix((a64.astype(np.complex128), jc - 1, ir - 1), shape=(n, n))

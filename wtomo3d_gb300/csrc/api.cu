@@ -79,30 +79,36 @@ __global__ void __launch_bounds__(256) k_residual(long long n, int m, const int 
     if (j1 < m) { atomicAdd(&nr[j1], sr1); atomicAdd(&nb[j1], sb1); }
 }
 
+// Xs = S R (new ordering, engine precision); S the Jacobi scaling of the factor.
 template <class T>
-__global__ void k_gather_new(long long n, int m, const int *__restrict__ perm, const double2 *__restrict__ R,
-                             cx<T> *__restrict__ Xs)
+__global__ void k_gather_new(long long n, int m, const int *__restrict__ perm, const double *__restrict__ s,
+                             const double2 *__restrict__ R, cx<T> *__restrict__ Xs)
 {
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n * m) return;
     long long i = q / m;
     int j = (int)(q % m);
-    double2 v = R[(long long)perm[i] * MAXRHS + j];
-    Xs[i * MAXRHS + j] = cx<T>((T)v.x, (T)v.y);
+    const long long o = perm[i];
+    double2 v = R[o * MAXRHS + j];
+    const double w = s[o];
+    Xs[i * MAXRHS + j] = cx<T>((T)(v.x * w), (T)(v.y * w));
 }
 
+// Xn += S Xs (natural ordering, FP64 accumulate).
 template <class T>
-__global__ void k_scatter_add_nat(long long n, int m, const int *__restrict__ perm, const cx<T> *__restrict__ Xs,
-                                  double2 *__restrict__ Xn)
+__global__ void k_scatter_add_nat(long long n, int m, const int *__restrict__ perm, const double *__restrict__ s,
+                                  const cx<T> *__restrict__ Xs, double2 *__restrict__ Xn)
 {
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n * m) return;
     long long i = q / m;
     int j = (int)(q % m);
     cx<T> v = Xs[i * MAXRHS + j];
-    double2 *d = Xn + (long long)perm[i] * MAXRHS + j;
-    d->x += (double)v.re;
-    d->y += (double)v.im;
+    const long long o = perm[i];
+    const double w = s[o];
+    double2 *d = Xn + o * MAXRHS + j;
+    d->x += (double)v.re * w;
+    d->y += (double)v.im * w;
 }
 
 __global__ void k_c64_to_c128(long long n, const float2 *__restrict__ s, double2 *__restrict__ d)
@@ -190,13 +196,14 @@ int refine(wt3d_solver *h, Engine<T> &E, int m, bool adjoint, double tol, int ma
     WT_CUDA(cudaMemcpyAsync(h->Rn.p, h->Bn.p, sizeof(double2) * n * MAXRHS, cudaMemcpyDeviceToDevice, st));
     std::vector<double> hn(2 * MAXRHS);
     int it = 0, rc = WT3D_OK;
+    double prev_worst = INFINITY;
     const int th = 256;
     const unsigned nb = (unsigned)ceil_div(n * m, th);
     for (;;) {
-        k_gather_new<T><<<nb, th, 0, st>>>(n, m, h->perm.p, h->Rn.p, E.X.p);
+        k_gather_new<T><<<nb, th, 0, st>>>(n, m, h->perm.p, E.scale.p, h->Rn.p, E.X.p);
         rc = E.run(*sc, st);
         if (rc) return rc;
-        k_scatter_add_nat<T><<<nb, th, 0, st>>>(n, m, h->perm.p, E.X.p, h->Xn.p);
+        k_scatter_add_nat<T><<<nb, th, 0, st>>>(n, m, h->perm.p, E.scale.p, E.X.p, h->Xn.p);
         WT_CUDA(cudaMemsetAsync(h->norms.p, 0, sizeof(double) * 2 * MAXRHS, st));
         k_residual<<<152 * 8, 256, 0, st>>>(n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, h->Xn.p, h->Bn.p,
                                             h->Rn.p, h->norms.p, h->norms.p + MAXRHS, adjoint ? 1 : 0);
@@ -212,6 +219,10 @@ int refine(wt3d_solver *h, Engine<T> &E, int m, bool adjoint, double tol, int ma
         if (!(worst == worst)) { rc = WT3D_ERR_NOCONV; break; }   // NaN
         if (worst <= tol) break;
         if (it >= maxit) { rc = WT3D_ERR_NOCONV; break; }
+        // stop when a step no longer halves the worst residual: the FP64
+        // residual itself has reached its rounding floor (|A||x|/|b| * eps)
+        if (it >= 2 && worst > 0.5 * prev_worst) { rc = WT3D_ERR_NOCONV; break; }
+        prev_worst = worst;
         it++;
     }
     if (iters) *iters = it;
@@ -362,10 +373,10 @@ int wt3d_solver_create(wt3d_solver **out, const wt3d_grid *g, int precision)
         return rc;
     if (precision == WT3D_PREC_MIXED) {
         h->e32.reset(new Engine<float>());
-        rc = h->e32->init(h->sym, map);
+        rc = h->e32->init(h->sym, map, h->irptr.p, h->jcptr.p);
     } else {
         h->e64.reset(new Engine<double>());
-        rc = h->e64->init(h->sym, map);
+        rc = h->e64->init(h->sym, map, h->irptr.p, h->jcptr.p);
     }
     if (rc) return rc;
     auto t1 = std::chrono::steady_clock::now();
@@ -627,5 +638,24 @@ extern "C" int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *
     }
     std::copy(S.border.begin(), S.border.end(), border);
     std::copy(S.rel.begin(), S.rel.end(), rel);
+    return WT3D_OK;
+}
+
+// Copy internal device state to the host for checks: what = 0 factor pool
+// (complex entries of the engine precision), 1 pivot indices, 2 the two update
+// buffers back to back.  count = elements to copy.
+extern "C" int wt3d_debug_fetch(wt3d_solver *h, int what, void *out, long long count)
+{
+    if (!h || !out) return WT3D_ERR_ARG;
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    if (what == 0) {
+        if (h->e32) WT_CUDA(cudaMemcpy(out, h->e32->fac.p, sizeof(cx<float>) * std::min<long long>(count, h->e32->fac.n), cudaMemcpyDeviceToHost));
+        else WT_CUDA(cudaMemcpy(out, h->e64->fac.p, sizeof(cx<double>) * std::min<long long>(count, h->e64->fac.n), cudaMemcpyDeviceToHost));
+    } else if (what == 1) {
+        const int *p = h->e32 ? h->e32->ipiv.p : h->e64->ipiv.p;
+        WT_CUDA(cudaMemcpy(out, p, sizeof(int) * std::min<long long>(count, h->n), cudaMemcpyDeviceToHost));
+    } else {
+        return WT3D_ERR_ARG;
+    }
     return WT3D_OK;
 }

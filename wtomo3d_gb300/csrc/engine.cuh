@@ -79,7 +79,7 @@ public:
     DevVec<unsigned long long> maxabs;
     std::unique_ptr<Schedule<T>> fsched;
     std::map<int, std::unique_ptr<Schedule<T>>> ssched[2];   // [adjoint][m]
-    double pivot_rel = 1e-7;
+    double pivot_rel = 1e-20;   // only (near-)zero pivots are replaced: Dirichlet rows carry unit pivots next to O(1e8) stiffness entries
     bool use_graphs = true;
 
     size_t device_bytes() const
@@ -88,9 +88,14 @@ public:
                fr.n * sizeof(FrontDev) + map.n * 8;
     }
 
-    int init(const Symbolic &sym, const std::vector<long long> &hmap)
+    const int *d_irptr = nullptr, *d_jcptr = nullptr;   // natural 0-based CSR of the operator
+    DevVec<double> scale;                              // Jacobi scaling 1/sqrt|a_ii|, natural ordering
+
+    int init(const Symbolic &sym, const std::vector<long long> &hmap, const int *irp, const int *jcp)
     {
         S = &sym;
+        d_irptr = irp;
+        d_jcptr = jcp;
         int rc;
         if ((rc = fac.alloc(sym.fac_total))) return rc;
         if ((rc = upd0.alloc(std::max<long long>(sym.upd_size[0], 1)))) return rc;
@@ -102,6 +107,7 @@ public:
         if ((rc = map.upload(hmap))) return rc;
         if ((rc = npert.alloc(1))) return rc;
         if ((rc = maxabs.alloc(1))) return rc;
+        if ((rc = scale.alloc(sym.n))) return rc;
         std::vector<FrontDev> h(sym.fronts.size());
         for (size_t f = 0; f < h.size(); f++) {
             const Front &F = sym.fronts[f];
@@ -172,15 +178,20 @@ public:
         const Symbolic &sym = *S;
         cx<T> *F = fac.p;
         cx<T> *U[2] = {upd0.p, upd1.p};
-        const long long nnz = (long long)map.n;
-        // zero the factor pool, scatter the operator
+        // zero the factor pool, scale and scatter the operator
         {
             cx<T> *fp = F; size_t bytes = fac.n * sizeof(cx<T>);
             long long *mp = map.p;
             Engine<T> *self = this;
+            const long long n = sym.n;
             sc->launches.push_back([fp, bytes](cudaStream_t st) { cudaMemsetAsync(fp, 0, bytes, st); });
-            sc->launches.push_back([self, mp, nnz, fp](cudaStream_t st) {
-                k_scatter<T><<<ceil_div(nnz, 256), 256, 0, st>>>(nnz, mp, self->a_dev, fp);
+            sc->launches.push_back([self, n](cudaStream_t st) {
+                k_jacobi_scale<<<ceil_div(n, 256), 256, 0, st>>>(n, self->d_irptr, self->d_jcptr, self->a_dev,
+                                                                 self->scale.p);
+            });
+            sc->launches.push_back([self, mp, n, fp](cudaStream_t st) {
+                k_scatter<T><<<ceil_div(n, 256), 256, 0, st>>>(n, self->d_irptr, self->d_jcptr, mp, self->a_dev,
+                                                               self->scale.p, fp);
             });
         }
         const int nlev = (int)sym.levels.size();
