@@ -137,6 +137,8 @@ typedef struct wt3d_stats {
     double    t_analyse_ms, t_assemble_ms, t_factor_ms, t_solve_ms; /* last calls */
     int       perturbed_pivots;    /* pivots replaced by the static threshold */
     int       levels;              /* depth of the elimination tree + 1       */
+    int       kernels_factor;      /* kernels launched by the last factor call */
+    int       kernels_solve;       /* kernels launched by the last solve call  */
 } wt3d_stats;
 int wt3d_get_stats(const wt3d_solver *h, wt3d_stats *st);
 
@@ -150,6 +152,19 @@ int wt3d_analyse_info(int nx, int ny, int nz, int leaf_nodes, long long *info, d
  * (new indices) and their positions in the parent front (rel). */
 int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *perm, int *fp, int *fb, int *ffirst,
                         int *fparent, int *flevel, int *border, int *rel);
+
+/* Select the CUDA device of the calling thread (one process per GPU). */
+int wt3d_set_device(int dev);
+
+/* The CUDA stream (cudaStream_t) every call on this handle runs on, for
+ * callers that time or order work against it. */
+void *wt3d_get_stream(wt3d_solver *h);
+
+/* Factor the current operator once with an event pair around every launch
+ * (no CUDA graph).  out[7] = ms in {memset, scatter, extend-add, panel, trsm,
+ * gemm, diagonal solve} launches, out[7] = GEMM real flops, out[8] = GEMM
+ * launches.  out must hold 9 doubles. */
+int wt3d_profile_factor(wt3d_solver *h, double *out);
 
 /* Copy internal device state to the host for checks (what = 0: factor pool,
  * complex entries of the handle's precision; 1: pivot indices). */

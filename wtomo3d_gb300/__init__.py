@@ -68,7 +68,8 @@ class Stats(ctypes.Structure):
                 ("factor_bytes", ctypes.c_double), ("device_bytes", ctypes.c_double),
                 ("t_analyse_ms", ctypes.c_double), ("t_assemble_ms", ctypes.c_double),
                 ("t_factor_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double),
-                ("perturbed_pivots", ctypes.c_int), ("levels", ctypes.c_int)]
+                ("perturbed_pivots", ctypes.c_int), ("levels", ctypes.c_int),
+                ("kernels_factor", ctypes.c_int), ("kernels_solve", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -103,6 +104,10 @@ def lib():
                                         ctypes.c_int]
         L.wt3d_apply.argtypes = [vp, ctypes.c_int, vp, vp]
         L.wt3d_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+        L.wt3d_get_stream.restype = vp
+        L.wt3d_get_stream.argtypes = [vp]
+        L.wt3d_profile_factor.argtypes = [vp, vp]
+        L.wt3d_set_device.argtypes = [ctypes.c_int]
         ip = ctypes.POINTER(ctypes.c_int)
         L.strumpack_serial_finter.argtypes = [ip, ip, ip, vp, vp, vp, vp, vp, ip]
         L.strumpack_serial_finter.restype = None
@@ -125,6 +130,11 @@ def _f32(a, n):
     if a.size != n:
         raise ValueError("model array has %d entries, expected %d" % (a.size, n))
     return a
+
+
+def set_device(dev):
+    """Select the CUDA device of the calling thread for this library."""
+    _check(lib().wt3d_set_device(int(dev)))
 
 
 def pattern(nx, ny, nz, base=1):
@@ -215,6 +225,31 @@ class Solver:
         Y = np.empty_like(Xf, order="F")
         _check(lib().wt3d_apply(self._h, Xf.shape[1], _ptr(Xf), _ptr(Y)))
         return Y[:, 0] if one else Y
+
+    @property
+    def stream(self):
+        """cudaStream_t (as an int) every call on this handle runs on."""
+        return lib().wt3d_get_stream(self._h) or 0
+
+    def solve_device(self, d_B, d_X, nrhs, tol=1e-8, maxit=20, adjoint=False, allow_noconv=False):
+        """Solve with device pointers (column-major n x nrhs complex128)."""
+        relres = np.zeros(nrhs)
+        iters = ctypes.c_int(0)
+        rc = lib().wt3d_solve_device(self._h, nrhs, ctypes.c_void_p(d_B), ctypes.c_void_p(d_X), tol, maxit,
+                                     _ptr(relres), ctypes.byref(iters), int(adjoint))
+        _check(rc, allow=(WT3D_ERR_NOCONV,) if allow_noconv else ())
+        self.last_relres, self.last_iters = relres, iters.value
+        return relres
+
+    def profile_factor(self):
+        """Per-kernel-kind milliseconds of one factorisation (no graph)."""
+        out = np.zeros(9)
+        _check(lib().wt3d_profile_factor(self._h, _ptr(out)))
+        kinds = ["memset", "scatter", "extend_add", "panel", "trsm", "gemm", "diag_solve"]
+        d = {k + "_ms": float(out[i]) for i, k in enumerate(kinds)}
+        d["gemm_flops"] = float(out[7])
+        d["gemm_launches"] = int(out[8])
+        return d
 
     def stats(self):
         s = Stats()

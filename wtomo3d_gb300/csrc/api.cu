@@ -138,6 +138,7 @@ struct wt3d_solver {
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool have_model = false, have_values = false, have_factor = false;
+    long long kernels_solve = 0;
     wt3d_stats stats{};
     ~wt3d_solver()
     {
@@ -203,6 +204,7 @@ int refine(wt3d_solver *h, Engine<T> &E, int m, bool adjoint, double tol, int ma
         k_gather_new<T><<<nb, th, 0, st>>>(n, m, h->perm.p, E.scale.p, h->Rn.p, E.X.p);
         rc = E.run(*sc, st);
         if (rc) return rc;
+        h->kernels_solve += sc->kernels() + 3;   // + gather, scatter-add, residual
         k_scatter_add_nat<T><<<nb, th, 0, st>>>(n, m, h->perm.p, E.scale.p, E.X.p, h->Xn.p);
         WT_CUDA(cudaMemsetAsync(h->norms.p, 0, sizeof(double) * 2 * MAXRHS, st));
         k_residual<<<152 * 8, 256, 0, st>>>(n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, h->Xn.p, h->Bn.p,
@@ -236,10 +238,12 @@ int solve_dev_cm(wt3d_solver *h, int nrhs, const double2 *d_B, double2 *d_X, dou
     if (!h->have_factor) { set_error("solve before factor"); return WT3D_ERR_STATE; }
     const long long n = h->n;
     int worst_rc = WT3D_OK, maxits = 0;
+    h->kernels_solve = 0;
     cudaEventRecord(h->ev0, h->st);
     for (int c0 = 0; c0 < nrhs; c0 += MAXRHS) {
         int m = std::min(MAXRHS, nrhs - c0);
         k_cm_to_rm<<<ceil_div(n, 256), 256, 0, h->st>>>(n, m, d_B + (long long)c0 * n, h->Bn.p);
+        h->kernels_solve += 2;   // layout conversions in and out
         int its = 0, rc;
         if (h->e32) rc = refine<float>(h, *h->e32, m, adjoint, tol, maxit, relres ? relres + c0 : nullptr, &its);
         else rc = refine<double>(h, *h->e64, m, adjoint, tol, maxit, relres ? relres + c0 : nullptr, &its);
@@ -251,6 +255,7 @@ int solve_dev_cm(wt3d_solver *h, int nrhs, const double2 *d_B, double2 *d_X, dou
     cudaEventRecord(h->ev1, h->st);
     WT_CUDA(cudaStreamSynchronize(h->st));
     h->stats.t_solve_ms = ms_between(h->ev0, h->ev1);
+    h->stats.kernels_solve = (int)h->kernels_solve;
     if (iters) *iters = maxits;
     return worst_rc;
 }
@@ -428,6 +433,7 @@ static int factor_values(wt3d_solver *h)
     WT_CUDA(cudaStreamSynchronize(h->st));
     h->stats.t_factor_ms = ms_between(h->ev0, h->ev1);
     h->stats.perturbed_pivots = np;
+    h->stats.kernels_factor = 2 + (h->e32 ? h->e32->fsched->kernels() : h->e64->fsched->kernels());
     h->stats.device_bytes = (double)(h->e32 ? h->e32->device_bytes() : h->e64->device_bytes()) +
                             (double)h->nnz * (16 + 4 + 4) + (double)h->n * MAXRHS * 16 * 3;
     h->have_factor = true;
@@ -446,7 +452,9 @@ int wt3d_factor(wt3d_solver *h, double omega_re, double omega_im)
     WT_CUDA(cudaStreamSynchronize(h->st));
     h->stats.t_assemble_ms = ms_between(h->ev0, h->ev1);
     h->have_values = true;
-    return factor_values(h);
+    rc = factor_values(h);
+    h->stats.kernels_factor += 1;   // the assembly kernel
+    return rc;
 }
 
 int wt3d_set_values_c64(wt3d_solver *h, const float _Complex *a)
@@ -644,6 +652,17 @@ extern "C" int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *
 // Copy internal device state to the host for checks: what = 0 factor pool
 // (complex entries of the engine precision), 1 pivot indices, 2 the two update
 // buffers back to back.  count = elements to copy.
+extern "C" void *wt3d_get_stream(wt3d_solver *h) { return h ? (void *)h->st : nullptr; }
+
+extern "C" int wt3d_profile_factor(wt3d_solver *h, double *out)
+{
+    if (!h || !out || !h->have_values) return WT3D_ERR_STATE;
+    int rc = h->e32 ? h->e32->profile_factor(h->a.p, h->nnz, h->st, out)
+                    : h->e64->profile_factor(h->a.p, h->nnz, h->st, out);
+    if (!rc) h->have_factor = true;
+    return rc;
+}
+
 extern "C" int wt3d_debug_fetch(wt3d_solver *h, int what, void *out, long long count)
 {
     if (!h || !out) return WT3D_ERR_ARG;
@@ -657,5 +676,13 @@ extern "C" int wt3d_debug_fetch(wt3d_solver *h, int what, void *out, long long c
     } else {
         return WT3D_ERR_ARG;
     }
+    return WT3D_OK;
+}
+
+// Select the CUDA device for the calling thread (multi-GPU replicas: one
+// process per GPU).
+extern "C" int wt3d_set_device(int dev)
+{
+    WT_CUDA(cudaSetDevice(dev));
     return WT3D_OK;
 }

@@ -50,10 +50,25 @@ struct DevVec {
 
 using Launch = std::function<void(cudaStream_t)>;
 
+// Launch kinds, for the per-kernel profile.
+enum LaunchKind { LK_MEMSET = 0, LK_SCATTER, LK_EXTEND_ADD, LK_PANEL, LK_TRSM, LK_GEMM, LK_DIAG, LK_NKINDS };
+
+struct LaunchRec {
+    Launch fn;
+    int kind;
+    double flops;   // real-flop count of a GEMM launch (sum of 8 M N K)
+};
+
 // A list of launches plus the task arrays they read.
 template <class T>
 struct Schedule {
-    std::vector<Launch> launches;
+    std::vector<LaunchRec> launches;
+    int kernels() const
+    {
+        int c = 0;
+        for (auto &l : launches) c += l.kind != LK_MEMSET;
+        return c;
+    }
     DevVec<PanelTask> panel;
     DevVec<RowTask> row;
     DevVec<ColTask> col;
@@ -161,9 +176,11 @@ public:
         int nt = (int)(all.size() - b);
         long long ntiles = tiles - t0;
         Schedule<T> *psc = &sc;
-        sc.launches.push_back([psc, b, nt, ntiles](cudaStream_t st) {
+        double fl = 0;
+        for (size_t i = b; i < all.size(); i++) fl += 8.0 * all[i].M * (double)all[i].N * all[i].K;
+        sc.launches.push_back({[psc, b, nt, ntiles](cudaStream_t st) {
             k_gemm<T><<<(unsigned)ntiles, 256, 0, st>>>(psc->gemm.p + b, nt);
-        });
+        }, LK_GEMM, fl});
     }
 
     int build_factor_schedule()
@@ -184,15 +201,15 @@ public:
             long long *mp = map.p;
             Engine<T> *self = this;
             const long long n = sym.n;
-            sc->launches.push_back([fp, bytes](cudaStream_t st) { cudaMemsetAsync(fp, 0, bytes, st); });
-            sc->launches.push_back([self, n](cudaStream_t st) {
+            sc->launches.push_back({[fp, bytes](cudaStream_t st) { cudaMemsetAsync(fp, 0, bytes, st); }, LK_MEMSET, 0});
+            sc->launches.push_back({[self, n](cudaStream_t st) {
                 k_jacobi_scale<<<ceil_div(n, 256), 256, 0, st>>>(n, self->d_irptr, self->d_jcptr, self->a_dev,
                                                                  self->scale.p);
-            });
-            sc->launches.push_back([self, mp, n, fp](cudaStream_t st) {
+            }, LK_SCATTER, 0});
+            sc->launches.push_back({[self, mp, n, fp](cudaStream_t st) {
                 k_scatter<T><<<ceil_div(n, 256), 256, 0, st>>>(n, self->d_irptr, self->d_jcptr, mp, self->a_dev,
                                                                self->scale.p, fp);
-            });
+            }, LK_SCATTER, 0});
         }
         const int nlev = (int)sym.levels.size();
         for (int L = nlev - 1; L >= 0; L--) {
@@ -203,7 +220,7 @@ public:
             if (usz > 0) {
                 cx<T> *up = U[L & 1];
                 size_t bytes = usz * sizeof(cx<T>);
-                sc->launches.push_back([up, bytes](cudaStream_t st) { cudaMemsetAsync(up, 0, bytes, st); });
+                sc->launches.push_back({[up, bytes](cudaStream_t st) { cudaMemsetAsync(up, 0, bytes, st); }, LK_MEMSET, 0});
             }
             // extend-add, one child slot at a time (siblings overlap in the parent)
             for (int slot = 0; slot < 2; slot++) {
@@ -219,10 +236,10 @@ public:
                 }
                 if (he.size() > b0) {
                     int nt = (int)(he.size() - b0);
-                    sc->launches.push_back([psc, this, b0, nt, rows](cudaStream_t st) {
+                    sc->launches.push_back({[psc, this, b0, nt, rows](cudaStream_t st) {
                         k_extend_add<T><<<ceil_div(rows * 32, 256), 256, 0, st>>>(
                             psc->ea.p + b0, nt, rows, fr.p, rel.p, fac.p, upd0.p, upd1.p);
-                    });
+                    }, LK_EXTEND_ADD, 0});
                 }
             }
             // blocked partial LU, level-synchronous over fronts
@@ -250,17 +267,17 @@ public:
                 size_t smp = sizeof(cx<T>) * KB * (KB + 1);
                 size_t smr = sizeof(cx<T>) * (KB * (KB + 1) + KB * (TRW + 1));
                 size_t smc = sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1));
-                sc->launches.push_back([psc, this, p0, np, smp](cudaStream_t st) {
+                sc->launches.push_back({[psc, this, p0, np, smp](cudaStream_t st) {
                     k_panel<T><<<np, 256, smp, st>>>(psc->panel.p + p0, fr.p, fac.p, ipiv.p, maxabs.p, pivot_rel, npert.p);
-                });
+                }, LK_PANEL, 0});
                 if (nr)
-                    sc->launches.push_back([psc, this, r0, nr, smr](cudaStream_t st) {
+                    sc->launches.push_back({[psc, this, r0, nr, smr](cudaStream_t st) {
                         k_trsm_row<T><<<nr, TRW, smr, st>>>(psc->row.p + r0, fr.p, fac.p, ipiv.p);
-                    });
+                    }, LK_TRSM, 0});
                 if (ncl)
-                    sc->launches.push_back([psc, this, c0, ncl, smc](cudaStream_t st) {
+                    sc->launches.push_back({[psc, this, c0, ncl, smc](cudaStream_t st) {
                         k_trsm_col<T><<<ncl, TCR, smc, st>>>(psc->col.p + c0, fr.p, fac.p);
-                    });
+                    }, LK_TRSM, 0});
                 push_gemm_launch(*sc, hg, g0, tiles);
             }
             // Schur complement F22 -= L21 U12 (K = p)
@@ -306,9 +323,9 @@ public:
         auto diag_launch = [&](size_t p0, int mode) {
             int np = (int)(hp.size() - p0);
             if (!np) return;
-            sc->launches.push_back([psc, this, p0, np, smd, m, mode, Xp, ldx](cudaStream_t st) {
+            sc->launches.push_back({[psc, this, p0, np, smd, m, mode, Xp, ldx](cudaStream_t st) {
                 k_diag_solve<T><<<np, MAXRHS, smd, st>>>(psc->panel.p + p0, fr.p, fac.p, ipiv.p, Xp, ldx, m, mode);
-            });
+            }, LK_DIAG, 0});
         };
         // ---- forward sweep: leaves to root ----
         for (int L = nlev - 1; L >= 0; L--) {
@@ -419,7 +436,7 @@ public:
             if (!sc.graph) {
                 cudaGraph_t g;
                 WT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                for (auto &l : sc.launches) l(st);
+                for (auto &l : sc.launches) l.fn(st);
                 WT_CUDA(cudaStreamEndCapture(st, &g));
                 cudaError_t e = cudaGraphInstantiate(&sc.graph, g, 0);
                 cudaGraphDestroy(g);
@@ -431,8 +448,40 @@ public:
             }
             WT_CUDA(cudaGraphLaunch(sc.graph, st));
         } else {
-            for (auto &l : sc.launches) l(st);
+            for (auto &l : sc.launches) l.fn(st);
         }
+        WT_CUDA(cudaGetLastError());
+        return WT3D_OK;
+    }
+
+    // Factorisation with one event pair around every launch (no graph):
+    // out[k] = milliseconds spent in launches of kind k, out[LK_NKINDS] =
+    // GEMM real flops, out[LK_NKINDS+1] = GEMM launches.
+    int profile_factor(const double2 *d_a, long long nnz, cudaStream_t st, double *out)
+    {
+        a_dev = d_a;
+        WT_CUDA(cudaMemsetAsync(maxabs.p, 0, sizeof(unsigned long long), st));
+        k_maxabs<<<1216, 256, 0, st>>>(nnz, d_a, maxabs.p);
+        const size_t nl = fsched->launches.size();
+        std::vector<cudaEvent_t> ev(2 * nl);
+        for (auto &e : ev) WT_CUDA(cudaEventCreate(&e));
+        for (size_t i = 0; i < nl; i++) {
+            WT_CUDA(cudaEventRecord(ev[2 * i], st));
+            fsched->launches[i].fn(st);
+            WT_CUDA(cudaEventRecord(ev[2 * i + 1], st));
+        }
+        WT_CUDA(cudaStreamSynchronize(st));
+        for (int k = 0; k < LK_NKINDS + 2; k++) out[k] = 0;
+        for (size_t i = 0; i < nl; i++) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+            out[fsched->launches[i].kind] += ms;
+            if (fsched->launches[i].kind == LK_GEMM) {
+                out[LK_NKINDS] += fsched->launches[i].flops;
+                out[LK_NKINDS + 1] += 1;
+            }
+        }
+        for (auto &e : ev) cudaEventDestroy(e);
         WT_CUDA(cudaGetLastError());
         return WT3D_OK;
     }
