@@ -161,14 +161,25 @@ int wt3d_set_device(int dev);
 void *wt3d_get_stream(wt3d_solver *h);
 
 /* Factor the current operator once with an event pair around every launch
- * (no CUDA graph).  out[7] = ms in {memset, scatter, extend-add, panel, trsm,
- * gemm, diagonal solve} launches, out[7] = GEMM real flops, out[8] = GEMM
- * launches.  out must hold 9 doubles. */
+ * (no CUDA graph).  out[0..8] = ms in {memset, scatter, extend-add, panel,
+ * trsm, SIMT gemm, diagonal solve, tensor-core operand split, tensor-core
+ * gemm} launches, out[9] = GEMM real flops (both paths), out[10] = GEMM
+ * launches.  out must hold 11 doubles. */
 int wt3d_profile_factor(wt3d_solver *h, double *out);
 
 /* Copy internal device state to the host for checks (what = 0: factor pool,
  * complex entries of the handle's precision; 1: pivot indices). */
 int wt3d_debug_fetch(wt3d_solver *h, int what, void *out, long long count);
+
+/* One complex64 GEMM C -= A B on host row-major arrays through the tensor-core
+ * kernel (path 1) or the SIMT kernel (path 0); for checks of the kernels. */
+int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int lda, const void *B, int ldb, void *C,
+                    int ldc);
+
+/* Device-resident timing of the GEMM kernels: average ms of `iters`
+ * launches of C -= A B (M x K by K x N complex64, device-filled operands);
+ * path 1 = tensor-core kernel (operand split excluded), 0 = SIMT kernel. */
+int wt3d_bench_gemm(int path, int M, int N, int K, int iters, double *ms_out);
 
 /* Last error message of the calling thread (static storage). */
 const char *wt3d_last_error(void);

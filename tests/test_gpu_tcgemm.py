@@ -1,0 +1,56 @@
+"""The tcgen05 complex64 GEMM (3xTF32 split, real expansion of B) against a
+complex128 numpy product, next to the SIMT kernel, on ragged shapes."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import wtomo3d_gb300 as wt
+
+pytestmark = pytest.mark.gpu
+
+
+def gemm(path, A, B, C):
+    L = wt.lib()
+    L.wt3d_debug_gemm.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                       ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    M, K = A.shape
+    N = B.shape[1]
+    A = np.ascontiguousarray(A, np.complex64)
+    B = np.ascontiguousarray(B, np.complex64)
+    C = np.ascontiguousarray(C, np.complex64).copy()
+    p = lambda a: ctypes.c_void_p(a.ctypes.data)
+    rc = L.wt3d_debug_gemm(path, M, N, K, p(A), A.shape[1], p(B), B.shape[1], p(C), C.shape[1])
+    assert rc == 0, L.wt3d_last_error()
+    return C
+
+
+@pytest.mark.parametrize("shape", [(128, 128, 16), (130, 70, 37), (64, 200, 64), (300, 260, 129), (512, 640, 1000)])
+@pytest.mark.parametrize("path", [1, 0])
+def test_gemm_accuracy(shape, path):
+    M, N, K = shape
+    r = np.random.default_rng(M * 7 + N * 3 + K)
+    A = (r.standard_normal((M, K)) + 1j * r.standard_normal((M, K))).astype(np.complex64)
+    B = (r.standard_normal((K, N)) + 1j * r.standard_normal((K, N))).astype(np.complex64)
+    C = (r.standard_normal((M, N)) + 1j * r.standard_normal((M, N))).astype(np.complex64)
+    ref = C.astype(np.complex128) - A.astype(np.complex128) @ B.astype(np.complex128)
+    out = gemm(path, A, B, C)
+    # FP32-class product: error relative to sum |a||b| per entry
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64) + np.abs(C)
+    err = (np.abs(out - ref) / scale).max()
+    assert err < 1e-6 + 3e-7 * np.sqrt(K), err   # FP32 accumulation grows with K
+
+
+def test_gemm_strided_views():
+    """Sub-blocks of larger arrays (the front layout): lda/ldb/ldc > widths."""
+    r = np.random.default_rng(1)
+    F = (r.standard_normal((400, 900)) + 1j * r.standard_normal((400, 900))).astype(np.complex64)
+    L = wt.lib()
+    p = lambda a: ctypes.c_void_p(a.ctypes.data)
+    A = F[100:300, 0:64]
+    B = F[0:64, 300:800]
+    C = F[100:300, 300:800]
+    ref = C.astype(np.complex128) - A.astype(np.complex128) @ B.astype(np.complex128)
+    out = gemm(1, A, B, C)
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64) + np.abs(C)
+    assert (np.abs(out - ref) / scale).max() < 2e-6

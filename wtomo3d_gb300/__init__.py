@@ -243,12 +243,13 @@ class Solver:
 
     def profile_factor(self):
         """Per-kernel-kind milliseconds of one factorisation (no graph)."""
-        out = np.zeros(9)
+        kinds = ["memset", "scatter", "extend_add", "panel", "trsm", "gemm_simt", "diag_solve", "tc_split",
+                 "gemm_tc"]
+        out = np.zeros(len(kinds) + 2)
         _check(lib().wt3d_profile_factor(self._h, _ptr(out)))
-        kinds = ["memset", "scatter", "extend_add", "panel", "trsm", "gemm", "diag_solve"]
         d = {k + "_ms": float(out[i]) for i, k in enumerate(kinds)}
-        d["gemm_flops"] = float(out[7])
-        d["gemm_launches"] = int(out[8])
+        d["gemm_flops"] = float(out[len(kinds)])
+        d["gemm_launches"] = int(out[len(kinds) + 1])
         return d
 
     def stats(self):

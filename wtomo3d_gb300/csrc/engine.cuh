@@ -3,55 +3,21 @@
 #pragma once
 #include "internal.h"
 #include "mf_kernels.cuh"
+#include "devvec.cuh"
+#include "tc_gemm.h"
+#include <type_traits>
+#include <cstdlib>
 #include <functional>
 #include <map>
 #include <memory>
 
 namespace wt3d {
 
-template <class T>
-struct DevVec {
-    T *p = nullptr;
-    size_t n = 0;
-    int alloc(size_t count)
-    {
-        free();
-        if (count == 0) return WT3D_OK;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-        if (e != cudaSuccess) {
-            p = nullptr;
-            set_error(std::string("cudaMalloc(") + std::to_string(count * sizeof(T)) + " B): " + cudaGetErrorString(e));
-            return WT3D_ERR_NOMEM;
-        }
-        n = count;
-        return WT3D_OK;
-    }
-    int upload(const std::vector<T> &v)
-    {
-        int rc = alloc(v.size());
-        if (rc) return rc;
-        if (!v.empty() && cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) {
-            set_error("upload failed");
-            return WT3D_ERR_CUDA;
-        }
-        return WT3D_OK;
-    }
-    void free()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    ~DevVec() { free(); }
-    DevVec() = default;
-    DevVec(const DevVec &) = delete;
-    DevVec &operator=(const DevVec &) = delete;
-};
-
 using Launch = std::function<void(cudaStream_t)>;
 
 // Launch kinds, for the per-kernel profile.
-enum LaunchKind { LK_MEMSET = 0, LK_SCATTER, LK_EXTEND_ADD, LK_PANEL, LK_TRSM, LK_GEMM, LK_DIAG, LK_NKINDS };
+enum LaunchKind { LK_MEMSET = 0, LK_SCATTER, LK_EXTEND_ADD, LK_PANEL, LK_TRSM, LK_GEMM, LK_DIAG, LK_SPLIT,
+                  LK_TCGEMM, LK_NKINDS };
 
 struct LaunchRec {
     Launch fn;
@@ -74,6 +40,8 @@ struct Schedule {
     DevVec<ColTask> col;
     DevVec<GemmTask<T>> gemm;
     DevVec<EATask> ea;
+    std::vector<std::vector<GemmTask<float>>> tc_pending;   // tensor-core task lists, built after allocation
+    std::vector<std::unique_ptr<TcLaunch>> tc;
     cudaGraphExec_t graph = nullptr;
     ~Schedule()
     {
@@ -94,7 +62,12 @@ public:
     DevVec<unsigned long long> maxabs;
     std::unique_ptr<Schedule<T>> fsched;
     std::map<int, std::unique_ptr<Schedule<T>>> ssched[2];   // [adjoint][m]
-    double pivot_rel = 1e-20;   // only (near-)zero pivots are replaced: Dirichlet rows carry unit pivots next to O(1e8) stiffness entries
+    double pivot_rel = 1e-20;
+    // tcgen05 path for complex64 front updates (WT3D_TC=0 selects the SIMT kernel)
+    bool use_tc = std::is_same<T, float>::value && !(getenv("WT3D_TC") && getenv("WT3D_TC")[0] == '0');
+    DevVec<float> tcws;                                 // tensor-core split-operand workspace
+    DevVec<int> tc_err;                                 // barrier-timeout flag of the tensor-core kernel
+    std::vector<Schedule<T> *> built_tc;   // only (near-)zero pivots are replaced: Dirichlet rows carry unit pivots next to O(1e8) stiffness entries
     bool use_graphs = true;
 
     size_t device_bytes() const
@@ -123,6 +96,9 @@ public:
         if ((rc = npert.alloc(1))) return rc;
         if ((rc = maxabs.alloc(1))) return rc;
         if ((rc = scale.alloc(sym.n))) return rc;
+        if ((rc = tc_err.alloc(1))) return rc;
+        WT_CUDA(cudaMemset(tc_err.p, 0, sizeof(int)));
+        if (use_tc && (rc = tc_init())) return rc;
         std::vector<FrontDev> h(sym.fronts.size());
         for (size_t f = 0; f < h.size(); f++) {
             const Front &F = sym.fronts[f];
@@ -166,21 +142,79 @@ public:
         v.push_back(g);
     }
 
-    // Appends a gemm launch over tasks [b, e) with local tile numbering.
-    static void push_gemm_launch(Schedule<T> &sc, std::vector<GemmTask<T>> &all, size_t b, long long tiles)
+    // Appends the launches for GEMM tasks [b, end) of `all`: tasks the
+    // tensor-core kernel takes (complex64 path) go to a tcgen05 launch, the
+    // rest to the SIMT kernel with tile numbering rebased to the launch.
+    void push_gemm_launch(Schedule<T> &sc, std::vector<GemmTask<T>> &all, size_t b, long long /*tiles*/)
     {
         if (all.size() == b) return;
-        // rebase tile0 to the launch
-        long long t0 = all[b].tile0;
-        for (size_t i = b; i < all.size(); i++) all[i].tile0 -= t0;
-        int nt = (int)(all.size() - b);
-        long long ntiles = tiles - t0;
-        Schedule<T> *psc = &sc;
+        std::vector<GemmTask<T>> simt;
+        if constexpr (std::is_same<T, float>::value) {
+            std::vector<GemmTask<float>> tcv;
+            for (size_t i = b; i < all.size(); i++) {
+                if (use_tc && tc_eligible(all[i])) tcv.push_back(all[i]);
+                else simt.push_back(all[i]);
+            }
+            if (!tcv.empty()) {
+                double fl = 0;
+                for (auto &g : tcv) fl += 8.0 * g.M * (double)g.N * g.K;
+                const int idx = (int)sc.tc_pending.size();
+                sc.tc_pending.push_back(std::move(tcv));
+                Schedule<T> *psc = &sc;
+                sc.launches.push_back({[psc, idx](cudaStream_t st) { tc_split(*psc->tc[idx], st); }, LK_SPLIT, 0});
+                sc.launches.push_back({[psc, idx, this](cudaStream_t st) { tc_mma(*psc->tc[idx], tc_err.p, st); },
+                                       LK_TCGEMM, fl});
+            }
+        } else {
+            simt.assign(all.begin() + b, all.end());
+        }
+        all.resize(b);
+        if (simt.empty()) return;
+        long long tiles = 0;
         double fl = 0;
-        for (size_t i = b; i < all.size(); i++) fl += 8.0 * all[i].M * (double)all[i].N * all[i].K;
-        sc.launches.push_back({[psc, b, nt, ntiles](cudaStream_t st) {
-            k_gemm<T><<<(unsigned)ntiles, 256, 0, st>>>(psc->gemm.p + b, nt);
+        for (auto &g : simt) {
+            g.tile0 = tiles;
+            tiles += (long long)((g.M + GBM - 1) / GBM) * g.tiles_n;
+            fl += 8.0 * g.M * (double)g.N * g.K;
+            all.push_back(g);
+        }
+        const int nt = (int)simt.size();
+        Schedule<T> *psc = &sc;
+        sc.launches.push_back({[psc, b, nt, tiles](cudaStream_t st) {
+            k_gemm<T><<<(unsigned)tiles, 256, 0, st>>>(psc->gemm.p + b, nt);
         }, LK_GEMM, fl});
+    }
+
+    // Allocates the shared tensor-core workspace and builds the tensor maps of
+    // every pending tensor-core launch of a schedule.
+    int finish_tc(Schedule<T> &sc)
+    {
+        if constexpr (std::is_same<T, float>::value) {
+            long long need = 0;
+            for (auto &v : sc.tc_pending) need = std::max(need, tc_workspace_floats(v.data(), (int)v.size()));
+            if (need > (long long)tcws.n) {
+                int rc = tcws.alloc(need);
+                if (rc) return rc;
+                // schedules built earlier point into the old workspace: rebuild their maps
+                for (auto *o : built_tc) {
+                    for (size_t i = 0; i < o->tc_pending.size(); i++) {
+                        o->tc[i].reset(new TcLaunch());
+                        if ((rc = tc_build_launch(*o->tc[i], o->tc_pending[i].data(), (int)o->tc_pending[i].size(),
+                                                  tcws.p)))
+                            return rc;
+                    }
+                    if (o->graph) { cudaGraphExecDestroy(o->graph); o->graph = nullptr; }
+                }
+            }
+            sc.tc.clear();
+            for (auto &v : sc.tc_pending) {
+                sc.tc.emplace_back(new TcLaunch());
+                int rc = tc_build_launch(*sc.tc.back(), v.data(), (int)v.size(), tcws.p);
+                if (rc) return rc;
+            }
+            built_tc.push_back(&sc);
+        }
+        return WT3D_OK;
     }
 
     int build_factor_schedule()
@@ -301,6 +335,7 @@ public:
         if ((rc = sc->col.upload(hc))) return rc;
         if ((rc = sc->gemm.upload(hg))) return rc;
         if ((rc = sc->ea.upload(he))) return rc;
+        if ((rc = finish_tc(*sc))) return rc;
         fsched = std::move(sc);
         return WT3D_OK;
     }
@@ -422,7 +457,7 @@ public:
                 }
             }
         }
-        if (sc->panel.upload(hp) || sc->gemm.upload(hg)) return nullptr;
+        if (sc->panel.upload(hp) || sc->gemm.upload(hg) || finish_tc(*sc)) return nullptr;
         Schedule<T> *ret = sc.get();
         ssched[adjoint][m] = std::move(sc);
         return ret;
@@ -476,7 +511,7 @@ public:
             float ms = 0;
             cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
             out[fsched->launches[i].kind] += ms;
-            if (fsched->launches[i].kind == LK_GEMM) {
+            if (fsched->launches[i].kind == LK_GEMM || fsched->launches[i].kind == LK_TCGEMM) {
                 out[LK_NKINDS] += fsched->launches[i].flops;
                 out[LK_NKINDS + 1] += 1;
             }

@@ -83,7 +83,7 @@ __global__ void k_scatter(long long n, const int *__restrict__ irptr, const int 
     }
 }
 
-__global__ void k_jacobi_scale(long long n, const int *__restrict__ irptr, const int *__restrict__ jcptr,
+static __global__ void k_jacobi_scale(long long n, const int *__restrict__ irptr, const int *__restrict__ jcptr,
                                const double2 *__restrict__ a, double *__restrict__ s)
 {
     long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -94,7 +94,7 @@ __global__ void k_jacobi_scale(long long n, const int *__restrict__ irptr, const
     s[r] = (d > 0 && d < INFINITY) ? 1.0 / sqrt(d) : 1.0;
 }
 
-__global__ void k_maxabs(long long n, const double2 *__restrict__ a, unsigned long long *out)
+static __global__ void k_maxabs(long long n, const double2 *__restrict__ a, unsigned long long *out)
 {
     double m = 0;
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {

@@ -1,0 +1,563 @@
+// Complex64 GEMM  C -= A * B  on the 5th-generation tensor cores (tcgen05) of
+// sm_103a, accurate to FP32 through a three-term TF32 split.
+//
+// Complex product as one real GEMM: with A stored interleaved (row i =
+// [re a_i0, im a_i0, re a_i1, ...], i.e. an M x 2K real matrix, K-major as
+// stored) and B expanded to the 2N x 2K K-major real matrix
+//     row 2j   = [ re b_0j, -im b_0j,  re b_1j, -im b_1j, ...]
+//     row 2j+1 = [ im b_0j,  re b_0j,  im b_1j,  re b_1j, ...]
+// the real product A_r * B~^T is the interleaved complex C (8 real flops per
+// complex multiply-add, nothing wasted).
+//
+// Precision: each operand x is split as hi = rn_tf32(x), lo = rn_tf32(x - hi),
+// both exact TF32 values with x = hi + lo to ~2^-24 relative;
+// D = Ahi Bhi + Ahi Blo + Alo Bhi in an FP32 TMEM accumulator gives an
+// FP32-class product (the dropped Alo Blo term is ~2^-24 relative).
+//
+// Kernel structure (one 128 x 128-complex output tile per CTA, 6 warps):
+//   warp 0      TMA producer (cp.async.bulk.tensor, SWIZZLE_128B tiles) and
+//               TMEM allocator;
+//   warp 1      single-thread tcgen05.mma issuer (kind::tf32, M=128, N=256),
+//               tcgen05.commit releases smem stages and signals the epilogue;
+//   warps 2..5  epilogue: tcgen05.ld of the 128 x 256 FP32 accumulator,
+//               C -= D with 128-byte row segments.
+// Every mbarrier wait has an iteration limit; on expiry the kernel records an
+// error code, skips ahead, frees its TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include "tc_gemm.h"
+#include <cstring>
+
+namespace wt3d {
+
+constexpr int TC_BM = 128;                 // complex rows per tile
+constexpr int TC_BNR = 256;                // real columns per tile (128 complex)
+constexpr int TC_BK = 32;                  // real k per stage (128 bytes of FP32)
+constexpr int TC_STAGES = 2;
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 4;     // 16 KB
+constexpr int TC_B_BYTES = TC_BNR * TC_BK * 4;    // 32 KB
+constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;
+constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
+constexpr int TC_THREADS = 192;
+constexpr unsigned TC_WAIT_LIMIT = 1u << 24;
+
+// ---------------------------------------------------------------------------
+// PTX helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Bounded wait for the phase with the given parity; returns false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    const uint32_t a = smem_u32(bar);
+    for (unsigned it = 0; it < TC_WAIT_LIMIT; it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// K-major operand tile in the 128-byte-swizzle canonical layout: 8-row atoms
+// of 128-byte rows, atoms 1024 bytes apart along M/N.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);        // start address
+    d |= (uint64_t)1 << 16;                           // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;                 // stride byte offset between 8-row atoms
+    d |= (uint64_t)1 << 46;                           // descriptor version (sm_100 family)
+    d |= (uint64_t)2 << 61;                           // swizzle: 128B
+    return d;
+}
+
+// kind::tf32 instruction descriptor: FP32 accumulate, TF32 A and B, both
+// K-major, M = 128, N = 256.
+__host__ __device__ constexpr uint32_t tf32_idesc(int M, int N)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+#define TMEM_LD32(taddr, v)                                                                                       \
+    asm volatile(                                                                                                 \
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18," \
+        "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"                                            \
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),          \
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),   \
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), \
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])  \
+        : "r"(taddr))
+
+// ---------------------------------------------------------------------------
+// operand split / expansion pre-pass
+// ---------------------------------------------------------------------------
+// Round to the nearest TF32 value (10 explicit mantissa bits), ties to even.
+__device__ __forceinline__ float rn_tf32(float x)
+{
+    uint32_t u = __float_as_uint(x);
+    if ((u & 0x7F800000u) == 0x7F800000u) return x;          // inf / nan unchanged
+    u += 0xFFFu + ((u >> 13) & 1u);
+    return __uint_as_float(u & 0xFFFFE000u);
+}
+
+// x = hi + lo + O(2^-24 |x|) with hi and lo both exact TF32 values, so the
+// tensor core's reading of the operands loses nothing.
+__device__ __forceinline__ void split_tf32(float x, float &hi, float &lo)
+{
+    hi = rn_tf32(x);
+    lo = rn_tf32(x - hi);
+}
+
+// One thread per (row, complex k) of A: Ahi/Alo rows of Kr floats.
+__global__ void k_split_a(const TcTask *__restrict__ tasks, int ntasks, long long total)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= total) return;
+    int lo_t = 0, hi_t = ntasks - 1;
+    while (lo_t < hi_t) {
+        int mid = (lo_t + hi_t + 1) >> 1;
+        if (tasks[mid].a_work0 <= q) lo_t = mid;
+        else hi_t = mid - 1;
+    }
+    const TcTask &t = tasks[lo_t];
+    const long long r = q - t.a_work0;
+    const int kc = t.Kr / 2;
+    const int i = (int)(r / kc), k = (int)(r % kc);
+    cx<float> v(0.f, 0.f);
+    if (k < t.K) v = t.A[(long long)i * t.lda + k];
+    float h0, l0, h1, l1;
+    split_tf32(v.re, h0, l0);
+    split_tf32(v.im, h1, l1);
+    const long long o = (long long)i * t.Kr + 2 * k;
+    *reinterpret_cast<float2 *>(t.ahi + o) = make_float2(h0, h1);
+    *reinterpret_cast<float2 *>(t.alo + o) = make_float2(l0, l1);
+}
+
+// 32 x 32 complex tiles of B (k x j) transposed through shared memory into the
+// expanded K-major rows 2j, 2j+1 of B~.
+__global__ void __launch_bounds__(256) k_split_b(const TcTask *__restrict__ tasks, int ntasks, long long total_tiles)
+{
+    __shared__ float2 tile[32][33];
+    long long q = blockIdx.x;
+    if (q >= total_tiles) return;
+    int lo_t = 0, hi_t = ntasks - 1;
+    while (lo_t < hi_t) {
+        int mid = (lo_t + hi_t + 1) >> 1;
+        if (tasks[mid].b_work0 <= q) lo_t = mid;
+        else hi_t = mid - 1;
+    }
+    const TcTask &t = tasks[lo_t];
+    const long long r = q - t.b_work0;
+    const int kt = t.Kr / 64;                 // 32-complex k tiles
+    const int j0 = (int)(r / kt) * 32, k0 = (int)(r % kt) * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+    for (int kk = ty; kk < 32; kk += 8) {
+        int k = k0 + kk, j = j0 + tx;
+        cx<float> v(0.f, 0.f);
+        if (k < t.K && j < t.N) v = t.B[(long long)k * t.ldb + j];
+        tile[kk][tx] = make_float2(v.re, v.im);
+    }
+    __syncthreads();
+    for (int jj = ty; jj < 32; jj += 8) {
+        const int j = j0 + jj;
+        if (j >= t.N) continue;
+        const float2 bt = tile[tx][jj];
+        const cx<float> b(bt.x, bt.y);
+        const int k = k0 + tx;
+        float rh, rl, ih, il, nih, nil;
+        split_tf32(b.re, rh, rl);
+        split_tf32(b.im, ih, il);
+        split_tf32(-b.im, nih, nil);
+        const long long o0 = (long long)(2 * j) * t.Kr + 2 * k, o1 = o0 + t.Kr;
+        *reinterpret_cast<float2 *>(t.bhi + o0) = make_float2(rh, nih);
+        *reinterpret_cast<float2 *>(t.blo + o0) = make_float2(rl, nil);
+        *reinterpret_cast<float2 *>(t.bhi + o1) = make_float2(ih, rh);
+        *reinterpret_cast<float2 *>(t.blo + o1) = make_float2(il, rl);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the tensor-core kernel
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_tc_gemm(const TcTask *__restrict__ tasks, int ntasks, const CUtensorMap *__restrict__ maps, int *err)
+{
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE_BYTES);
+    uint64_t *empty = full + TC_STAGES;
+    uint64_t *accum = empty + TC_STAGES;
+    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(accum + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long gt = blockIdx.x;
+    int lo_t = 0, hi_t = ntasks - 1;
+    while (lo_t < hi_t) {
+        int mid = (lo_t + hi_t + 1) >> 1;
+        if (tasks[mid].tile0 <= gt) lo_t = mid;
+        else hi_t = mid - 1;
+    }
+    const TcTask &t = tasks[lo_t];
+    const long long lt = gt - t.tile0;
+    const int m0 = (int)(lt / t.tiles_n) * TC_BM;
+    const int n0r = (int)(lt % t.tiles_n) * TC_BNR;
+    const int nk = t.Kr / TC_BK;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
+                     "r"(256));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (threadIdx.x == 32) {
+        for (int s = 0; s < TC_STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accum, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = *tmem_holder;
+
+    if (warp == 0 && lane == 0) {
+        // ---------------- TMA producer ----------------
+        const CUtensorMap *mp = maps + t.map0;
+        for (int ks = 0; ks < nk; ks++) {
+            const int s = ks % TC_STAGES;
+            const uint32_t ph = ((ks / TC_STAGES) & 1) ^ 1;
+            if (!mbar_wait(&empty[s], ph)) atomicCAS(err, 0, 1);
+            uint8_t *st = smem + s * TC_STAGE_BYTES;
+            mbar_expect_tx(&full[s], TC_STAGE_BYTES);
+            tma_load_2d(st, mp + 0, ks * TC_BK, m0, &full[s]);
+            tma_load_2d(st + TC_A_BYTES, mp + 1, ks * TC_BK, m0, &full[s]);
+            tma_load_2d(st + 2 * TC_A_BYTES, mp + 2, ks * TC_BK, n0r, &full[s]);
+            tma_load_2d(st + 2 * TC_A_BYTES + TC_B_BYTES, mp + 3, ks * TC_BK, n0r, &full[s]);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // ---------------- MMA issuer ----------------
+        constexpr uint32_t idesc = tf32_idesc(TC_BM, TC_BNR);
+        for (int ks = 0; ks < nk; ks++) {
+            const int s = ks % TC_STAGES;
+            const uint32_t ph = (ks / TC_STAGES) & 1;
+            if (!mbar_wait(&full[s], ph)) atomicCAS(err, 0, 2);
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t base = smem_u32(smem + s * TC_STAGE_BYTES);
+            const uint32_t a_hi = base, a_lo = base + TC_A_BYTES;
+            const uint32_t b_hi = base + 2 * TC_A_BYTES, b_lo = b_hi + TC_B_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < TC_BK / 8; kk++) {
+                const uint32_t off = kk * 32;   // 8 TF32 elements = 32 bytes along K
+                const uint64_t dah = sw128_desc(a_hi + off), dal = sw128_desc(a_lo + off);
+                const uint64_t dbh = sw128_desc(b_hi + off), dbl = sw128_desc(b_lo + off);
+                umma_tf32(tmem, dah, dbh, idesc, (ks | kk) != 0);
+                umma_tf32(tmem, dah, dbl, idesc, 1);
+                umma_tf32(tmem, dal, dbh, idesc, 1);
+            }
+            umma_commit(&empty[s]);
+        }
+        umma_commit(accum);
+    } else if (warp >= 2) {
+        // ---------------- epilogue ----------------
+        if (!mbar_wait(accum, 0)) atomicCAS(err, 0, 3);
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const int q = warp & 3;                 // TMEM lane quarter this warp may access
+        const int row = m0 + 32 * q + lane;
+        const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16);
+        cx<float> *crow = t.C + (long long)row * t.ldc;
+        const int c0 = n0r / 2;
+#pragma unroll 1
+        for (int ch = 0; ch < TC_BNR / 32; ch++) {
+            uint32_t v[32];
+            TMEM_LD32(tq + ch * 32, v);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            if (row < t.M) {
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    const int c = c0 + ch * 16 + i;
+                    if (c < t.N) {
+                        cx<float> o = crow[c];
+                        o.re -= __uint_as_float(v[2 * i]);
+                        o.im -= __uint_as_float(v[2 * i + 1]);
+                        crow[c] = o;
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+static int make_map(CUtensorMap *m, float *base, long long rows, int Kr, int box_rows)
+{
+    auto fn = encode_fn();
+    if (!fn) { set_error("cuTensorMapEncodeTiled unavailable"); return WT3D_ERR_CUDA; }
+    cuuint64_t gdim[2] = {(cuuint64_t)Kr, (cuuint64_t)rows};
+    cuuint64_t gstr[1] = {(cuuint64_t)Kr * 4};
+    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, gdim, gstr, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+        return WT3D_ERR_CUDA;
+    }
+    return WT3D_OK;
+}
+
+static long long align_up(long long x, long long a) { return (x + a - 1) / a * a; }
+
+long long tc_workspace_floats(const GemmTask<float> *g, int n)
+{
+    long long w = 0;
+    for (int i = 0; i < n; i++) {
+        const long long Kr = align_up(2LL * g[i].K, 2 * TC_BK);
+        w += align_up((long long)g[i].M * Kr, 256) * 2 + align_up(2LL * g[i].N * Kr, 256) * 2;
+    }
+    return w;
+}
+
+bool tc_eligible(const GemmTask<float> &g)
+{
+    return !g.brow && !g.crow && !g.conjA && g.M >= 32 && g.N >= 32 && g.K >= 8;
+}
+
+int tc_build_launch(TcLaunch &L, const GemmTask<float> *g, int n, float *ws)
+{
+    std::vector<TcTask> tasks(n);
+    std::vector<CUtensorMap> maps(4 * n);
+    long long off = 0, tiles = 0, aw = 0, bw = 0;
+    for (int i = 0; i < n; i++) {
+        TcTask &t = tasks[i];
+        t.A = g[i].A; t.lda = g[i].lda;
+        t.B = g[i].B; t.ldb = g[i].ldb;
+        t.C = g[i].C; t.ldc = g[i].ldc;
+        t.M = g[i].M; t.N = g[i].N; t.K = g[i].K;
+        t.Kr = (int)align_up(2LL * t.K, 2 * TC_BK);   // whole 32-complex tiles for the B transpose
+        const long long asz = align_up((long long)t.M * t.Kr, 256), bsz = align_up(2LL * t.N * t.Kr, 256);
+        t.ahi = ws + off; off += asz;
+        t.alo = ws + off; off += asz;
+        t.bhi = ws + off; off += bsz;
+        t.blo = ws + off; off += bsz;
+        t.tiles_n = (int)((2LL * t.N + TC_BNR - 1) / TC_BNR);
+        t.tile0 = tiles;
+        tiles += (long long)((t.M + TC_BM - 1) / TC_BM) * t.tiles_n;
+        t.a_work0 = aw;
+        aw += (long long)t.M * (t.Kr / 2);
+        t.b_work0 = bw;
+        bw += (long long)((t.N + 31) / 32) * (t.Kr / 64);
+        t.map0 = 4 * i;
+        int rc;
+        if ((rc = make_map(&maps[4 * i + 0], t.ahi, t.M, t.Kr, TC_BM)) ||
+            (rc = make_map(&maps[4 * i + 1], t.alo, t.M, t.Kr, TC_BM)) ||
+            (rc = make_map(&maps[4 * i + 2], t.bhi, 2LL * t.N, t.Kr, TC_BNR)) ||
+            (rc = make_map(&maps[4 * i + 3], t.blo, 2LL * t.N, t.Kr, TC_BNR)))
+            return rc;
+    }
+    L.ntasks = n;
+    L.tiles = tiles;
+    L.a_work = aw;
+    L.b_tiles = bw;
+    int rc;
+    if ((rc = L.tasks.upload(tasks))) return rc;
+    std::vector<unsigned char> raw(maps.size() * sizeof(CUtensorMap));
+    memcpy(raw.data(), maps.data(), raw.size());
+    if ((rc = L.maps.upload(raw))) return rc;
+    return WT3D_OK;
+}
+
+void tc_split(const TcLaunch &L, cudaStream_t st)
+{
+    if (L.ntasks == 0) return;
+    k_split_a<<<ceil_div(L.a_work, 256), 256, 0, st>>>(L.tasks.p, L.ntasks, L.a_work);
+    k_split_b<<<(unsigned)L.b_tiles, 256, 0, st>>>(L.tasks.p, L.ntasks, L.b_tiles);
+}
+
+void tc_mma(const TcLaunch &L, int *err, cudaStream_t st)
+{
+    if (L.ntasks == 0) return;
+    k_tc_gemm<<<(unsigned)L.tiles, TC_THREADS, TC_SMEM, st>>>(L.tasks.p, L.ntasks,
+                                                              reinterpret_cast<const CUtensorMap *>(L.maps.p), err);
+}
+
+int tc_init()
+{
+    static bool done = false;
+    if (done) return WT3D_OK;
+    WT_CUDA(cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    if (!encode_fn()) { set_error("cuTensorMapEncodeTiled unavailable"); return WT3D_ERR_CUDA; }
+    done = true;
+    return WT3D_OK;
+}
+
+}  // namespace wt3d
+
+// ---------------------------------------------------------------------------
+// C ABI check entry: one GEMM C -= A B on host complex64 arrays (row-major),
+// through the tensor-core path (path = 1) or the SIMT path (path = 0).
+// ---------------------------------------------------------------------------
+using namespace wt3d;
+extern "C" int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int lda, const void *B, int ldb, void *C,
+                               int ldc)
+{
+    DevVec<cx<float>> dA, dB, dC;
+    int rc;
+    if ((rc = dA.alloc((size_t)M * lda)) || (rc = dB.alloc((size_t)K * ldb)) || (rc = dC.alloc((size_t)M * ldc)))
+        return rc;
+    WT_CUDA(cudaMemcpy(dA.p, A, sizeof(cx<float>) * M * lda, cudaMemcpyHostToDevice));
+    WT_CUDA(cudaMemcpy(dB.p, B, sizeof(cx<float>) * K * ldb, cudaMemcpyHostToDevice));
+    WT_CUDA(cudaMemcpy(dC.p, C, sizeof(cx<float>) * M * ldc, cudaMemcpyHostToDevice));
+    GemmTask<float> g{};
+    g.A = dA.p; g.B = dB.p; g.C = dC.p; g.lda = lda; g.ldb = ldb; g.ldc = ldc; g.M = M; g.N = N; g.K = K;
+    g.tiles_n = (N + GBN - 1) / GBN;
+    g.tile0 = 0;
+    DevVec<int> err;
+    if ((rc = err.alloc(1))) return rc;
+    WT_CUDA(cudaMemset(err.p, 0, sizeof(int)));
+    if (path == 1) {
+        if ((rc = tc_init())) return rc;
+        DevVec<float> ws;
+        if ((rc = ws.alloc(tc_workspace_floats(&g, 1)))) return rc;
+        TcLaunch L;
+        if ((rc = tc_build_launch(L, &g, 1, ws.p))) return rc;
+        tc_split(L, 0);
+        tc_mma(L, err.p, 0);
+    } else {
+        DevVec<GemmTask<float>> dt;
+        std::vector<GemmTask<float>> v{g};
+        if ((rc = dt.upload(v))) return rc;
+        long long tiles = (long long)((M + GBM - 1) / GBM) * g.tiles_n;
+        k_gemm<float><<<(unsigned)tiles, 256>>>(dt.p, 1);
+    }
+    WT_CUDA(cudaGetLastError());
+    WT_CUDA(cudaDeviceSynchronize());
+    int herr = 0;
+    WT_CUDA(cudaMemcpy(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) { set_error("tensor-core GEMM barrier wait expired (code " + std::to_string(herr) + ")"); return WT3D_ERR_CUDA; }
+    WT_CUDA(cudaMemcpy(C, dC.p, sizeof(cx<float>) * M * ldc, cudaMemcpyDeviceToHost));
+    return WT3D_OK;
+}
+
+// Device-resident GEMM timing (operands filled on the device): avg ms of
+// `iters` launches of C -= A B with M x K, K x N complex64 row-major operands.
+static __global__ void k_fill(cx<float> *p, long long n, unsigned seed)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned h = (unsigned)(i * 2654435761u) ^ seed;
+    h ^= h >> 13; h *= 0x5bd1e995u; h ^= h >> 15;
+    p[i] = cx<float>((float)(h & 0xFFFF) / 65536.0f - 0.5f, (float)(h >> 16) / 65536.0f - 0.5f);
+}
+
+extern "C" int wt3d_bench_gemm(int path, int M, int N, int K, int iters, double *ms_out)
+{
+    DevVec<cx<float>> dA, dB, dC;
+    int rc;
+    if ((rc = dA.alloc((size_t)M * K)) || (rc = dB.alloc((size_t)K * N)) || (rc = dC.alloc((size_t)M * N))) return rc;
+    k_fill<<<ceil_div((long long)M * K, 256), 256>>>(dA.p, (long long)M * K, 1);
+    k_fill<<<ceil_div((long long)K * N, 256), 256>>>(dB.p, (long long)K * N, 2);
+    k_fill<<<ceil_div((long long)M * N, 256), 256>>>(dC.p, (long long)M * N, 3);
+    GemmTask<float> g{};
+    g.A = dA.p; g.B = dB.p; g.C = dC.p; g.lda = K; g.ldb = N; g.ldc = N; g.M = M; g.N = N; g.K = K;
+    g.tiles_n = (N + GBN - 1) / GBN;
+    DevVec<int> err;
+    if ((rc = err.alloc(1))) return rc;
+    WT_CUDA(cudaMemset(err.p, 0, sizeof(int)));
+    DevVec<float> ws;
+    TcLaunch L;
+    DevVec<GemmTask<float>> dt;
+    if (path == 1) {
+        if ((rc = tc_init()) || (rc = ws.alloc(tc_workspace_floats(&g, 1))) || (rc = tc_build_launch(L, &g, 1, ws.p)))
+            return rc;
+        tc_split(L, 0);
+    } else {
+        std::vector<GemmTask<float>> v{g};
+        if ((rc = dt.upload(v))) return rc;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const long long tiles = (long long)((M + GBM - 1) / GBM) * g.tiles_n;
+    for (int w = 0; w < 2; w++) {   // warm-up
+        if (path == 1) tc_mma(L, err.p, 0);
+        else k_gemm<float><<<(unsigned)tiles, 256>>>(dt.p, 1);
+    }
+    cudaEventRecord(e0);
+    for (int i = 0; i < iters; i++) {
+        if (path == 1) tc_mma(L, err.p, 0);
+        else k_gemm<float><<<(unsigned)tiles, 256>>>(dt.p, 1);
+    }
+    cudaEventRecord(e1);
+    WT_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    *ms_out = ms / iters;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    WT_CUDA(cudaGetLastError());
+    int herr = 0;
+    WT_CUDA(cudaMemcpy(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    return herr ? WT3D_ERR_CUDA : WT3D_OK;
+}

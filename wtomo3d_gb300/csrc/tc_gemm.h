@@ -1,0 +1,34 @@
+// Tensor-core (tcgen05, 3xTF32) complex64 GEMM: host interface.
+#pragma once
+#include "mf_kernels.cuh"
+#include "devvec.cuh"
+
+namespace wt3d {
+
+// One GEMM of a tensor-core launch (complex dims; Kr = real K padded to 32).
+struct TcTask {
+    const cx<float> *A;
+    const cx<float> *B;
+    cx<float> *C;
+    float *ahi, *alo, *bhi, *blo;   // split operands in the launch workspace
+    int lda, ldb, ldc, M, N, K, Kr;
+    int tiles_n;
+    int map0;                       // first of this task's 4 tensor maps
+    long long tile0, a_work0, b_work0;
+};
+
+struct TcLaunch {
+    DevVec<TcTask> tasks;
+    DevVec<unsigned char> maps;    // CUtensorMap array (4 per task)
+    int ntasks = 0;
+    long long tiles = 0, a_work = 0, b_tiles = 0;
+};
+
+int tc_init();
+bool tc_eligible(const GemmTask<float> &g);
+long long tc_workspace_floats(const GemmTask<float> *g, int n);
+int tc_build_launch(TcLaunch &L, const GemmTask<float> *g, int n, float *ws);
+void tc_split(const TcLaunch &L, cudaStream_t st);
+void tc_mma(const TcLaunch &L, int *err, cudaStream_t st);
+
+}  // namespace wt3d
