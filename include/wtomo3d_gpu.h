@@ -86,6 +86,21 @@ int wt3d_assemble_device(const wt3d_grid *g, const float *d_vp, const float *d_v
                          const float *d_rho, double omega_re, double omega_im,
                          const int *d_irptr, void *d_a, void *stream);
 
+/* ---- plane-wave sources ------------------------------------------------
+ * Layered 1-D medium for the Thomson-Haskell response: nl >= 2 layers, layer
+ * nl is the half-space; ztop[0] = 0 and ztop[i] is the depth (m) of the top of
+ * layer i+1 (HASKELL_MODULE vp1d/vs1d/rh1d/h1d, modules.F90:204-213). */
+typedef struct wt3d_layered1d {
+    int nl;
+    const double *vp, *vs, *rho, *ztop;
+} wt3d_layered1d;
+
+/* HASKGRN (haskgrn.f:31-672): response U(z), W(z) at the nz node depths
+ * zorig + dz*(iz-1) to a unit P (s_wave = 0) or S plane wave of incidence
+ * angle ain (radians) at angular frequency omega.  Host, FP64. */
+int wt3d_haskgrn(const wt3d_layered1d *m, double omega, double ain, int s_wave, int nz, double dz,
+                 double zorig, double _Complex *U, double _Complex *W);
+
 /* ---- handle-based solver (re-entrant siblings of the job protocol) ------ */
 typedef struct wt3d_solver wt3d_solver;
 
@@ -105,6 +120,20 @@ int wt3d_factor(wt3d_solver *h, double omega_re, double omega_im);
  * (strumpack_finter.c:68-92). */
 int wt3d_set_values_c64(wt3d_solver *h, const float _Complex *a);
 int wt3d_factor_values(wt3d_solver *h);
+
+/* Background model (host floats, (nz,nx,ny)) of the scattered-field sources:
+ * the dap/mup/rhop arrays SETCOEFS3D reads with ibg = 1 (setcoefs3d.f:98-101). */
+int wt3d_set_background(wt3d_solver *h, const float *vp, const float *vs, const float *rho);
+
+/* Plane-wave scattered-field sources at the last factored omega, replacing
+ * haskgrn + plane-wave expansion + hetfldsrc (hetfldsrc.f90:17-1038):
+ *   u0_j = [U_j(z) rx, U_j(z) ry, W_j(z)] exp(i omega p_j (x rx + y ry)),
+ *   (rx, ry) = -(cos baz_j, sin baz_j), p_j = sin(ain_j) / v_halfspace,
+ *   f_j = (A_bg - A) u0_j   (source spectrum 1, srcin = 3).
+ * d_F: device complex128, column-major n x nsrc.  d_U0 (optional, may be NULL):
+ * device complex128 column-major n x nsrc receiving u0. */
+int wt3d_rhs_planewave(wt3d_solver *h, const wt3d_layered1d *m, int nsrc, const double *ain,
+                       const double *baz, const int *s_wave, void *d_F, void *d_U0);
 
 /* Solve A X = B for nrhs right-hand sides (host arrays, column k of B at
  * B + k*n, complex128).  Mixed precision refines in FP64 until every column

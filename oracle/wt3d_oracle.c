@@ -162,3 +162,154 @@ int ora_node_blocks_c128(const ora_grid *g, const float *vp, const float *vs, co
 {
     return node_blocks_c128(g, vp, vs, rho, omega_re, omega_im, iz, ix, iy, blk, active);
 }
+
+/* ---------------------------------------------------------------------- */
+/* HASKGRN (haskgrn.f:31-672): Thomson-Haskell 1-D response at the nodes   */
+/* iz = 1..nz to a unit incident P (s_wave = 0) or S plane wave.  FP64.    */
+/* Layer tops h1d[0..nl-1] (h1d[0] = 0), layer nl is the half-space;       */
+/* vp1disc = vp1d, vs1disc = vs1d.  Kept quirks of the reference: the      */
+/* layer-entry refresh tests vp1disc(m) / vs1disc(m) with the loop index m */
+/* left over from the previous propagation loop (haskgrn.f:454,466), and   */
+/* nodes below the last interface are placed in layer nl-1 (the layer      */
+/* search ends with i = nl, haskgrn.f:427-434).                            */
+/* ---------------------------------------------------------------------- */
+static void hk_layer_cs(double hc, double r1, double r2, double cv, double vp, double vs,
+                        double *e1, double *c01, double *s01, double *e2, double *c02, double *s02)
+{
+    double z01 = hc * r1, z02 = hc * r2, x;
+    if (cv > vp) { *e1 = 1; *c01 = cos(z01); *s01 = sin(z01); }
+    else { x = exp(z01); *e1 = -1; *c01 = 0.5 * (x + 1. / x); *s01 = 0.5 * (x - 1. / x); }
+    if (cv > vs) { *e2 = 1; *c02 = cos(z02); *s02 = sin(z02); }
+    else { x = exp(z02); *e2 = -1; *c02 = 0.5 * (x + 1. / x); *s02 = 0.5 * (x - 1. / x); }
+}
+
+/* product of the layer matrices of layers 1..top into b (4x2), H53 p.21-23 */
+static void hk_propagate(int top, const double *vs, const double *r1, const double *r2, const double *e1,
+                         const double *e2, const double *c01, const double *s01, const double *c02,
+                         const double *s02, const double *tt, const double *aag, const double *aag1,
+                         const double *xh, const double *xh1, double b[4][2])
+{
+    b[0][0] = 1; b[0][1] = 0; b[1][0] = 0; b[1][1] = 1;
+    b[2][0] = 0; b[2][1] = 0; b[3][0] = 0; b[3][1] = 0;
+    for (int m = 0; m < top; m++) {
+        double pd = s01[m] / r1[m], qd = s02[m] / r2[m];
+        double pm = e1[m] * s01[m] * r1[m], qm = e2[m] * s02[m] * r2[m];
+        double cp = c01[m], cq = c02[m], tm = tt[m], ag = aag[m], ag1 = aag1[m], x = xh[m], y = xh1[m];
+        double a[4][4];
+        if (vs[m] != 0.0) {
+            a[0][0] = ag * cp - ag1 * cq;  a[0][1] = ag1 * pd + ag * qm;
+            a[0][2] = (cq - cp) / tm;      a[0][3] = (pd + qm) / tm;
+            a[1][0] = -ag * pm - ag1 * qd; a[1][1] = ag * cq - ag1 * cp;
+            a[1][2] = (pm + qd) / tm;      a[1][3] = a[0][2];
+            a[2][0] = tm * ag * ag1 * (cp - cq); a[2][1] = tm * (y * pd + x * qm);
+            a[2][2] = a[1][1];             a[2][3] = a[0][1];
+            a[3][0] = tm * (x * pm + y * qd); a[3][1] = a[2][0];
+            a[3][2] = a[1][0];             a[3][3] = a[0][0];
+        } else {
+            for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) a[i][j] = 0;
+            a[0][1] = -pd; a[0][2] = -cp / tm; a[1][1] = cp; a[1][2] = pm / tm;
+            a[2][1] = tm * pd; a[2][2] = cp;
+        }
+        double d[4][2];
+        d[0][0] = a[0][0] * b[0][0] - a[0][1] * b[1][0] + a[0][2] * b[2][0] - a[0][3] * b[3][0];
+        d[0][1] = a[0][0] * b[0][1] + a[0][1] * b[1][1] + a[0][2] * b[2][1] + a[0][3] * b[3][1];
+        d[1][0] = a[1][0] * b[0][0] + a[1][1] * b[1][0] + a[1][2] * b[2][0] + a[1][3] * b[3][0];
+        d[1][1] = -a[1][0] * b[0][1] + a[1][1] * b[1][1] - a[1][2] * b[2][1] + a[1][3] * b[3][1];
+        d[2][0] = a[2][0] * b[0][0] - a[2][1] * b[1][0] + a[2][2] * b[2][0] - a[2][3] * b[3][0];
+        d[2][1] = a[2][0] * b[0][1] + a[2][1] * b[1][1] + a[2][2] * b[2][1] + a[2][3] * b[3][1];
+        d[3][0] = a[3][0] * b[0][0] + a[3][1] * b[1][0] + a[3][2] * b[2][0] + a[3][3] * b[3][0];
+        d[3][1] = -a[3][0] * b[0][1] + a[3][1] * b[1][1] - a[3][2] * b[2][1] + a[3][3] * b[3][1];
+        for (int i = 0; i < 4; i++) { b[i][0] = d[i][0]; b[i][1] = d[i][1]; }
+    }
+}
+
+int ora_haskgrn(int nl, const double *vp, const double *vs, const double *rh, const double *h1d, double omega,
+                double ain, int s_wave, int nz, double dz, double zorig, double complex *ugrn,
+                double complex *wgrn)
+{
+    if (nl < 1 || nl > 64) return 1;
+    double r1[64], r2[64], aag[64], aag1[64], tt[64], xh[64], xh1[64], h[64];
+    double e1[64], e2[64], c01[64], s01[64], c02[64], s02[64];
+    const double cv = (s_wave ? vs[nl - 1] : vp[nl - 1]) / sin(ain);
+    const double pic = omega / cv;
+    for (int i = 0; i < nl - 1; i++) h[i] = h1d[i + 1] - h1d[i];
+    for (int m = 0; m < nl; m++) {
+        double cova = cv / vp[m];
+        double covb = vs[m] != 0.0 ? cv / vs[m] : 1.0;
+        double x = cova * cova - 1.;
+        r1[m] = copysign(sqrt(fabs(x)), x);
+        x = covb * covb - 1.;
+        r2[m] = copysign(sqrt(fabs(x)), x);
+        aag[m] = 2. / (covb * covb);
+        aag1[m] = aag[m] - 1.;
+        if (m < nl - 1) {
+            tt[m] = rh[m] * cv * cv;
+            xh[m] = aag[m] * aag[m];
+            xh1[m] = aag1[m] * aag1[m];
+            hk_layer_cs(pic * h[m], r1[m], r2[m], cv, vp[m], vs[m], &e1[m], &c01[m], &s01[m], &e2[m], &c02[m],
+                        &s02[m]);
+        }
+    }
+    /* scaled inverse E of the half-space (haskgrn.f:201-211) */
+    double x = -aag1[nl - 1] * cv * cv;
+    double e11 = 2. * vs[nl - 1] * vs[nl - 1], e13 = -1. / rh[nl - 1];
+    double e22 = x / r1[nl - 1], e24 = e13 / r1[nl - 1], e31 = x / r2[nl - 1], e33 = -e13 / r2[nl - 1];
+    double e42 = -e11, e44 = e13;
+    double b[4][2];
+    hk_propagate(nl - 1, vs, r1, r2, e1, e2, c01, s01, c02, s02, tt, aag, aag1, xh, xh1, b);
+    double c11 = e11 * b[0][0] + e13 * b[2][0], c12 = e11 * b[0][1] + e13 * b[2][1];
+    double c21 = e22 * b[1][0] + e24 * b[3][0], c22 = e22 * b[1][1] + e24 * b[3][1];
+    double c31 = e31 * b[0][0] + e33 * b[2][0], c32 = e31 * b[0][1] + e33 * b[2][1];
+    double c41 = e42 * b[1][0] + e44 * b[3][0], c42 = e42 * b[1][1] + e44 * b[3][1];
+    double scl1 = -1. / (vp[nl - 1] * vp[nl - 1]), scl2 = -1. / (2.0 * vs[nl - 1] * vs[nl - 1]);
+    c11 *= scl1; c12 *= scl1; c21 *= scl1; c22 *= scl1;
+    c31 *= scl2; c32 *= scl2; c41 *= scl2; c42 *= scl2;
+    x = -c11 * c42 + c21 * c32 + c31 * c22 - c41 * c12;
+    double y = c11 * c32 + c21 * c42 - c31 * c12 - c41 * c22;
+    double ag = x * x + y * y;
+    double tm = s_wave ? cv / (vs[nl - 1] * ag) : 2. * cv / (vp[nl - 1] * ag);
+    double wr, wi, ur, ui;
+    if (!s_wave) {
+        wr = tm * (c31 * x - c41 * y); wi = tm * (-c31 * y - c41 * x);
+        ur = tm * (c42 * x - c32 * y); ui = tm * (-c42 * y - c32 * x);
+    } else {
+        wr = tm * (-c11 * x + c21 * y); wi = tm * (c11 * y + c21 * x);
+        ur = tm * (-c22 * x + c12 * y); ui = tm * (c22 * y + c12 * x);
+    }
+    const double qrw = wr, qiw = wi, qru = ur, qiu = ui;
+    ugrn[0] = qru + I * qiu;
+    wgrn[0] = qrw + I * qiw;
+    int ibovo = 1, ifin = 0;
+    int mstale = nl;   /* Fortran loop index after "do 7 m = 1, nl-1" */
+    for (int iz = 2; iz <= nz; iz++) {
+        double dept = dz * (iz - 1) + zorig;
+        int i;
+        for (i = 2; i <= nl; i++)
+            if (dept < h1d[i - 1]) break;
+        if (i > nl) i = nl;
+        int ibov = i - 1;
+        double dloc = dept - h1d[i - 2];
+        if (dloc < 0.) return 2;
+        if (ibov != ibovo) {
+            ibovo = ibov;
+            if (ibov > 1) {
+                ifin++;
+                /* refresh layer ifin with its full thickness, comparing against the stale m */
+                hk_layer_cs(pic * h[ifin - 1], r1[ifin - 1], r2[ifin - 1], cv, vp[mstale - 1], vs[mstale - 1],
+                            &e1[ifin - 1], &c01[ifin - 1], &s01[ifin - 1], &e2[ifin - 1], &c02[ifin - 1],
+                            &s02[ifin - 1]);
+            }
+        }
+        hk_layer_cs(pic * dloc, r1[ibov - 1], r2[ibov - 1], cv, vp[ibov - 1], vs[ibov - 1], &e1[ibov - 1],
+                    &c01[ibov - 1], &s01[ibov - 1], &e2[ibov - 1], &c02[ibov - 1], &s02[ibov - 1]);
+        hk_propagate(ibov, vs, r1, r2, e1, e2, c01, s01, c02, s02, tt, aag, aag1, xh, xh1, b);
+        mstale = ibov + 1;
+        ur = b[0][0] * qru - b[0][1] * qiw;
+        ui = b[0][0] * qiu + b[0][1] * qrw;
+        wr = -b[1][0] * qiu + b[1][1] * qrw;
+        wi = b[1][0] * qru + b[1][1] * qiw;
+        ugrn[iz - 1] = ur + I * ui;
+        wgrn[iz - 1] = wr + I * wi;
+    }
+    return 0;
+}

@@ -77,6 +77,13 @@ void ora_spmv_c128(int n, const int *irptr, const int *jcptr, const double compl
 long long ora_point_source(const ora_grid *g, double xloc, double yloc, double zloc,
                            int comp, double complex sterm, double complex *rhs);
 
+/* HASKGRN (haskgrn.f:31-672) in FP64: ugrn[nz], wgrn[nz] for a unit incident
+ * P (s_wave = 0) or S plane wave with incidence angle ain (radians) at angular
+ * frequency omega, nl layers with tops h1d[] (h1d[0] = 0; layer nl = half-space). */
+int ora_haskgrn(int nl, const double *vp1d, const double *vs1d, const double *rh1d, const double *h1d,
+                double omega, double ain, int s_wave, int nz, double dz, double zorig,
+                double complex *ugrn, double complex *wgrn);
+
 #ifdef __cplusplus
 }
 #endif

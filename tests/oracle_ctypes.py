@@ -35,6 +35,8 @@ class Oracle:
         L.ora_node_blocks_c128.argtypes = [ctypes.POINTER(OGrid), vp, vp, vp, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp]
         L.ora_spmv_c128.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp]
+        L.ora_haskgrn.argtypes = [ctypes.c_int, vp, vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, vp]
         self.L = L
 
     @staticmethod
@@ -75,3 +77,29 @@ class Oracle:
         ierr = self.L.ora_node_blocks_c128(ctypes.byref(og), _p(vp), _p(vs), _p(rho), om.real, om.imag,
                                            iz, ix, iy, _p(blk), _p(act))
         return blk.reshape(27, 3, 3), act, ierr
+
+    def haskgrn(self, vp, vs, rho, ztop, omega, ain, nz, dz, s_wave=False, zorig=0.0):
+        arr = [np.ascontiguousarray(a, np.float64) for a in (vp, vs, rho, ztop)]
+        U = np.zeros(nz, np.complex128)
+        W = np.zeros(nz, np.complex128)
+        rc = self.L.ora_haskgrn(len(arr[0]), *[_p(a) for a in arr], float(omega), float(ain), int(bool(s_wave)),
+                                int(nz), float(dz), float(zorig), _p(U), _p(W))
+        assert rc == 0, rc
+        return U, W
+
+    def planewave(self, g, layers1d, omega, ain, baz, s_wave=False):
+        """Incident field u0 on the grid (the definition documented with the
+        GPU kernel): [U rx, U ry, W] exp(i omega p (x rx + y ry))."""
+        vp, vs, rho, zt = layers1d
+        U, W = self.haskgrn(vp, vs, rho, zt, omega, ain, g.nz, g.dx, s_wave)
+        vh = vs[-1] if s_wave else vp[-1]
+        p = np.sin(ain) / vh
+        rx, ry = -np.cos(baz), -np.sin(baz)
+        iz, ix, iy = np.meshgrid(np.arange(g.nz), np.arange(g.nx), np.arange(g.ny), indexing="ij")
+        iz, ix, iy = [t.reshape(-1, order="F") for t in (iz, ix, iy)]
+        ph = np.exp(1j * omega * p * (ix * g.dx * rx + iy * g.dx * ry))
+        u0 = np.zeros(3 * len(iz), np.complex128)
+        u0[0::3] = U[iz] * rx * ph
+        u0[1::3] = U[iz] * ry * ph
+        u0[2::3] = W[iz] * ph
+        return u0

@@ -62,6 +62,25 @@ class Grid(ctypes.Structure):
         return pmld, pmlf, ipml
 
 
+class Layered1D(ctypes.Structure):
+    """wt3d_layered1d: nl layers (the last is the half-space), ztop[0] = 0."""
+    _fields_ = [("nl", ctypes.c_int), ("vp", ctypes.c_void_p), ("vs", ctypes.c_void_p),
+                ("rho", ctypes.c_void_p), ("ztop", ctypes.c_void_p)]
+
+    def __init__(self, vp, vs, rho, ztop):
+        self._keep = [np.ascontiguousarray(a, np.float64) for a in (vp, vs, rho, ztop)]
+        super().__init__(len(self._keep[0]), *[ctypes.c_void_p(a.ctypes.data) for a in self._keep])
+
+
+def haskgrn(layers, omega, ain, nz, dz, s_wave=False, zorig=0.0):
+    """Thomson-Haskell response (U, W) at nz node depths (host, FP64)."""
+    U = np.zeros(nz, np.complex128)
+    W = np.zeros(nz, np.complex128)
+    _check(lib().wt3d_haskgrn(ctypes.byref(layers), float(omega), float(ain), int(bool(s_wave)), int(nz),
+                              float(dz), float(zorig), _ptr(U), _ptr(W)))
+    return U, W
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("n", ctypes.c_longlong), ("nnz", ctypes.c_longlong), ("nfronts", ctypes.c_longlong),
                 ("factor_entries", ctypes.c_longlong), ("factor_flops", ctypes.c_double),
@@ -108,6 +127,10 @@ def lib():
         L.wt3d_get_stream.argtypes = [vp]
         L.wt3d_profile_factor.argtypes = [vp, vp]
         L.wt3d_set_device.argtypes = [ctypes.c_int]
+        L.wt3d_haskgrn.argtypes = [ctypes.POINTER(Layered1D), ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, vp]
+        L.wt3d_set_background.argtypes = [vp, vp, vp, vp]
+        L.wt3d_rhs_planewave.argtypes = [vp, ctypes.POINTER(Layered1D), ctypes.c_int, vp, vp, vp, vp, vp]
         ip = ctypes.POINTER(ctypes.c_int)
         L.strumpack_serial_finter.argtypes = [ip, ip, ip, vp, vp, vp, vp, vp, ip]
         L.strumpack_serial_finter.restype = None
@@ -251,6 +274,30 @@ class Solver:
         d["gemm_flops"] = float(out[len(kinds)])
         d["gemm_launches"] = int(out[len(kinds) + 1])
         return d
+
+    def set_background(self, vp, vs, rho):
+        n = self.grid.nnodes
+        self._bg = (_f32(vp, n), _f32(vs, n), _f32(rho, n))
+        _check(lib().wt3d_set_background(self._h, *[_ptr(a) for a in self._bg]))
+
+    def rhs_planewave(self, layers, ain, baz, s_wave=None, d_F=None, d_U0=None):
+        """Scattered-field plane-wave sources at the factored omega.  With device
+        pointers d_F (and d_U0) writes there; otherwise returns host arrays
+        (F, U0) of shape (n, nsrc)."""
+        ain = np.ascontiguousarray(ain, np.float64)
+        baz = np.ascontiguousarray(baz, np.float64)
+        ns = len(ain)
+        sw = np.ascontiguousarray(s_wave if s_wave is not None else np.zeros(ns), np.int32)
+        if d_F is not None:
+            _check(lib().wt3d_rhs_planewave(self._h, ctypes.byref(layers), ns, _ptr(ain), _ptr(baz), _ptr(sw),
+                                            ctypes.c_void_p(d_F), ctypes.c_void_p(d_U0 or 0)))
+            return None
+        import torch
+        F = torch.zeros((ns, self.grid.n), dtype=torch.complex128, device="cuda")
+        U0 = torch.zeros_like(F)
+        _check(lib().wt3d_rhs_planewave(self._h, ctypes.byref(layers), ns, _ptr(ain), _ptr(baz), _ptr(sw),
+                                        ctypes.c_void_p(F.data_ptr()), ctypes.c_void_p(U0.data_ptr())))
+        return F.cpu().numpy().T.copy(), U0.cpu().numpy().T.copy()
 
     def stats(self):
         s = Stats()

@@ -111,6 +111,16 @@ __global__ void k_scatter_add_nat(long long n, int m, const int *__restrict__ pe
     d->y += (double)v.im * w;
 }
 
+__global__ void k_pw_expand(int nx, int ny, int nz, double dx, int m, const double2 *__restrict__ Uz,
+                            const double2 *__restrict__ Wz, const double *__restrict__ kx,
+                            const double *__restrict__ ky, const double *__restrict__ rx,
+                            const double *__restrict__ ry, double2 *__restrict__ U0, int ld);
+__global__ void k_hetfld(long long n, int m, const int *__restrict__ irptr, const int *__restrict__ jcptr,
+                         const double2 *__restrict__ a, const double2 *__restrict__ abg,
+                         const double2 *__restrict__ U0, int ld, double2 *__restrict__ F);
+int haskgrn_host(const wt3d_layered1d &M, double omega, double ain, int s_wave, int nz, double dz, double zorig,
+                 std::complex<double> *U, std::complex<double> *W);
+
 __global__ void k_c64_to_c128(long long n, const float2 *__restrict__ s, double2 *__restrict__ d)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -132,6 +142,10 @@ struct wt3d_solver {
     DevVec<double> ro;
     DevVec<float> vp, vs, rho;
     DevVec<double2> Bn, Xn, Rn, T1;
+    DevVec<double2> abg, bgda, bgmu;      // background operator and Lame arrays
+    DevVec<double> bgro;
+    bool have_bg = false;
+    double om_re = 0, om_im = 0;          // omega of the assembled operator
     DevVec<double> norms;
     std::unique_ptr<Engine<float>> e32;
     std::unique_ptr<Engine<double>> e64;
@@ -452,9 +466,86 @@ int wt3d_factor(wt3d_solver *h, double omega_re, double omega_im)
     WT_CUDA(cudaStreamSynchronize(h->st));
     h->stats.t_assemble_ms = ms_between(h->ev0, h->ev1);
     h->have_values = true;
+    h->om_re = omega_re;
+    h->om_im = omega_im;
     rc = factor_values(h);
     h->stats.kernels_factor += 1;   // the assembly kernel
     return rc;
+}
+
+int wt3d_set_background(wt3d_solver *h, const float *vp, const float *vs, const float *rho)
+{
+    if (!h || !vp || !vs || !rho) { set_error("wt3d_set_background: null pointer"); return WT3D_ERR_ARG; }
+    const long long nn = h->n / 3;
+    int rc;
+    if (!h->bgro.p && ((rc = h->bgda.alloc(nn)) || (rc = h->bgmu.alloc(nn)) || (rc = h->bgro.alloc(nn)))) return rc;
+    DevVec<float> dvp, dvs, drho;
+    if ((rc = dvp.alloc(nn)) || (rc = dvs.alloc(nn)) || (rc = drho.alloc(nn))) return rc;
+    WT_CUDA(cudaMemcpyAsync(dvp.p, vp, sizeof(float) * nn, cudaMemcpyHostToDevice, h->st));
+    WT_CUDA(cudaMemcpyAsync(dvs.p, vs, sizeof(float) * nn, cudaMemcpyHostToDevice, h->st));
+    WT_CUDA(cudaMemcpyAsync(drho.p, rho, sizeof(float) * nn, cudaMemcpyHostToDevice, h->st));
+    if ((rc = device_lame(nn, dvp.p, dvs.p, drho.p, h->bgda.p, h->bgmu.p, h->bgro.p, h->st))) return rc;
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    h->have_bg = true;
+    return WT3D_OK;
+}
+
+int wt3d_haskgrn(const wt3d_layered1d *m, double omega, double ain, int s_wave, int nz, double dz, double zorig,
+                 double _Complex *U, double _Complex *W)
+{
+    if (!m || !U || !W || nz < 1) { set_error("wt3d_haskgrn: bad arguments"); return WT3D_ERR_ARG; }
+    return haskgrn_host(*m, omega, ain, s_wave, nz, dz, zorig, reinterpret_cast<std::complex<double> *>(U),
+                        reinterpret_cast<std::complex<double> *>(W));
+}
+
+int wt3d_rhs_planewave(wt3d_solver *h, const wt3d_layered1d *m, int nsrc, const double *ain, const double *baz,
+                       const int *s_wave, void *d_F, void *d_U0)
+{
+    if (!h || !m || nsrc < 1 || !ain || !baz || !d_F) { set_error("wt3d_rhs_planewave: bad arguments"); return WT3D_ERR_ARG; }
+    if (!h->have_values || !h->have_bg) { set_error("wt3d_rhs_planewave: needs a factored operator and a background"); return WT3D_ERR_STATE; }
+    const int nx = h->grid.nx, ny = h->grid.ny, nz = h->grid.nz;
+    const long long n = h->n;
+    int rc;
+    if (!h->abg.p && (rc = h->abg.alloc(h->nnz))) return rc;
+    if ((rc = device_assemble(h->grid, h->bgda.p, h->bgmu.p, h->bgro.p, h->om_re, h->om_im, h->irptr.p, h->abg.p,
+                              h->st)))
+        return rc;
+    const int nl = m->nl;
+    for (int c0 = 0; c0 < nsrc; c0 += MAXRHS) {
+        const int mm = std::min(MAXRHS, nsrc - c0);
+        std::vector<std::complex<double>> Uz((size_t)mm * nz), Wz((size_t)mm * nz);
+        std::vector<double> kx(mm), ky(mm), rx(mm), ry(mm);
+        for (int j = 0; j < mm; j++) {
+            const int sw = s_wave ? s_wave[c0 + j] : 0;
+            if ((rc = haskgrn_host(*m, h->om_re, ain[c0 + j], sw, nz, h->grid.dx, 0.0, &Uz[(size_t)j * nz],
+                                   &Wz[(size_t)j * nz])))
+                return rc;
+            const double vh = sw ? m->vs[nl - 1] : m->vp[nl - 1];
+            const double p = std::sin(ain[c0 + j]) / vh;
+            rx[j] = -std::cos(baz[c0 + j]);
+            ry[j] = -std::sin(baz[c0 + j]);
+            kx[j] = h->om_re * p * rx[j];
+            ky[j] = h->om_re * p * ry[j];
+        }
+        DevVec<double2> dU, dW;
+        DevVec<double> dkx, dky, drx, dry;
+        std::vector<double2> hu(Uz.size()), hw(Wz.size());
+        for (size_t i = 0; i < Uz.size(); i++) {
+            hu[i] = make_double2(Uz[i].real(), Uz[i].imag());
+            hw[i] = make_double2(Wz[i].real(), Wz[i].imag());
+        }
+        if ((rc = dU.upload(hu)) || (rc = dW.upload(hw)) || (rc = dkx.upload(kx)) || (rc = dky.upload(ky)) ||
+            (rc = drx.upload(rx)) || (rc = dry.upload(ry)))
+            return rc;
+        k_pw_expand<<<ceil_div((n / 3) * mm, 256), 256, 0, h->st>>>(nx, ny, nz, h->grid.dx, mm, dU.p, dW.p, dkx.p,
+                                                                     dky.p, drx.p, dry.p, h->Rn.p, MAXRHS);
+        k_hetfld<<<152 * 8, 256, 0, h->st>>>(n, mm, h->irptr.p, h->jcptr.p, h->a.p, h->abg.p, h->Rn.p, MAXRHS,
+                                             (double2 *)d_F + (long long)c0 * n);
+        if (d_U0) k_rm_to_cm<<<ceil_div(n, 256), 256, 0, h->st>>>(n, mm, h->Rn.p, (double2 *)d_U0 + (long long)c0 * n);
+        WT_CUDA(cudaGetLastError());
+        WT_CUDA(cudaStreamSynchronize(h->st));
+    }
+    return WT3D_OK;
 }
 
 int wt3d_set_values_c64(wt3d_solver *h, const float _Complex *a)

@@ -62,6 +62,7 @@ public:
     DevVec<unsigned long long> maxabs;
     std::unique_ptr<Schedule<T>> fsched;
     std::map<int, std::unique_ptr<Schedule<T>>> ssched[2];   // [adjoint][m]
+    static constexpr int WB = 512;   // outer block width of the two-level LU
     double pivot_rel = 1e-20;
     // tcgen05 path for complex64 front updates (WT3D_TC=0 selects the SIMT kernel)
     bool use_tc = std::is_same<T, float>::value && !(getenv("WT3D_TC") && getenv("WT3D_TC")[0] == '0');
@@ -276,42 +277,70 @@ public:
                     }, LK_EXTEND_ADD, 0});
                 }
             }
-            // blocked partial LU, level-synchronous over fronts
+            // Two-level blocked partial LU, level-synchronous over fronts.
+            // Inner KB-wide panels: panel LU, row band (all columns right of
+            // the panel), column band (all rows below), and rank-KB updates
+            // confined to the rows or the columns of the current WB-wide outer
+            // block.  Once an outer block is done, the rows and columns below
+            // and right of it receive one rank-WB update, so most of the
+            // elimination runs as K = WB GEMMs on the tensor cores.
             int maxp = 0;
             for (int f : fl) maxp = std::max(maxp, sym.fronts[f].p);
-            for (int k = 0; k < maxp; k += KB) {
-                size_t p0 = hp.size(), r0 = hr.size(), c0 = hc.size(), g0 = hg.size();
+            for (int c0 = 0; c0 < maxp; c0 += WB) {
+                for (int k = c0; k < std::min(c0 + WB, maxp); k += KB) {
+                    size_t p0 = hp.size(), r0 = hr.size(), cc0 = hc.size(), g0 = hg.size();
+                    long long tiles = 0;
+                    for (int f : fl) {
+                        const Front &Fr = sym.fronts[f];
+                        if (Fr.p <= k) continue;
+                        const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k), k2 = k + kb;
+                        const int cend = std::min(c0 + WB, Fr.p);
+                        hp.push_back(PanelTask{f, k});
+                        for (int c = k2; c < nf; c += TRW) hr.push_back(RowTask{f, k, c});
+                        for (int r = k2; r < Fr.p; r += TCR) hc.push_back(ColTask{f, k, r, 0});
+                        for (int r = 0; r < Fr.b; r += TCR) hc.push_back(ColTask{f, k, r, 1});
+                        cx<T> *Pb = F + Fr.fac_off;
+                        cx<T> *Lo = Pb + (long long)Fr.p * nf;
+                        // rows inside the outer block, every column right of the panel
+                        add_gemm(hg, tiles, Pb + (long long)k2 * nf + k, nf, Pb + (long long)k * nf + k2, nf,
+                                 Pb + (long long)k2 * nf + k2, nf, cend - k2, nf - k2, kb);
+                        // rows below the outer block, columns inside it
+                        add_gemm(hg, tiles, Pb + (long long)cend * nf + k, nf, Pb + (long long)k * nf + k2, nf,
+                                 Pb + (long long)cend * nf + k2, nf, Fr.p - cend, cend - k2, kb);
+                        add_gemm(hg, tiles, Lo + k, Fr.p, Pb + (long long)k * nf + k2, nf, Lo + k2, Fr.p, Fr.b,
+                                 cend - k2, kb);
+                    }
+                    int np = (int)(hp.size() - p0), nr = (int)(hr.size() - r0), ncl = (int)(hc.size() - cc0);
+                    size_t smp = sizeof(cx<T>) * KB * (KB + 1);
+                    size_t smr = sizeof(cx<T>) * (KB * (KB + 1) + KB * (TRW + 1));
+                    size_t smc = sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1));
+                    sc->launches.push_back({[psc, this, p0, np, smp](cudaStream_t st) {
+                        k_panel<T><<<np, 256, smp, st>>>(psc->panel.p + p0, fr.p, fac.p, ipiv.p, maxabs.p, pivot_rel, npert.p);
+                    }, LK_PANEL, 0});
+                    if (nr)
+                        sc->launches.push_back({[psc, this, r0, nr, smr](cudaStream_t st) {
+                            k_trsm_row<T><<<nr, TRW, smr, st>>>(psc->row.p + r0, fr.p, fac.p, ipiv.p);
+                        }, LK_TRSM, 0});
+                    if (ncl)
+                        sc->launches.push_back({[psc, this, cc0, ncl, smc](cudaStream_t st) {
+                            k_trsm_col<T><<<ncl, TCR, smc, st>>>(psc->col.p + cc0, fr.p, fac.p);
+                        }, LK_TRSM, 0});
+                    push_gemm_launch(*sc, hg, g0, tiles);
+                }
+                // rank-WB update of everything below and right of the outer block
+                size_t g0 = hg.size();
                 long long tiles = 0;
                 for (int f : fl) {
                     const Front &Fr = sym.fronts[f];
-                    if (Fr.p <= k) continue;
-                    const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k), k2 = k + kb;
-                    hp.push_back(PanelTask{f, k});
-                    for (int c = k2; c < nf; c += TRW) hr.push_back(RowTask{f, k, c});
-                    for (int r = k2; r < Fr.p; r += TCR) hc.push_back(ColTask{f, k, r, 0});
-                    for (int r = 0; r < Fr.b; r += TCR) hc.push_back(ColTask{f, k, r, 1});
+                    if (Fr.p <= c0) continue;
+                    const int nf = Fr.nf(), cend = std::min(c0 + WB, Fr.p), w = cend - c0;
                     cx<T> *Pb = F + Fr.fac_off;
                     cx<T> *Lo = Pb + (long long)Fr.p * nf;
-                    add_gemm(hg, tiles, Pb + (long long)k2 * nf + k, nf, Pb + (long long)k * nf + k2, nf,
-                             Pb + (long long)k2 * nf + k2, nf, Fr.p - k2, nf - k2, kb);
-                    add_gemm(hg, tiles, Lo + k, Fr.p, Pb + (long long)k * nf + k2, nf, Lo + k2, Fr.p, Fr.b,
-                             Fr.p - k2, kb);
+                    add_gemm(hg, tiles, Pb + (long long)cend * nf + c0, nf, Pb + (long long)c0 * nf + cend, nf,
+                             Pb + (long long)cend * nf + cend, nf, Fr.p - cend, nf - cend, w);
+                    add_gemm(hg, tiles, Lo + c0, Fr.p, Pb + (long long)c0 * nf + cend, nf, Lo + cend, Fr.p, Fr.b,
+                             Fr.p - cend, w);
                 }
-                int np = (int)(hp.size() - p0), nr = (int)(hr.size() - r0), ncl = (int)(hc.size() - c0);
-                size_t smp = sizeof(cx<T>) * KB * (KB + 1);
-                size_t smr = sizeof(cx<T>) * (KB * (KB + 1) + KB * (TRW + 1));
-                size_t smc = sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1));
-                sc->launches.push_back({[psc, this, p0, np, smp](cudaStream_t st) {
-                    k_panel<T><<<np, 256, smp, st>>>(psc->panel.p + p0, fr.p, fac.p, ipiv.p, maxabs.p, pivot_rel, npert.p);
-                }, LK_PANEL, 0});
-                if (nr)
-                    sc->launches.push_back({[psc, this, r0, nr, smr](cudaStream_t st) {
-                        k_trsm_row<T><<<nr, TRW, smr, st>>>(psc->row.p + r0, fr.p, fac.p, ipiv.p);
-                    }, LK_TRSM, 0});
-                if (ncl)
-                    sc->launches.push_back({[psc, this, c0, ncl, smc](cudaStream_t st) {
-                        k_trsm_col<T><<<ncl, TCR, smc, st>>>(psc->col.p + c0, fr.p, fac.p);
-                    }, LK_TRSM, 0});
                 push_gemm_launch(*sc, hg, g0, tiles);
             }
             // Schur complement F22 -= L21 U12 (K = p)

@@ -20,7 +20,8 @@
 //   warp 1      single-thread tcgen05.mma issuer (kind::tf32, M=128, N=256),
 //               tcgen05.commit releases smem stages and signals the epilogue;
 //   warps 2..5  epilogue: tcgen05.ld of the 128 x 256 FP32 accumulator,
-//               C -= D with 128-byte row segments.
+//               staged through shared memory, C -= D with coalesced
+//               256-byte warp accesses.
 // Every mbarrier wait has an iteration limit; on expiry the kernel records an
 // error code, skips ahead, frees its TMEM and returns.
 #include <cuda.h>
@@ -298,28 +299,50 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         umma_commit(accum);
     } else if (warp >= 2) {
         // ---------------- epilogue ----------------
+        // The accumulator is staged row-major in the (now idle) pipeline
+        // shared memory, then C is read-modified-written by whole warps on
+        // contiguous 256-byte row segments.
         if (!mbar_wait(accum, 0)) atomicCAS(err, 0, 3);
         asm volatile("tcgen05.fence::after_thread_sync;");
         const int q = warp & 3;                 // TMEM lane quarter this warp may access
-        const int row = m0 + 32 * q + lane;
         const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16);
-        cx<float> *crow = t.C + (long long)row * t.ldc;
-        const int c0 = n0r / 2;
+        float *stage = reinterpret_cast<float *>(smem);     // 128 rows x EP floats
+        constexpr int EP = TC_BNR + 4;
+        float *myrow = stage + (32 * q + lane) * EP;
 #pragma unroll 1
         for (int ch = 0; ch < TC_BNR / 32; ch++) {
             uint32_t v[32];
             TMEM_LD32(tq + ch * 32, v);
             asm volatile("tcgen05.wait::ld.sync.aligned;");
-            if (row < t.M) {
 #pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    const int c = c0 + ch * 16 + i;
-                    if (c < t.N) {
-                        cx<float> o = crow[c];
-                        o.re -= __uint_as_float(v[2 * i]);
-                        o.im -= __uint_as_float(v[2 * i + 1]);
-                        crow[c] = o;
-                    }
+            for (int i = 0; i < 32; i += 4)
+                *reinterpret_cast<float4 *>(myrow + ch * 32 + i) =
+                    make_float4(__uint_as_float(v[i]), __uint_as_float(v[i + 1]), __uint_as_float(v[i + 2]),
+                                __uint_as_float(v[i + 3]));
+        }
+        asm volatile("bar.sync 1, 128;" ::: "memory");   // the four epilogue warps only
+        const int c0 = n0r / 2;
+        const int ew = warp - 2;                // 0..3
+#pragma unroll 1
+        for (int r = ew; r < TC_BM; r += 4) {
+            const int row = m0 + r;
+            if (row >= t.M) break;
+            cx<float> *crow = t.C + (long long)row * t.ldc + c0;
+            const float *srow = stage + r * EP;
+            cx<float> o[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int c = lane + 32 * j;
+                if (c0 + c < t.N) o[j] = crow[c];
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int c = lane + 32 * j;
+                if (c0 + c < t.N) {
+                    const float2 d = *reinterpret_cast<const float2 *>(srow + 2 * c);
+                    o[j].re -= d.x;
+                    o[j].im -= d.y;
+                    crow[c] = o[j];
                 }
             }
         }
@@ -381,7 +404,9 @@ long long tc_workspace_floats(const GemmTask<float> *g, int n)
 
 bool tc_eligible(const GemmTask<float> &g)
 {
-    return !g.brow && !g.crow && !g.conjA && g.M >= 32 && g.N >= 32 && g.K >= 8;
+    // large enough that the tensor-core tile (128 x 128 complex) is not mostly
+    // padding; the narrow right-hand-side blocks of the solves stay on SIMT
+    return !g.brow && !g.crow && !g.conjA && g.M >= 64 && g.N >= 96 && g.K >= 32;
 }
 
 int tc_build_launch(TcLaunch &L, const GemmTask<float> *g, int n, float *ws)

@@ -65,3 +65,16 @@ def point_force(nx, ny, nz, dx, xloc, yloc, zloc, comp=2, sterm=1.0 + 0.0j):
     g = (izs - 1) + nz * (ixs - 1) + nz * nx * (iys - 1)
     b[3 * g + comp] = sterm
     return b
+
+
+def layered1d(nz, dx, layer_vp=(3000.0, 4000.0, 5000.0, 6000.0), vpvs=1.73):
+    """1-D description of layered(): (vp, vs, rho, ztop) float64 arrays for the
+    Thomson-Haskell response, ztop[i] the depth of the first node of layer i
+    (layer index iz*nl//nz), the last layer being the half-space."""
+    nl = len(layer_vp)
+    vp = np.asarray(layer_vp, np.float64)
+    first = np.array([-(-i * nz // nl) for i in range(nl)], np.float64)   # ceil(i nz / nl)
+    ztop = first * dx
+    vs = (vp / vpvs).astype(np.float32).astype(np.float64)
+    rho = (310.0 * np.power(vp, 0.25)).astype(np.float32).astype(np.float64)
+    return vp, vs, rho, ztop
