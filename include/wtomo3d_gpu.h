@@ -127,7 +127,9 @@ int wt3d_set_background(wt3d_solver *h, const float *vp, const float *vs, const 
 
 /* Plane-wave scattered-field sources at the last factored omega, replacing
  * haskgrn + plane-wave expansion + hetfldsrc (hetfldsrc.f90:17-1038):
- *   u0_j = [U_j(z) rx, U_j(z) ry, W_j(z)] exp(i omega p_j (x rx + y ry)),
+ *   u0_j = [U_j*(z) rx, U_j*(z) ry, W_j*(z)] exp(i omega p_j (x rx + y ry)),
+ *   (* = complex conjugate: Haskell's time sign is the reverse of the
+ *   operator's, dispersion.f:17-22),
  *   (rx, ry) = -(cos baz_j, sin baz_j), p_j = sin(ain_j) / v_halfspace,
  *   f_j = (A_bg - A) u0_j   (source spectrum 1, srcin = 3).
  * d_F: device complex128, column-major n x nsrc.  d_U0 (optional, may be NULL):
@@ -195,6 +197,11 @@ void *wt3d_get_stream(wt3d_solver *h);
  * gemm} launches, out[9] = GEMM real flops (both paths), out[10] = GEMM
  * launches.  out must hold 11 doubles. */
 int wt3d_profile_factor(wt3d_solver *h, double *out);
+
+/* One forward + backward substitution pass over m right-hand sides (no CUDA
+ * graph, an event pair per launch): out[0..10] as wt3d_profile_factor,
+ * out[11] = ms of one FP64 residual over m columns.  out holds 12 doubles. */
+int wt3d_profile_solve(wt3d_solver *h, int m, double *out);
 
 /* Copy internal device state to the host for checks (what = 0: factor pool,
  * complex entries of the handle's precision; 1: pivot indices). */

@@ -89,9 +89,11 @@ class Oracle:
 
     def planewave(self, g, layers1d, omega, ain, baz, s_wave=False):
         """Incident field u0 on the grid (the definition documented with the
-        GPU kernel): [U rx, U ry, W] exp(i omega p (x rx + y ry))."""
+        GPU kernel): [U* rx, U* ry, W*] exp(i omega p (x rx + y ry)), with the
+        Haskell response conjugated to the operator's time sign."""
         vp, vs, rho, zt = layers1d
         U, W = self.haskgrn(vp, vs, rho, zt, omega, ain, g.nz, g.dx, s_wave)
+        U, W = U.conj(), W.conj()
         vh = vs[-1] if s_wave else vp[-1]
         p = np.sin(ain) / vh
         rx, ry = -np.cos(baz), -np.sin(baz)

@@ -76,7 +76,7 @@ def test_incident_field_solves_background_interior(oracle):
     # interior nodes away from the PML and the free surface
     rows = [3 * node(iz, ix, 4) + c for iz in range(8, 16) for ix in range(6, 14) for c in (0, 2)]
     rel = np.abs(r[rows]).max() / (om * om * 2400.0 * np.abs(u0).max())
-    assert rel < 0.02, rel
+    assert rel < 2e-3, rel
 
 
 def test_scattered_field_solve(case):

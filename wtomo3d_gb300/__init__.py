@@ -126,6 +126,7 @@ def lib():
         L.wt3d_get_stream.restype = vp
         L.wt3d_get_stream.argtypes = [vp]
         L.wt3d_profile_factor.argtypes = [vp, vp]
+        L.wt3d_profile_solve.argtypes = [vp, ctypes.c_int, vp]
         L.wt3d_set_device.argtypes = [ctypes.c_int]
         L.wt3d_haskgrn.argtypes = [ctypes.POINTER(Layered1D), ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                    ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, vp]
@@ -298,6 +299,18 @@ class Solver:
         _check(lib().wt3d_rhs_planewave(self._h, ctypes.byref(layers), ns, _ptr(ain), _ptr(baz), _ptr(sw),
                                         ctypes.c_void_p(F.data_ptr()), ctypes.c_void_p(U0.data_ptr())))
         return F.cpu().numpy().T.copy(), U0.cpu().numpy().T.copy()
+
+    def profile_solve(self, m):
+        """Per-kernel-kind milliseconds of one substitution pass over m columns
+        and of one FP64 residual."""
+        kinds = ["memset", "scatter", "extend_add", "panel", "trsm", "gemm_simt", "diag_solve", "tc_split",
+                 "gemm_tc"]
+        out = np.zeros(12)
+        _check(lib().wt3d_profile_solve(self._h, int(m), _ptr(out)))
+        d = {k + "_ms": float(out[i]) for i, k in enumerate(kinds) if out[i] > 0}
+        d["gemm_flops"] = float(out[9])
+        d["residual_ms"] = float(out[11])
+        return d
 
     def stats(self):
         s = Stats()

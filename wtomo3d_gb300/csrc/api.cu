@@ -754,6 +754,32 @@ extern "C" int wt3d_profile_factor(wt3d_solver *h, double *out)
     return rc;
 }
 
+// One forward+backward pass over m right-hand sides (whatever X holds) with
+// per-launch events; out as wt3d_profile_factor, plus out[11] = ms of one FP64
+// residual over m columns.
+extern "C" int wt3d_profile_solve(wt3d_solver *h, int m, double *out)
+{
+    if (!h || !out || !h->have_factor || m < 1 || m > MAXRHS) return WT3D_ERR_STATE;
+    int rc;
+    if (h->e32) {
+        Schedule<float> *sc = h->e32->solve_schedule(m, false);
+        if (!sc) return WT3D_ERR_NOMEM;
+        rc = h->e32->profile_schedule(*sc, h->st, out);
+    } else {
+        Schedule<double> *sc = h->e64->solve_schedule(m, false);
+        if (!sc) return WT3D_ERR_NOMEM;
+        rc = h->e64->profile_schedule(*sc, h->st, out);
+    }
+    if (rc) return rc;
+    cudaEventRecord(h->ev0, h->st);
+    k_residual<<<152 * 8, 256, 0, h->st>>>(h->n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, h->Xn.p, h->Bn.p,
+                                           h->Rn.p, h->norms.p, h->norms.p + MAXRHS, 0);
+    cudaEventRecord(h->ev1, h->st);
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    out[11] = ms_between(h->ev0, h->ev1);
+    return WT3D_OK;
+}
+
 extern "C" int wt3d_debug_fetch(wt3d_solver *h, int what, void *out, long long count)
 {
     if (!h || !out) return WT3D_ERR_ARG;

@@ -550,6 +550,32 @@ public:
         return WT3D_OK;
     }
 
+    // One pass of a solve schedule with an event pair per launch: out[k] = ms of kind k.
+    int profile_schedule(Schedule<T> &sc, cudaStream_t st, double *out)
+    {
+        const size_t nl = sc.launches.size();
+        std::vector<cudaEvent_t> ev(2 * nl);
+        for (auto &e : ev) WT_CUDA(cudaEventCreate(&e));
+        for (size_t i = 0; i < nl; i++) {
+            WT_CUDA(cudaEventRecord(ev[2 * i], st));
+            sc.launches[i].fn(st);
+            WT_CUDA(cudaEventRecord(ev[2 * i + 1], st));
+        }
+        WT_CUDA(cudaStreamSynchronize(st));
+        for (int k = 0; k < LK_NKINDS + 2; k++) out[k] = 0;
+        for (size_t i = 0; i < nl; i++) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+            out[sc.launches[i].kind] += ms;
+            if (sc.launches[i].kind == LK_GEMM || sc.launches[i].kind == LK_TCGEMM) {
+                out[LK_NKINDS] += sc.launches[i].flops;
+                out[LK_NKINDS + 1] += 1;
+            }
+        }
+        for (auto &e : ev) cudaEventDestroy(e);
+        return WT3D_OK;
+    }
+
     int factor(const double2 *d_a, long long nnz, cudaStream_t st, int *h_npert)
     {
         if (d_a != a_dev && fsched->graph) { cudaGraphExecDestroy(fsched->graph); fsched->graph = nullptr; }

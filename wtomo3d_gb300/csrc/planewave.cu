@@ -3,12 +3,14 @@
 //   * haskgrn (host, FP64): Thomson-Haskell response U(z), W(z) of a layered
 //     1-D medium to a unit incident P or S plane wave (haskgrn.f:31-672).
 //   * k_pw_expand (device): the incident field on the 3-D grid,
-//         u0 = [U(z) rx, U(z) ry, W(z)] exp(i omega p (x rx + y ry)),
+//         u0 = [U*(z) rx, U*(z) ry, W*(z)] exp(i omega p (x rx + y ry)),
 //     with (rx, ry) = -(cos baz, sin baz) the horizontal propagation
 //     direction of a wave arriving from back-azimuth baz and p = 1/cv the
-//     horizontal slowness used by haskgrn (e^{-i omega t} convention, matching
-//     eyeom = -i omega of pml3d.f:186).  The reference's own expansion
-//     (planewvexp.f90) is not in the tree; this is the definition used here.
+//     horizontal slowness used by haskgrn.  The operator uses plane waves
+//     exp(i(kx - omega t)) while Haskell's response is for the reverse sign,
+//     so the background is conjugated (dispersion.f:17-22).  The reference's
+//     own expansion (planewvexp.f90) is not in the tree; this is the
+//     definition used here.
 //   * k_hetfld (device): the scattered-field source f = (A_bg - A) u0 of
 //     hetfldsrc.f90:55-1028 as a row-wise product with the two assembled
 //     operators, times the source spectrum (1 for srcin = 3, srcsub.f:249-257).
@@ -184,7 +186,9 @@ __global__ void k_pw_expand(int nx, int ny, int nz, double dx, int m, const doub
     const double ph = kx[j] * (ix * dx) + ky[j] * (iy * dx);
     double s, c;
     sincos(ph, &s, &c);
-    const double2 u = Uz[(long long)j * nz + iz], w = Wz[(long long)j * nz + iz];
+    double2 u = Uz[(long long)j * nz + iz], w = Wz[(long long)j * nz + iz];
+    u.y = -u.y;   // conjugate: Haskell's time sign is the reverse of the operator's
+    w.y = -w.y;
     const double2 ue = make_double2(u.x * c - u.y * s, u.x * s + u.y * c);
     const double2 we = make_double2(w.x * c - w.y * s, w.x * s + w.y * c);
     double2 *o = U0 + (3 * g) * ld + j;
