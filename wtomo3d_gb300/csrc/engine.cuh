@@ -53,7 +53,7 @@ template <class T>
 class Engine {
 public:
     const Symbolic *S = nullptr;
-    DevVec<cx<T>> fac, upd0, upd1, X;
+    DevVec<cx<T>> fac, upd0, upd1, X, dinv;   // dinv: per KB panel L_D^{-1}, U_D^{-1} (KB x KB each)
     DevVec<int> ipiv, border;
     DevVec<int> rel;
     DevVec<FrontDev> fr;
@@ -101,7 +101,10 @@ public:
         WT_CUDA(cudaMemset(tc_err.p, 0, sizeof(int)));
         if (use_tc && (rc = tc_init())) return rc;
         std::vector<FrontDev> h(sym.fronts.size());
+        long long npan = 0;
         for (size_t f = 0; f < h.size(); f++) {
+            h[f].pan = (int)npan;
+            npan += (sym.fronts[f].p + KB - 1) / KB;
             const Front &F = sym.fronts[f];
             h[f].fac = F.fac_off;
             h[f].upd = F.upd_off;
@@ -112,9 +115,10 @@ public:
             h[f].parity = F.level & 1;
         }
         if ((rc = fr.upload(h))) return rc;
+        if ((rc = dinv.alloc((size_t)npan * 2 * KB * KB))) return rc;
         static bool attr_done = false;
         if (!attr_done) {
-            size_t sp = sizeof(cx<T>) * KB * (KB + 1);
+            size_t sp = sizeof(cx<T>) * (KB * (KB + 1) + 2 * KB * (KB + 1));
             cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp);
             cudaFuncSetAttribute(k_trsm_row<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (TRW + 1))));
@@ -171,19 +175,40 @@ public:
         }
         all.resize(b);
         if (simt.empty()) return;
-        long long tiles = 0;
-        double fl = 0;
-        for (auto &g : simt) {
-            g.tile0 = tiles;
-            tiles += (long long)((g.M + GBM - 1) / GBM) * g.tiles_n;
-            fl += 8.0 * g.M * (double)g.N * g.K;
-            all.push_back(g);
-        }
-        const int nt = (int)simt.size();
+        // tasks with at most 32 columns go to the tall-skinny kernel
+        std::vector<GemmTask<T>> narrow, wide;
+        for (auto &g : simt) (g.N <= TSBN ? narrow : wide).push_back(g);
         Schedule<T> *psc = &sc;
-        sc.launches.push_back({[psc, b, nt, tiles](cudaStream_t st) {
-            k_gemm<T><<<(unsigned)tiles, 256, 0, st>>>(psc->gemm.p + b, nt);
-        }, LK_GEMM, fl});
+        if (!narrow.empty()) {
+            const size_t b0 = all.size();
+            long long tiles = 0;
+            double fl = 0;
+            for (auto &g : narrow) {
+                g.tile0 = tiles;
+                tiles += (g.M + TSBM - 1) / TSBM;
+                fl += 8.0 * g.M * (double)g.N * g.K;
+                all.push_back(g);
+            }
+            const int nt = (int)narrow.size();
+            sc.launches.push_back({[psc, b0, nt, tiles](cudaStream_t st) {
+                k_gemm_ts<T><<<(unsigned)tiles, 256, 0, st>>>(psc->gemm.p + b0, nt);
+            }, LK_GEMM, fl});
+        }
+        if (!wide.empty()) {
+            const size_t b0 = all.size();
+            long long tiles = 0;
+            double fl = 0;
+            for (auto &g : wide) {
+                g.tile0 = tiles;
+                tiles += (long long)((g.M + GBM - 1) / GBM) * g.tiles_n;
+                fl += 8.0 * g.M * (double)g.N * g.K;
+                all.push_back(g);
+            }
+            const int nt = (int)wide.size();
+            sc.launches.push_back({[psc, b0, nt, tiles](cudaStream_t st) {
+                k_gemm<T><<<(unsigned)tiles, 256, 0, st>>>(psc->gemm.p + b0, nt);
+            }, LK_GEMM, fl});
+        }
     }
 
     // Allocates the shared tensor-core workspace and builds the tensor maps of
@@ -311,11 +336,12 @@ public:
                                  cend - k2, kb);
                     }
                     int np = (int)(hp.size() - p0), nr = (int)(hr.size() - r0), ncl = (int)(hc.size() - cc0);
-                    size_t smp = sizeof(cx<T>) * KB * (KB + 1);
+                    size_t smp = sizeof(cx<T>) * (KB * (KB + 1) + 2 * KB * (KB + 1));
                     size_t smr = sizeof(cx<T>) * (KB * (KB + 1) + KB * (TRW + 1));
                     size_t smc = sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1));
                     sc->launches.push_back({[psc, this, p0, np, smp](cudaStream_t st) {
-                        k_panel<T><<<np, 256, smp, st>>>(psc->panel.p + p0, fr.p, fac.p, ipiv.p, maxabs.p, pivot_rel, npert.p);
+                        k_panel<T><<<np, 256, smp, st>>>(psc->panel.p + p0, fr.p, fac.p, ipiv.p, maxabs.p, pivot_rel, npert.p,
+                                                         dinv.p);
                     }, LK_PANEL, 0});
                     if (nr)
                         sc->launches.push_back({[psc, this, r0, nr, smr](cudaStream_t st) {
@@ -388,7 +414,7 @@ public:
             int np = (int)(hp.size() - p0);
             if (!np) return;
             sc->launches.push_back({[psc, this, p0, np, smd, m, mode, Xp, ldx](cudaStream_t st) {
-                k_diag_solve<T><<<np, MAXRHS, smd, st>>>(psc->panel.p + p0, fr.p, fac.p, ipiv.p, Xp, ldx, m, mode);
+                k_diag_solve<T><<<np, 256, smd, st>>>(psc->panel.p + p0, fr.p, dinv.p, ipiv.p, Xp, ldx, m, mode);
             }, LK_DIAG, 0});
         };
         // ---- forward sweep: leaves to root ----

@@ -22,6 +22,7 @@ struct FrontDev {
     long long upd;     // F22 offset in its parity buffer
     long long border;  // offset into the border index array
     int p, b, first, parity;
+    int pan;           // index of the front's first KB panel (tile-inverse store)
 };
 
 struct PanelTask { int f, k; };
@@ -149,12 +150,12 @@ template <class T>
 __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
                                                cx<T> *__restrict__ fac, int *__restrict__ ipiv,
                                                const unsigned long long *__restrict__ amax2, double pivot_rel,
-                                               int *__restrict__ npert)
+                                               int *__restrict__ npert, cx<T> *__restrict__ inv)
 {
     // static-pivot threshold: pivot_rel * max |a_ij| of the assembled operator
     const T thresh = (T)(pivot_rel * sqrt(__longlong_as_double((long long)*amax2)));
     extern __shared__ __align__(16) unsigned char smraw[];
-    cx<T> *S = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1)
+    cx<T> *S = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1), then 2 KB scratch columns
     __shared__ int s_piv;
     const PanelTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
@@ -215,6 +216,38 @@ __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tas
     for (int idx = tid; idx < kb * kb; idx += blockDim.x) {
         int i = idx / kb, j = idx % kb;
         D[(long long)i * nf + j] = S[i * LD + j];
+    }
+    // Inverses of the unit-lower L_D and upper U_D factors of the tile, for the
+    // substitution passes of the solves (dense products instead of serial
+    // recurrences).  Thread c < kb: column c of L_D^{-1}; kb <= c < 2kb:
+    // column c-kb of U_D^{-1}.  Padded to KB x KB with the identity.
+    cx<T> *Li = inv + (long long)(F.pan + k / KB) * (2 * KB * KB);
+    cx<T> *Ui = Li + KB * KB;
+    cx<T> *col = S + KB * LD;            // per-thread scratch column, 2 KB x (KB + 1)
+    const int c = tid;
+    if (c < 2 * KB) {
+        const bool up = c >= KB;
+        const int cc = up ? c - KB : c;
+        cx<T> *x = col + c * (KB + 1);
+        if (!up) {
+            for (int i = 0; i < KB; i++) {
+                cx<T> s = (i == cc) ? cx<T>(1) : cx<T>(0);
+                if (i < kb && cc < kb)
+                    for (int l = cc; l < i; l++) s = s - S[i * LD + l] * x[l];
+                x[i] = s;
+            }
+        } else {
+            for (int i = KB - 1; i >= 0; i--) {
+                cx<T> s = (i == cc) ? cx<T>(1) : cx<T>(0);
+                if (i < kb && cc < kb) {
+                    for (int l = i + 1; l <= cc; l++) s = s - S[i * LD + l] * x[l];
+                    s = cdiv(s, S[i * LD + i]);
+                }
+                x[i] = s;
+            }
+        }
+        cx<T> *dst = up ? Ui : Li;
+        for (int i = 0; i < KB; i++) dst[i * KB + cc] = x[i];
     }
 }
 
@@ -409,30 +442,118 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmTask<T> *__restrict__ ta
 }
 
 // ---------------------------------------------------------------------------
-// solve: diagonal-tile triangular solves on the RHS block of a front
-// mode 0: forward  (swaps + unit lower L_D)
-// mode 1: backward (upper U_D)
-// mode 2: adjoint forward  (U_D^H, lower, non-unit)
-// mode 3: adjoint backward (L_D^H, unit upper, then reverse swaps)
+// Tall-skinny SIMT complex GEMM  C -= op(A) * B  for N <= 32 (the right-hand
+// side blocks of the substitution passes): 128 x 32 tiles, 4 x 4 complex
+// outputs per thread, every A element read once per tile.
+// ---------------------------------------------------------------------------
+constexpr int TSBM = 128, TSBN = 32, TSBK = 16;
+template <class T>
+__global__ void __launch_bounds__(256) k_gemm_ts(const GemmTask<T> *__restrict__ tasks, int ntasks)
+{
+    __shared__ cx<T> As[TSBK][TSBM + 1];
+    __shared__ cx<T> Bs[TSBK][TSBN];
+    const int ti = find_task(tasks, ntasks, (long long)blockIdx.x);
+    const GemmTask<T> t = tasks[ti];
+    const int m0 = (int)((long long)blockIdx.x - t.tile0) * TSBM;
+    const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3;   // 8 column groups x 32 row groups
+    cx<T> acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = cx<T>(0);
+    for (int k0 = 0; k0 < t.K; k0 += TSBK) {
+        if (!t.conjA) {
+#pragma unroll
+            for (int q = 0; q < (TSBM * TSBK) / 256; q++) {
+                const int idx = tid + q * 256;
+                const int i = idx / TSBK, kk = idx % TSBK;
+                const int r = m0 + i, c = k0 + kk;
+                As[kk][i] = (r < t.M && c < t.K) ? t.A[(long long)r * t.lda + c] : cx<T>(0);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < (TSBM * TSBK) / 256; q++) {
+                const int idx = tid + q * 256;
+                const int kk = idx / TSBM, i = idx % TSBM;
+                const int r = m0 + i, c = k0 + kk;
+                As[kk][i] = (r < t.M && c < t.K) ? conj(t.A[(long long)c * t.lda + r]) : cx<T>(0);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < (TSBK * TSBN) / 256; q++) {
+            const int idx = tid + q * 256;
+            const int kk = idx / TSBN, j = idx % TSBN;
+            const int r = k0 + kk;
+            cx<T> v(0);
+            if (r < t.K && j < t.N) {
+                const long long row = t.brow ? (long long)t.brow[r] : (long long)r;
+                v = t.B[row * t.ldb + j];
+            }
+            Bs[kk][j] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < TSBK; kk++) {
+            cx<T> a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) a[i] = As[kk][ty + 32 * i];
+#pragma unroll
+            for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx + 8 * j];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    acc[i][j].re = fma(a[i].re, b[j].re, fma(-a[i].im, b[j].im, acc[i][j].re));
+                    acc[i][j].im = fma(a[i].re, b[j].im, fma(a[i].im, b[j].re, acc[i][j].im));
+                }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int r = m0 + ty + 32 * i;
+        if (r >= t.M) continue;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int c = tx + 8 * j;
+            if (c >= t.N) continue;
+            if (t.crow) atomic_sub(t.C + (long long)t.crow[r] * t.ldc + c, acc[i][j]);
+            else {
+                cx<T> *p = t.C + (long long)r * t.ldc + c;
+                *p = *p - acc[i][j];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// solve: diagonal-tile substitution on the RHS block of a front, as a dense
+// product with the tile inverses the panel kernel stored (L_D^{-1}, U_D^{-1}):
+// mode 0: forward   Y <- L_D^{-1} P Y        (P: the tile's row interchanges)
+// mode 1: backward  Y <- U_D^{-1} Y
+// mode 2: adjoint forward  Y <- U_D^{-H} Y
+// mode 3: adjoint backward Y <- P^T L_D^{-H} Y
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void __launch_bounds__(MAXRHS) k_diag_solve(const PanelTask *__restrict__ tasks,
-                                                       const FrontDev *__restrict__ fr,
-                                                       const cx<T> *__restrict__ fac, const int *__restrict__ ipiv,
-                                                       cx<T> *__restrict__ X, int ldx, int m, int mode)
+__global__ void __launch_bounds__(256) k_diag_solve(const PanelTask *__restrict__ tasks,
+                                                    const FrontDev *__restrict__ fr,
+                                                    const cx<T> *__restrict__ inv, const int *__restrict__ ipiv,
+                                                    cx<T> *__restrict__ X, int ldx, int m, int mode)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    cx<T> *Ds = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1)
-    cx<T> *Ys = Ds + KB * (KB + 1);                 // KB x (MAXRHS+1)
+    cx<T> *Ms = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1): the operator of this mode
+    cx<T> *Ys = Ms + KB * (KB + 1);                 // KB x (MAXRHS+1)
     __shared__ int idx[KB];
     const PanelTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
-    const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
+    const int k = t.k, kb = min(KB, F.p - k);
     const int tid = threadIdx.x;
-    const cx<T> *D = fac + F.fac + (long long)k * nf + k;
-    for (int q = tid; q < kb * kb; q += blockDim.x) {
-        int i = q / kb, j = q % kb;
-        Ds[i * (KB + 1) + j] = D[(long long)i * nf + j];
+    const cx<T> *Li = inv + (long long)(F.pan + k / KB) * (2 * KB * KB);
+    const cx<T> *Mi = (mode == 0 || mode == 3) ? Li : Li + KB * KB;
+    const bool herm = mode >= 2;
+    for (int q = tid; q < KB * KB; q += blockDim.x) {
+        const int i = q / KB, j = q % KB;
+        Ms[i * (KB + 1) + j] = herm ? conj(Mi[j * KB + i]) : Mi[i * KB + j];
     }
     if (tid == 0) {
         for (int i = 0; i < kb; i++) idx[i] = i;
@@ -446,45 +567,27 @@ __global__ void __launch_bounds__(MAXRHS) k_diag_solve(const PanelTask *__restri
     cx<T> *Y = X + (long long)(F.first + k) * ldx;
     const int LY = MAXRHS + 1;
     for (int q = tid; q < kb * m; q += blockDim.x) {
-        int i = q / m, c = q % m;
+        const int i = q / m, c = q % m;
         Ys[i * LY + c] = Y[(long long)(mode == 0 ? idx[i] : i) * ldx + c];
     }
     __syncthreads();
-    if (tid < m) {
-        const int c = tid;
-        if (mode == 0) {
-            for (int i = 1; i < kb; i++) {
-                cx<T> s = Ys[i * LY + c];
-                for (int l = 0; l < i; l++) s = s - Ds[i * (KB + 1) + l] * Ys[l * LY + c];
-                Ys[i * LY + c] = s;
-            }
-        } else if (mode == 1) {
-            for (int i = kb - 1; i >= 0; i--) {
-                cx<T> s = Ys[i * LY + c];
-                for (int l = i + 1; l < kb; l++) s = s - Ds[i * (KB + 1) + l] * Ys[l * LY + c];
-                Ys[i * LY + c] = cdiv(s, Ds[i * (KB + 1) + i]);
-            }
-        } else if (mode == 2) {
-            // U_D^H y = s : lower triangular with conj(U[l][i])
-            for (int i = 0; i < kb; i++) {
-                cx<T> s = Ys[i * LY + c];
-                for (int l = 0; l < i; l++) s = s - conj(Ds[l * (KB + 1) + i]) * Ys[l * LY + c];
-                Ys[i * LY + c] = cdiv(s, conj(Ds[i * (KB + 1) + i]));
-            }
-        } else {
-            // L_D^H y = s : unit upper with conj(L[l][i])
-            for (int i = kb - 1; i >= 0; i--) {
-                cx<T> s = Ys[i * LY + c];
-                for (int l = i + 1; l < kb; l++) s = s - conj(Ds[l * (KB + 1) + i]) * Ys[l * LY + c];
-                Ys[i * LY + c] = s;
-            }
-        }
+    // out[i][c] = sum_l M[i][l] Y[l][c]; each thread keeps its outputs in registers
+    constexpr int PER = (KB * MAXRHS + 255) / 256;
+    cx<T> acc[PER];
+    int oi[PER], oc[PER];
+#pragma unroll
+    for (int r = 0; r < PER; r++) {
+        const int q = tid + r * 256;
+        oi[r] = q / m;
+        oc[r] = q % m;
+        acc[r] = cx<T>(0);
+        if (oi[r] < kb)
+            for (int l = 0; l < kb; l++) acc[r] = acc[r] + Ms[oi[r] * (KB + 1) + l] * Ys[l * LY + oc[r]];
     }
     __syncthreads();
-    for (int q = tid; q < kb * m; q += blockDim.x) {
-        int i = q / m, c = q % m;
-        Y[(long long)(mode == 3 ? idx[i] : i) * ldx + c] = Ys[i * LY + c];
-    }
+#pragma unroll
+    for (int r = 0; r < PER; r++)
+        if (oi[r] < kb) Y[(long long)(mode == 3 ? idx[oi[r]] : oi[r]) * ldx + oc[r]] = acc[r];
 }
 
 }  // namespace wt3d
