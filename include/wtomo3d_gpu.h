@@ -217,6 +217,24 @@ int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int lda, const
  * path 1 = tensor-core kernel (operand split excluded), 0 = SIMT kernel. */
 int wt3d_bench_gemm(int path, int M, int N, int K, int iters, double *ms_out);
 
+/* ---- allocation-free entry point ----------------------------------------
+ * No counterpart in the reference.  C -= A B for complex64 device arrays
+ * (row-major, leading dimensions in elements; A is M x K, B is K x N, C is
+ * M x N) on the tensor cores, like the front updates, without allocating any
+ * device memory: the operand split lives in a fixed scratch array inside the
+ * library, wt3d_gemm_noalloc_max_floats() floats (64 MiB) held on every GPU
+ * that loads the library until the process exits.  For callers that cannot
+ * call cudaMalloc (device memory owned by another allocator or budget, or a
+ * path that must not pay for allocation and its device synchronisation).
+ * Problems needing more than the limit (2 M Kr + 4 N Kr floats, Kr = 2K
+ * rounded up to 64) are rejected with WT3D_ERR_ARG.  The first call on a
+ * device resolves the scratch address on that device.  All calls share the
+ * scratch, so calls that overlap on the GPU race.  Runs on `stream`
+ * (cudaStream_t, NULL = default) and returns when the product is complete. */
+long long wt3d_gemm_noalloc_max_floats(void);
+int wt3d_gemm_noalloc(int M, int N, int K, const void *dA, int lda, const void *dB, int ldb, void *dC, int ldc,
+                      void *stream);
+
 /* Last error message of the calling thread (static storage). */
 const char *wt3d_last_error(void);
 
