@@ -41,6 +41,7 @@ constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
 constexpr int TC_THREADS = 192;
 constexpr unsigned TC_WAIT_LIMIT = 1u << 24;
+constexpr int TC_GROUP = 8;                 // row panels per rasterisation group
 
 // ---------------------------------------------------------------------------
 // PTX helpers
@@ -238,8 +239,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     const TcTask &t = tasks[lo_t];
     const long long lt = gt - t.tile0;
-    const int m0 = (int)(lt / t.tiles_n) * TC_BM;
-    const int n0r = (int)(lt % t.tiles_n) * TC_BNR;
+    // Grouped rasterisation: consecutive CTAs sweep a band of TC_GROUP row
+    // panels column by column, so a wave of resident CTAs shares a compact set
+    // of A and B panels in L2 instead of streaming all of B per row panel.
+    const int tiles_m = (t.M + TC_BM - 1) / TC_BM;
+    const long long per_group = (long long)TC_GROUP * t.tiles_n;
+    const int group = (int)(lt / per_group);
+    const int first_m = group * TC_GROUP;
+    const int gsize = min(tiles_m - first_m, TC_GROUP);
+    const int in_group = (int)(lt % per_group);
+    const int m0 = (first_m + in_group % gsize) * TC_BM;
+    const int n0r = (in_group / gsize) * TC_BNR;
     const int nk = t.Kr / TC_BK;
 
     if (warp == 0) {
