@@ -157,6 +157,46 @@ int wt3d_solve_device(wt3d_solver *h, int nrhs, const void *d_B, void *d_X,
 /* y = A x with the assembled complex128 operator (host arrays), for checks. */
 int wt3d_apply(wt3d_solver *h, int nrhs, const double _Complex *X, double _Complex *Y);
 
+/* y = A x on device arrays (complex128, column-major n x nrhs).  No
+ * reference counterpart (the reference never applies A outside STRUMPACK). */
+int wt3d_apply_device(wt3d_solver *h, int nrhs, const void *d_X, void *d_Y);
+
+/* Re-assemble the complex128 operator from the handle's current model
+ * (wt3d_set_model) at the last factored omega, keeping the factors.  Later
+ * solves refine against the new operator with the old factors as the
+ * preconditioner, which converges while the model change is small (model
+ * perturbations, line searches).  No reference counterpart. */
+int wt3d_update_operator(wt3d_solver *h);
+
+/* ---- adjoint-state gradient --------------------------------------------
+ * No counterpart on the reference's path: wtomo3d's gradient lives outside
+ * the forward-modelling routines.  The operator differentiated is the one
+ * ASMBLE builds (asmble.f90:96-601) from the Lame arrays of
+ * modelio.f90:78-92, with respect to the model arrays (Vp, Vs, rho) of the
+ * handle's current model at the last factored omega, including the
+ * mass-lumping weights (calcwts.f:1-75) and the PML stretch's dependence on
+ * the centre node's vp (pml3d.f:201-295).
+ *
+ * Contraction: grad[0..nn) = dchi/dVp, grad[nn..2nn) = dchi/dVs,
+ * grad[2nn..3nn) = dchi/drho at every node (nn = nx*ny*nz, model order), with
+ *     dchi/dm = -Re sum_j lam_j^H (dA/dm) u_j .
+ * d_U: forward wavefields (the total field for plane waves), d_Lam: adjoint
+ * wavefields, both device complex128 column-major n x nrhs; d_grad: device
+ * double[3*nn]. */
+int wt3d_gradient_contract(wt3d_solver *h, int nrhs, const void *d_U, const void *d_Lam, void *d_grad);
+
+/* Waveform misfit chi = 1/2 sum_j sum_r |u_j(rec_r) - dobs|^2 over the three
+ * components of nrec receivers at grid nodes rec_node[] (0-based node
+ * indices), and its gradient.  Forward: X = A^-1 F (d_F device n x nsrc),
+ * total field u = X + U0 (d_U0 device or NULL).  Adjoint: A^H lam =
+ * R^T (R u - dobs) with the resident factors.  dobs, dpred (may be NULL):
+ * host complex128 [(j*nrec + r)*3 + c]; grad: host double[3*nn] as above.
+ * Both solves refine to tol.  Returns WT3D_ERR_NOCONV (with outputs filled)
+ * if a solve did not reach tol. */
+int wt3d_misfit_gradient(wt3d_solver *h, int nsrc, const void *d_F, const void *d_U0, int nrec,
+                         const long long *rec_node, const double _Complex *dobs, double tol, int maxit,
+                         double *chi, double *grad, double _Complex *dpred);
+
 /* Statistics of the last factorisation. */
 typedef struct wt3d_stats {
     long long n, nnz;              /* unknowns, operator nonzeros             */
@@ -170,6 +210,7 @@ typedef struct wt3d_stats {
     int       levels;              /* depth of the elimination tree + 1       */
     int       kernels_factor;      /* kernels launched by the last factor call */
     int       kernels_solve;       /* kernels launched by the last solve call  */
+    double    t_gradient_ms;       /* last gradient contraction               */
 } wt3d_stats;
 int wt3d_get_stats(const wt3d_solver *h, wt3d_stats *st);
 

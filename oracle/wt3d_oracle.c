@@ -144,6 +144,92 @@ long long ora_point_source(const ora_grid *g, double xloc, double yloc, double z
 #undef LOGR
 #undef FN
 
+/* ---------------------------------------------------------------------- */
+/* Adjoint-state gradient in FP64 by central differences of node blocks.  */
+/* The reference has no gradient code on this path; this differentiates   */
+/* the restated ASMBLE operator numerically, independently of the GPU's    */
+/* analytic per-row derivatives.  For every node g and each of lambda, mu  */
+/* and rho (the Lame arrays of modelio.f90:78-92), the array entry at g is */
+/* moved by +-h (h = 1e-6 of the node's stiffness or density scale) and    */
+/* the blocks of the 27 rows that read node g are recomputed               */
+/* (setcoefs3d + fdfd3d, asmble.f90:96-601):                               */
+/*     dchi/dp = -Re sum_j lam_j^H (dA/dp) u_j,                            */
+/* then mu = Vs^2 rho, lambda = Vp^2 rho - 2 mu give (Vp, Vs, rho).        */
+/* ---------------------------------------------------------------------- */
+static void row_blocks_c128(const ora_grid *g, const double complex *da, const double complex *mu,
+                            const double *ro, double complex om, double pmld, double pmlf, int ipml,
+                            int iz, int ix, int iy, double complex blk[27][3][3], int act[27])
+{
+    coefs_c128 c;
+    setcoefs3d_c128(g, da, mu, ro, iz, ix, iy, &c);
+    for (int s = 0; s < 27; s++) {
+        act[s] = slot_active_c128(g, s, iz, ix, iy);
+        if (act[s]) fdfd3d_c128(g, &c, om, g->dx, pmld, pmlf, ipml, s, iz, ix, iy, blk[s]);
+    }
+}
+
+int ora_gradient_c128(const ora_grid *g, const float *vp, const float *vs, const float *rho,
+                      double omega_re, double omega_im, int nrhs, const double complex *U,
+                      const double complex *L, double *grad)
+{
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+    const long long nn = (long long)nx * ny * nz, n = 3 * nn;
+    double complex *da = (double complex *)malloc(sizeof(double complex) * nn);
+    double complex *mu = (double complex *)malloc(sizeof(double complex) * nn);
+    double *ro = (double *)malloc(sizeof(double) * nn);
+    if (!da || !mu || !ro) { free(da); free(mu); free(ro); return 1; }
+    lame_c128(nn, vp, vs, rho, da, mu, ro);
+    double pmld, pmlf; int ipml;
+    pml_params_c128(g, &pmld, &pmlf, &ipml);
+    const double complex om = omega_re + omega_im * I;
+    for (int iy = 1; iy <= ny; iy++)
+    for (int ix = 1; ix <= nx; ix++)
+    for (int iz = 1; iz <= nz; iz++) {
+        const long long off = (iz - 1) + (long long)nz * (ix - 1) + (long long)nz * nx * (iy - 1);
+        const double scale_s = fmax(fabs(creal(da[off])), fabs(creal(mu[off])));
+        double dl[3];
+        for (int p = 0; p < 3; p++) {
+            const double h = 1e-6 * (p < 2 ? scale_s : ro[off]);
+            double complex acc = 0;
+            for (int ry = iy - 1; ry <= iy + 1; ry++)
+            for (int rx = ix - 1; rx <= ix + 1; rx++)
+            for (int rz = iz - 1; rz <= iz + 1; rz++) {
+                if (ry < 1 || ry > ny || rx < 1 || rx > nx || rz < 1 || rz > nz) continue;
+                double complex bp[27][3][3], bm[27][3][3];
+                int act[27];
+                for (int sg = 0; sg < 2; sg++) {
+                    const double d = sg == 0 ? h : -h;
+                    if (p == 0) da[off] += d; else if (p == 1) mu[off] += d; else ro[off] += d;
+                    row_blocks_c128(g, da, mu, ro, om, pmld, pmlf, ipml, rz, rx, ry, sg == 0 ? bp : bm, act);
+                    if (p == 0) da[off] -= d; else if (p == 1) mu[off] -= d; else ro[off] -= d;
+                }
+                const long long row = (rz - 1) + (long long)nz * (rx - 1) + (long long)nz * nx * (ry - 1);
+                for (int s = 0; s < 27; s++) {
+                    if (!act[s]) continue;
+                    const int dy = s / 9 - 1, dxo = (s / 3) % 3 - 1, dz = s % 3 - 1;
+                    const long long nb = row + dz + (long long)nz * dxo + (long long)nz * nx * dy;
+                    for (int a = 0; a < 3; a++)
+                        for (int b = 0; b < 3; b++) {
+                            const double complex dB = (bp[s][a][b] - bm[s][a][b]) / (2.0 * h);
+                            if (dB == 0) continue;
+                            double complex t = 0;
+                            for (int j = 0; j < nrhs; j++)
+                                t += conj(L[(long long)j * n + 3 * row + a]) * U[(long long)j * n + 3 * nb + b];
+                            acc += dB * t;
+                        }
+                }
+            }
+            dl[p] = -creal(acc);
+        }
+        const double P = vp[off], S = vs[off], R = rho[off];
+        grad[off] = 2.0 * P * R * dl[0];
+        grad[nn + off] = 2.0 * S * R * dl[1] - 4.0 * S * R * dl[0];
+        grad[2 * nn + off] = (P * P - 2.0 * S * S) * dl[0] + S * S * dl[1] + dl[2];
+    }
+    free(da); free(mu); free(ro);
+    return 0;
+}
+
 int ora_assemble_c128(const ora_grid *g, const float *vp, const float *vs, const float *rho,
                       double omega_re, double omega_im, const int *irptr, double complex *a)
 {

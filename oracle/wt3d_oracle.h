@@ -67,6 +67,14 @@ int ora_node_blocks_c128(const ora_grid *g, const float *vp, const float *vs, co
                          double omega_re, double omega_im, int iz, int ix, int iy,
                          double complex *blk /*27*9*/, int *active /*27*/);
 
+/* FP64 adjoint-state gradient by central differences of node blocks.
+ * U (forward) and L (adjoint) wavefields: complex128, column-major 3nn x nrhs.
+ * grad[3*nn] = (dchi/dVp, dchi/dVs, dchi/drho) per node, with
+ * dchi/dm = -Re sum_j L_j^H (dA/dm) U_j for the operator ora_assemble_c128 builds. */
+int ora_gradient_c128(const ora_grid *g, const float *vp, const float *vs, const float *rho,
+                      double omega_re, double omega_im, int nrhs, const double complex *U,
+                      const double complex *L, double *grad);
+
 /* CSR complex128 SpMV y = A x (1-based CSR). */
 void ora_spmv_c128(int n, const int *irptr, const int *jcptr, const double complex *a,
                    const double complex *x, double complex *y);

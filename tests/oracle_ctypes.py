@@ -35,6 +35,8 @@ class Oracle:
         L.ora_node_blocks_c128.argtypes = [ctypes.POINTER(OGrid), vp, vp, vp, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp]
         L.ora_spmv_c128.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp]
+        L.ora_gradient_c128.argtypes = [ctypes.POINTER(OGrid), vp, vp, vp, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_int, vp, vp, vp]
         L.ora_haskgrn.argtypes = [ctypes.c_int, vp, vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, vp]
         self.L = L
@@ -77,6 +79,21 @@ class Oracle:
         ierr = self.L.ora_node_blocks_c128(ctypes.byref(og), _p(vp), _p(vs), _p(rho), om.real, om.imag,
                                            iz, ix, iy, _p(blk), _p(act))
         return blk.reshape(27, 3, 3), act, ierr
+
+    def gradient(self, g, vp, vs, rho, omega, U, Lam):
+        """FP64 gradient (dchi/dVp, dchi/dVs, dchi/drho), each (nz, nx, ny),
+        of dchi/dm = -Re sum_j Lam_j^H dA/dm U_j; U, Lam are (3nn, nrhs)."""
+        og = self.grid(g)
+        vp, vs, rho = [np.ascontiguousarray(np.asarray(x, np.float32).reshape(-1, order="F")) for x in (vp, vs, rho)]
+        U = np.asfortranarray(np.asarray(U, np.complex128).reshape(len(vp) * 3, -1))
+        Lam = np.asfortranarray(np.asarray(Lam, np.complex128).reshape(len(vp) * 3, -1))
+        assert U.shape == Lam.shape
+        grad = np.zeros(3 * len(vp), np.float64)
+        om = complex(omega)
+        rc = self.L.ora_gradient_c128(ctypes.byref(og), _p(vp), _p(vs), _p(rho), om.real, om.imag, U.shape[1],
+                                      _p(U), _p(Lam), _p(grad))
+        assert rc == 0
+        return [grad[k * len(vp):(k + 1) * len(vp)].reshape((g.nz, g.nx, g.ny), order="F") for k in range(3)]
 
     def haskgrn(self, vp, vs, rho, ztop, omega, ain, nz, dz, s_wave=False, zorig=0.0):
         arr = [np.ascontiguousarray(a, np.float64) for a in (vp, vs, rho, ztop)]

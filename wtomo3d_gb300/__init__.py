@@ -88,7 +88,8 @@ class Stats(ctypes.Structure):
                 ("t_analyse_ms", ctypes.c_double), ("t_assemble_ms", ctypes.c_double),
                 ("t_factor_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double),
                 ("perturbed_pivots", ctypes.c_int), ("levels", ctypes.c_int),
-                ("kernels_factor", ctypes.c_int), ("kernels_solve", ctypes.c_int)]
+                ("kernels_factor", ctypes.c_int), ("kernels_solve", ctypes.c_int),
+                ("t_gradient_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -122,6 +123,11 @@ def lib():
         L.wt3d_solve_device.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_double, ctypes.c_int, vp, vp,
                                         ctypes.c_int]
         L.wt3d_apply.argtypes = [vp, ctypes.c_int, vp, vp]
+        L.wt3d_apply_device.argtypes = [vp, ctypes.c_int, vp, vp]
+        L.wt3d_update_operator.argtypes = [vp]
+        L.wt3d_gradient_contract.argtypes = [vp, ctypes.c_int, vp, vp, vp]
+        L.wt3d_misfit_gradient.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, ctypes.c_double,
+                                           ctypes.c_int, vp, vp, vp]
         L.wt3d_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
         L.wt3d_get_stream.restype = vp
         L.wt3d_get_stream.argtypes = [vp]
@@ -249,6 +255,51 @@ class Solver:
         Y = np.empty_like(Xf, order="F")
         _check(lib().wt3d_apply(self._h, Xf.shape[1], _ptr(Xf), _ptr(Y)))
         return Y[:, 0] if one else Y
+
+    def apply_device(self, d_X, d_Y, nrhs):
+        """Y = A X on device arrays (column-major n x nrhs complex128)."""
+        _check(lib().wt3d_apply_device(self._h, int(nrhs), ctypes.c_void_p(d_X), ctypes.c_void_p(d_Y)))
+
+    def update_operator(self):
+        """Re-assemble A from the current model at the factored omega; the
+        factors stay and precondition later solves."""
+        _check(lib().wt3d_update_operator(self._h))
+
+    def _split_grad(self, g):
+        nn, G = self.grid.nnodes, self.grid
+        return [g[k * nn:(k + 1) * nn].reshape((G.nz, G.nx, G.ny), order="F") for k in range(3)]
+
+    def gradient_contract(self, d_U, d_Lam, nrhs, d_grad=None):
+        """-Re sum_j Lam_j^H dA/dm U_j for m = (Vp, Vs, rho) at every node.
+        With d_grad (device double[3*nn]) writes there; otherwise returns
+        three host arrays of shape (nz, nx, ny)."""
+        if d_grad is not None:
+            _check(lib().wt3d_gradient_contract(self._h, int(nrhs), ctypes.c_void_p(d_U), ctypes.c_void_p(d_Lam),
+                                                ctypes.c_void_p(d_grad)))
+            return None
+        import torch
+        g = torch.empty(3 * self.grid.nnodes, dtype=torch.float64, device="cuda")
+        _check(lib().wt3d_gradient_contract(self._h, int(nrhs), ctypes.c_void_p(d_U), ctypes.c_void_p(d_Lam),
+                                            ctypes.c_void_p(g.data_ptr())))
+        return self._split_grad(g.cpu().numpy())
+
+    def misfit_gradient(self, d_F, d_U0, nsrc, rec_node, dobs, tol=1e-8, maxit=20, allow_noconv=False):
+        """Waveform misfit 1/2 sum |u(rec) - dobs|^2 and its gradient.
+        d_F: device scattered-field (or point) RHS, d_U0: device background
+        field or None; rec_node: 0-based node indices; dobs: complex
+        [(j*nrec + r)*3 + c].  Returns (chi, [dVp, dVs, drho], dpred)."""
+        rec = np.ascontiguousarray(rec_node, np.int64)
+        dobs = np.ascontiguousarray(dobs, np.complex128).reshape(-1)
+        if dobs.size != nsrc * len(rec) * 3:
+            raise ValueError("dobs must hold nsrc * nrec * 3 values")
+        chi = ctypes.c_double(0)
+        grad = np.zeros(3 * self.grid.nnodes)
+        dpred = np.zeros_like(dobs)
+        rc = lib().wt3d_misfit_gradient(self._h, int(nsrc), ctypes.c_void_p(d_F), ctypes.c_void_p(d_U0 or 0),
+                                        len(rec), _ptr(rec), _ptr(dobs), tol, maxit, ctypes.byref(chi),
+                                        _ptr(grad), _ptr(dpred))
+        _check(rc, allow=(WT3D_ERR_NOCONV,) if allow_noconv else ())
+        return chi.value, self._split_grad(grad), dpred
 
     @property
     def stream(self):

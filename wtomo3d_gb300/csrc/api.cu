@@ -30,6 +30,16 @@ __global__ void k_rm_to_cm(long long n, int m, const double2 *__restrict__ rm, d
     for (int j = 0; j < m; j++) cm[(long long)j * n + i] = rm[i * MAXRHS + j];
 }
 
+__global__ void k_rm_to_cm_neg(long long n, int m, const double2 *__restrict__ rm, double2 *__restrict__ cm)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int j = 0; j < m; j++) {
+        const double2 v = rm[i * MAXRHS + j];
+        cm[(long long)j * n + i] = make_double2(-v.x, -v.y);
+    }
+}
+
 // R = B - op(A) X (op = A or A^H), per-column squared norms of R into nr and of B into nb.
 __global__ void __launch_bounds__(256) k_residual(long long n, int m, const int *__restrict__ irptr,
                                                   const int *__restrict__ jcptr, const double2 *__restrict__ a,
@@ -147,6 +157,7 @@ struct wt3d_solver {
     bool have_bg = false;
     double om_re = 0, om_im = 0;          // omega of the assembled operator
     DevVec<double> norms;
+    DevVec<double> gscr;                  // per-row derivative records of the gradient
     std::unique_ptr<Engine<float>> e32;
     std::unique_ptr<Engine<double>> e64;
     cudaStream_t st = nullptr;
@@ -627,6 +638,97 @@ int wt3d_apply(wt3d_solver *h, int nrhs, const double _Complex *X, double _Compl
     std::complex<double> *Yc = reinterpret_cast<std::complex<double> *>(Y);
     for (size_t i = 0; i < tmp.size(); i++) Yc[i] = -tmp[i];
     return WT3D_OK;
+}
+
+int wt3d_apply_device(wt3d_solver *h, int nrhs, const void *d_X, void *d_Y)
+{
+    if (!h || nrhs < 1 || !d_X || !d_Y) { set_error("wt3d_apply_device: bad arguments"); return WT3D_ERR_ARG; }
+    if (!h->have_values) { set_error("no operator"); return WT3D_ERR_STATE; }
+    const long long n = h->n;
+    for (int c0 = 0; c0 < nrhs; c0 += MAXRHS) {
+        int m = std::min(MAXRHS, nrhs - c0);
+        k_cm_to_rm<<<ceil_div(n, 256), 256, 0, h->st>>>(n, m, (const double2 *)d_X + (long long)c0 * n, h->Xn.p);
+        WT_CUDA(cudaMemsetAsync(h->Bn.p, 0, sizeof(double2) * n * MAXRHS, h->st));
+        WT_CUDA(cudaMemsetAsync(h->norms.p, 0, sizeof(double) * 2 * MAXRHS, h->st));
+        // R = 0 - A X, then Y = -R
+        k_residual<<<152 * 8, 256, 0, h->st>>>(n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, h->Xn.p, h->Bn.p,
+                                               h->Rn.p, h->norms.p, h->norms.p + MAXRHS, 0);
+        k_rm_to_cm_neg<<<ceil_div(n, 256), 256, 0, h->st>>>(n, m, h->Rn.p, (double2 *)d_Y + (long long)c0 * n);
+    }
+    WT_CUDA(cudaGetLastError());
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    return WT3D_OK;
+}
+
+int wt3d_update_operator(wt3d_solver *h)
+{
+    if (!h) { set_error("null handle"); return WT3D_ERR_ARG; }
+    if (!h->have_model || !h->have_values) { set_error("wt3d_update_operator: needs a model and a factored operator"); return WT3D_ERR_STATE; }
+    int rc = device_assemble(h->grid, h->da.p, h->mu.p, h->ro.p, h->om_re, h->om_im, h->irptr.p, h->a.p, h->st);
+    if (rc) return rc;
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    return WT3D_OK;
+}
+
+int wt3d_gradient_contract(wt3d_solver *h, int nrhs, const void *d_U, const void *d_Lam, void *d_grad)
+{
+    if (!h || nrhs < 1 || !d_U || !d_Lam || !d_grad) { set_error("wt3d_gradient_contract: bad arguments"); return WT3D_ERR_ARG; }
+    if (!h->have_model || !h->have_values) { set_error("wt3d_gradient_contract: needs a model and an assembled operator"); return WT3D_ERR_STATE; }
+    const long long nn = h->n / 3;
+    int rc;
+    if (!h->gscr.p && (rc = h->gscr.alloc((size_t)gradient_scratch_doubles(nn)))) return rc;
+    cudaEventRecord(h->ev0, h->st);
+    if ((rc = device_gradient(h->grid, h->da.p, h->mu.p, h->ro.p, h->vp.p, h->vs.p, h->rho.p, h->om_re, h->om_im,
+                              nrhs, h->n, d_U, d_Lam, h->gscr.p, (double *)d_grad, h->st)))
+        return rc;
+    cudaEventRecord(h->ev1, h->st);
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    h->stats.t_gradient_ms = ms_between(h->ev0, h->ev1);
+    return WT3D_OK;
+}
+
+int wt3d_misfit_gradient(wt3d_solver *h, int nsrc, const void *d_F, const void *d_U0, int nrec,
+                         const long long *rec_node, const double _Complex *dobs, double tol, int maxit, double *chi,
+                         double *grad, double _Complex *dpred)
+{
+    if (!h || nsrc < 1 || !d_F || nrec < 1 || !rec_node || !dobs || !chi || !grad) {
+        set_error("wt3d_misfit_gradient: bad arguments");
+        return WT3D_ERR_ARG;
+    }
+    if (!h->have_factor || !h->have_model) { set_error("wt3d_misfit_gradient: needs a model and a factor"); return WT3D_ERR_STATE; }
+    const long long n = h->n, nn = n / 3;
+    for (int r = 0; r < nrec; r++)
+        if (rec_node[r] < 0 || rec_node[r] >= nn) { set_error("wt3d_misfit_gradient: receiver node out of range"); return WT3D_ERR_ARG; }
+    const long long nd = (long long)nsrc * nrec * 3;
+    DevVec<double2> X, S, Lm, dd, dp, dr;
+    DevVec<long long> drec;
+    DevVec<double> dg;
+    int rc;
+    if ((rc = X.alloc((size_t)n * nsrc)) || (rc = S.alloc((size_t)n * nsrc)) || (rc = Lm.alloc((size_t)n * nsrc)) ||
+        (rc = dd.alloc(nd)) || (rc = dp.alloc(nd)) || (rc = dr.alloc(nd)) || (rc = drec.alloc(nrec)) ||
+        (rc = dg.alloc(3 * nn)))
+        return rc;
+    WT_CUDA(cudaMemcpyAsync(drec.p, rec_node, sizeof(long long) * nrec, cudaMemcpyHostToDevice, h->st));
+    WT_CUDA(cudaMemcpyAsync(dd.p, dobs, sizeof(double2) * nd, cudaMemcpyHostToDevice, h->st));
+    // forward wavefields; the total field adds the background u0
+    int rcf = solve_dev_cm(h, nsrc, (const double2 *)d_F, X.p, tol, maxit, nullptr, nullptr, false);
+    if (rcf && rcf != WT3D_ERR_NOCONV) return rcf;
+    if (d_U0 && (rc = device_add(n * nsrc, d_U0, X.p, h->st))) return rc;
+    WT_CUDA(cudaMemsetAsync(S.p, 0, sizeof(double2) * n * nsrc, h->st));
+    if ((rc = device_receivers(nsrc, nrec, n, drec.p, X.p, dd.p, dp.p, dr.p, S.p, h->st))) return rc;
+    std::vector<double2> res(nd);
+    WT_CUDA(cudaMemcpyAsync(res.data(), dr.p, sizeof(double2) * nd, cudaMemcpyDeviceToHost, h->st));
+    if (dpred) WT_CUDA(cudaMemcpyAsync(dpred, dp.p, sizeof(double2) * nd, cudaMemcpyDeviceToHost, h->st));
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    double c = 0;
+    for (const double2 &e : res) c += e.x * e.x + e.y * e.y;
+    *chi = 0.5 * c;
+    // adjoint wavefields: A^H lam = R^T (R u - d), reusing the factors
+    int rca = solve_dev_cm(h, nsrc, S.p, Lm.p, tol, maxit, nullptr, nullptr, true);
+    if (rca && rca != WT3D_ERR_NOCONV) return rca;
+    if ((rc = wt3d_gradient_contract(h, nsrc, X.p, Lm.p, dg.p))) return rc;
+    WT_CUDA(cudaMemcpy(grad, dg.p, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost));
+    return rcf ? rcf : rca;
 }
 
 int wt3d_get_stats(const wt3d_solver *h, wt3d_stats *st)

@@ -87,31 +87,10 @@ __global__ void __launch_bounds__(128) k_assemble(AsmParams p, const cx<R> *__re
     const int ix = (int)((g / p.nz) % p.nx);
     const int iy = (int)(g / ((long long)p.nz * p.nx));
     // 1-based indices as the reference uses them
-    const int jz = iz + 1, jx = ix + 1, jy = iy + 1;
-
-    unsigned mask = 0;
-#pragma unroll
-    for (int s = 0; s < 27; s++) {
-        int dy = s / 9 - 1, dxo = (s / 3) % 3 - 1, dz = s % 3 - 1;
-        bool ok = (iy + dy >= 0) && (iy + dy < p.ny) && (ix + dxo >= 0) && (ix + dxo < p.nx) &&
-                  (iz + dz >= 0) && (iz + dz < p.nz);
-        mask |= (ok ? 1u : 0u) << s;
-    }
-
-    // region dispatch of FDFD3D (fdfd3d.f:53-115)
-    const bool xyin = (jx > p.ipml) && (jx <= p.nx - p.ipml) && (jy > p.ipml) && (jy <= p.ny - p.ipml);
-    int region = REG_STENCIL;
-    int zidx = jz;  // z index fed to the stretch factor (0 = z stretch off)
-    // Interior nodes (all axes inside) can never sit on the outer faces, so the
-    // Dirichlet test may come first.  Above the bottom of the top PML layer a
-    // free surface switches the z stretch off: PFDFD3D when x and y are
-    // interior, PML3D evaluated at iz = ipml+1 otherwise.
-    if (jz == p.nz || jx == 1 || jx == p.nx || jy == 1 || jy == p.ny) region = REG_FIXED;
-    else if (jz <= p.ipml) {
-        if (jz == 1 && !p.fst) region = REG_FIXED;
-        else if (jz == 1 && !p.usemin) region = REG_TPFREE;
-        else if (p.fst) zidx = xyin ? 0 : p.ipml + 1;
-    }
+    const int jx = ix + 1, jy = iy + 1;
+    unsigned mask;
+    int region, zidx;
+    node_region(p, iz, ix, iy, region, zidx, mask);
 
     NodeCoefs<R> c;
     Stretch<R> f;

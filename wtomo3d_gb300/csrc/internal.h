@@ -18,6 +18,15 @@ int device_lame(long long nn, const float *d_vp, const float *d_vs, const float 
 int device_assemble(const wt3d_grid &g, const void *d_da, const void *d_mu, const double *d_ro, double om_re,
                     double om_im, const int *d_irptr, void *d_a, cudaStream_t st);
 
+// ---- adjoint gradient (gradient.cu) --------------------------------------
+long long gradient_scratch_doubles(long long nn);
+int device_gradient(const wt3d_grid &g, const void *d_da, const void *d_mu, const double *d_ro, const float *d_vp,
+                    const float *d_vs, const float *d_rho, double om_re, double om_im, int m, long long ld,
+                    const void *d_U, const void *d_L, double *d_D, double *d_grad, cudaStream_t st);
+int device_receivers(int m, int nrec, long long ld, const long long *d_rec, const void *d_U, const void *d_dobs,
+                     void *d_pred, void *d_res, void *d_S, cudaStream_t st);
+int device_add(long long total, const void *d_a, void *d_y, cudaStream_t st);
+
 // ---- symbolic analysis (symbolic.cpp) -------------------------------------
 // Nested dissection of the nx*ny*nz grid with one-node-thick plane
 // separators, and the multifrontal symbolic factorisation of the 3-dof

@@ -378,4 +378,35 @@ struct AsmParams {
     double om_re, om_im;
 };
 
+// Region dispatch of FDFD3D (fdfd3d.f:53-115) for the 0-based node (iz,ix,iy).
+// zidx is the z index fed to the stretch factor (0 = z stretch off); mask has
+// bit s set for every slot whose neighbour lies inside the grid.
+__device__ __forceinline__ void node_region(const AsmParams &p, int iz, int ix, int iy, int &region, int &zidx,
+                                            unsigned &mask)
+{
+    mask = 0;
+#pragma unroll
+    for (int s = 0; s < 27; s++) {
+        int dy = s / 9 - 1, dxo = (s / 3) % 3 - 1, dz = s % 3 - 1;
+        bool ok = (iy + dy >= 0) && (iy + dy < p.ny) && (ix + dxo >= 0) && (ix + dxo < p.nx) &&
+                  (iz + dz >= 0) && (iz + dz < p.nz);
+        mask |= (ok ? 1u : 0u) << s;
+    }
+    // 1-based indices as the reference uses them
+    const int jz = iz + 1, jx = ix + 1, jy = iy + 1;
+    const bool xyin = (jx > p.ipml) && (jx <= p.nx - p.ipml) && (jy > p.ipml) && (jy <= p.ny - p.ipml);
+    region = REG_STENCIL;
+    zidx = jz;
+    // Interior nodes (all axes inside) can never sit on the outer faces, so the
+    // Dirichlet test may come first.  Above the bottom of the top PML layer a
+    // free surface switches the z stretch off: PFDFD3D when x and y are
+    // interior, PML3D evaluated at iz = ipml+1 otherwise.
+    if (jz == p.nz || jx == 1 || jx == p.nx || jy == 1 || jy == p.ny) region = REG_FIXED;
+    else if (jz <= p.ipml) {
+        if (jz == 1 && !p.fst) region = REG_FIXED;
+        else if (jz == 1 && !p.usemin) region = REG_TPFREE;
+        else if (p.fst) zidx = xyin ? 0 : p.ipml + 1;
+    }
+}
+
 }  // namespace wt3d

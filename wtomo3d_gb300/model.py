@@ -78,3 +78,22 @@ def layered1d(nz, dx, layer_vp=(3000.0, 4000.0, 5000.0, 6000.0), vpvs=1.73):
     vs = (vp / vpvs).astype(np.float32).astype(np.float64)
     rho = (310.0 * np.power(vp, 0.25)).astype(np.float32).astype(np.float64)
     return vp, vs, rho, ztop
+
+
+def perturbed(vp, vs, dx, seed, std=0.03, corr_len=200.0):
+    """Multiplicative seeded Gaussian-correlated perturbation (std `std`) of
+    Vp and Vs; rho recomputed from the perturbed Vp by Gardner's relation."""
+    nz, nx, ny = np.shape(vp)
+    d = correlated_field(nx, ny, nz, dx, corr_len, seed)
+    vp2 = np.asarray(vp, np.float64) * (1.0 + std * d)
+    vs2 = np.asarray(vs, np.float64) * (1.0 + std * d)
+    return vp2.astype(np.float32), vs2.astype(np.float32), gardner(vp2)
+
+
+def surface_receivers(nx, ny, nz, ipml, nrx=8, nry=5, depth=0):
+    """0-based node indices of nrx x nry receivers on a regular grid at node
+    depth `depth`, spread over the area inside the lateral absorbing layers."""
+    ix = np.rint(np.linspace(ipml, nx - 1 - ipml, nrx)).astype(np.int64)
+    iy = np.rint(np.linspace(ipml, ny - 1 - ipml, nry)).astype(np.int64)
+    IY, IX = np.meshgrid(iy, ix, indexing="ij")
+    return (depth + nz * IX + nz * nx * IY).reshape(-1)
