@@ -211,8 +211,18 @@ typedef struct wt3d_stats {
     int       kernels_factor;      /* kernels launched by the last factor call */
     int       kernels_solve;       /* kernels launched by the last solve call  */
     double    t_gradient_ms;       /* last gradient contraction               */
+    double    workspace_bytes;     /* factorisation workspace shared by the
+                                      handles of this grid and precision     */
 } wt3d_stats;
 int wt3d_get_stats(const wt3d_solver *h, wt3d_stats *st);
+
+/* Device memory of a handle for grid g, before creating it (host analysis
+ * only, cached per grid): out[0] = bytes a factored handle holds on its own,
+ * out[1] = additional bytes once plane-wave sources are built (background
+ * operator), out[2] = level-parity update buffers of the factorisation
+ * workspace, shared by all handles of the same grid and precision (their
+ * factorisations are serialised).  No reference counterpart. */
+int wt3d_solver_bytes(const wt3d_grid *g, int precision, double *out);
 
 /* Host-only view of the analysis (nested dissection + symbolic
  * factorisation; no GPU needed).  info[8] = {fronts, factor entries, levels,

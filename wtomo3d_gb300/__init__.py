@@ -89,7 +89,7 @@ class Stats(ctypes.Structure):
                 ("t_factor_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double),
                 ("perturbed_pivots", ctypes.c_int), ("levels", ctypes.c_int),
                 ("kernels_factor", ctypes.c_int), ("kernels_solve", ctypes.c_int),
-                ("t_gradient_ms", ctypes.c_double)]
+                ("t_gradient_ms", ctypes.c_double), ("workspace_bytes", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -124,6 +124,7 @@ def lib():
                                         ctypes.c_int]
         L.wt3d_apply.argtypes = [vp, ctypes.c_int, vp, vp]
         L.wt3d_apply_device.argtypes = [vp, ctypes.c_int, vp, vp]
+        L.wt3d_solver_bytes.argtypes = [ctypes.POINTER(Grid), ctypes.c_int, vp]
         L.wt3d_update_operator.argtypes = [vp]
         L.wt3d_gradient_contract.argtypes = [vp, ctypes.c_int, vp, vp, vp]
         L.wt3d_misfit_gradient.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, ctypes.c_double,
@@ -185,6 +186,14 @@ def assemble(grid, vp, vs, rho, omega):
     om = complex(omega)
     _check(lib().wt3d_assemble(ctypes.byref(grid), _ptr(vp), _ptr(vs), _ptr(rho), om.real, om.imag, _ptr(a)))
     return a
+
+
+def solver_bytes(grid, precision=PREC_MIXED):
+    """(resident, plane-wave extra, shared workspace) device bytes of a
+    handle for `grid`, from the host analysis (cached per grid)."""
+    out = np.zeros(3)
+    _check(lib().wt3d_solver_bytes(ctypes.byref(grid), int(precision), _ptr(out)))
+    return float(out[0]), float(out[1]), float(out[2])
 
 
 class Solver:

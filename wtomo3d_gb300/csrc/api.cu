@@ -3,7 +3,9 @@
 // the complex64 multifrontal factorisation.
 #include "engine.cuh"
 #include "wtomo3d_gpu.h"
+#include <array>
 #include <chrono>
+#include <map>
 #include <complex>
 #include <cstring>
 #include <mutex>
@@ -141,10 +143,25 @@ __global__ void k_c64_to_c128(long long n, const float2 *__restrict__ s, double2
 
 using namespace wt3d;
 
+namespace wt3d {
+// Host analysis of one grid, shared by every handle of that grid: nested
+// dissection + symbolic factorisation, the CSR -> front scatter map and the
+// transposed CSR positions, and the factorisation workspaces of both
+// precisions (alive while a handle uses them).
+struct GridAnalysis {
+    Symbolic sym;
+    std::vector<long long> map;
+    std::vector<int> tpos;
+    std::mutex mu;
+    std::weak_ptr<FactorWorkspace<float>> ws32;
+    std::weak_ptr<FactorWorkspace<double>> ws64;
+};
+}  // namespace wt3d
+
 struct wt3d_solver {
     wt3d_grid grid{};
     int prec = WT3D_PREC_MIXED;
-    Symbolic sym;
+    std::shared_ptr<GridAnalysis> ga;
     long long n = 0, nnz = 0;
     DevVec<int> irptr, jcptr, tpos, perm;
     DevVec<double2> a;
@@ -285,6 +302,52 @@ int solve_dev_cm(wt3d_solver *h, int nrhs, const double2 *d_B, double2 *d_X, dou
     return worst_rc;
 }
 
+std::mutex g_ana_mu;
+std::map<std::array<int, 3>, std::shared_ptr<GridAnalysis>> g_ana;
+
+// Symbolic analysis of an nx*ny*nz grid, computed once per process.
+int grid_analysis(int nx, int ny, int nz, std::shared_ptr<GridAnalysis> &out)
+{
+    std::lock_guard<std::mutex> lk(g_ana_mu);
+    auto &slot = g_ana[{nx, ny, nz}];
+    if (!slot) {
+        auto ga = std::make_shared<GridAnalysis>();
+        int rc = symbolic_grid(nx, ny, nz, 64, ga->sym);
+        if (rc) { g_ana.erase({nx, ny, nz}); return rc; }
+        slot = ga;
+    }
+    out = slot;
+    return WT3D_OK;
+}
+
+// Device bytes a handle holds on its own once created and factored:
+// out[0] always, out[1] more once plane-wave sources are built, out[2] the
+// level-parity update buffers of the shared factorisation workspace.
+void handle_bytes(const Symbolic &S, long long nnz, int prec, double *out)
+{
+    const double n = (double)S.n, nn = n / 3, sz = prec == WT3D_PREC_MIXED ? 8.0 : 16.0;
+    long long npan = 0;
+    for (const Front &F : S.fronts) npan += (F.p + KB - 1) / KB;
+    const double engine = (double)S.fac_total * sz + n * MAXRHS * sz + (double)npan * 2 * KB * KB * sz + n * 4 +
+                          (double)(S.border.size() + S.rel.size()) * 4 + (double)S.fronts.size() * sizeof(FrontDev) +
+                          (double)nnz * 8 + n * 8;
+    const double api = (n + 1) * 4 + (double)nnz * (4 + 16 + 4) + n * 4 + 3 * n * MAXRHS * 16 + nn * (12 + 32 + 8);
+    out[0] = engine + api;
+    out[1] = (double)nnz * 16 + nn * (32 + 8);
+    out[2] = ((double)std::max<long long>(S.upd_size[0], 1) + (double)std::max<long long>(S.upd_size[1], 1)) * sz;
+}
+
+// Device bytes a handle currently holds (the shared workspace excluded).
+double own_bytes(const wt3d_solver *h)
+{
+    double b = (double)(h->e32 ? h->e32->device_bytes() : h->e64->device_bytes());
+    b += (double)(h->irptr.n + h->jcptr.n + h->tpos.n + h->perm.n) * 4;
+    b += (double)(h->a.n + h->da.n + h->mu.n + h->Bn.n + h->Xn.n + h->Rn.n + h->T1.n + h->abg.n + h->bgda.n +
+                  h->bgmu.n) * 16;
+    b += (double)(h->ro.n + h->bgro.n + h->norms.n + h->gscr.n) * 8 + (double)(h->vp.n + h->vs.n + h->rho.n) * 4;
+    return b;
+}
+
 }  // namespace
 
 extern "C" {
@@ -376,48 +439,64 @@ int wt3d_solver_create(wt3d_solver **out, const wt3d_grid *g, int precision)
     std::unique_ptr<wt3d_solver> h(new wt3d_solver());
     h->grid = *g;
     h->prec = precision;
-    if ((rc = symbolic_grid(g->nx, g->ny, g->nz, 64, h->sym))) return rc;
-    h->n = h->sym.n;
+    if ((rc = grid_analysis(g->nx, g->ny, g->nz, h->ga))) return rc;
+    GridAnalysis &ga = *h->ga;
+    const Symbolic &sym = ga.sym;
+    h->n = sym.n;
     h->nnz = wt3d_pattern_nnz(g->nx, g->ny, g->nz);
     WT_CUDA(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
     WT_CUDA(cudaEventCreate(&h->ev0));
     WT_CUDA(cudaEventCreate(&h->ev1));
     if ((rc = h->irptr.alloc(h->n + 1)) || (rc = h->jcptr.alloc(h->nnz)) || (rc = h->a.alloc(h->nnz))) return rc;
     if ((rc = device_pattern(g->nx, g->ny, g->nz, 0, h->irptr.p, h->jcptr.p, h->st))) return rc;
-    std::vector<int> hir(h->n + 1), hjc(h->nnz);
-    WT_CUDA(cudaMemcpyAsync(hir.data(), h->irptr.p, sizeof(int) * (h->n + 1), cudaMemcpyDeviceToHost, h->st));
-    WT_CUDA(cudaMemcpyAsync(hjc.data(), h->jcptr.p, sizeof(int) * h->nnz, cudaMemcpyDeviceToHost, h->st));
-    WT_CUDA(cudaStreamSynchronize(h->st));
-    std::vector<long long> map;
-    if ((rc = scatter_map(h->sym, hir, hjc, map))) return rc;
+    std::shared_ptr<FactorWorkspace<float>> w32;
+    std::shared_ptr<FactorWorkspace<double>> w64;
     {
-        // transposed positions for the adjoint residual
-        std::vector<int> tp(h->nnz), cur(hir.begin(), hir.end() - 1);
-        for (long long r = 0; r < h->n; r++)
-            for (long long k = hir[r]; k < hir[r + 1]; k++) tp[k] = cur[hjc[k]]++;
-        if ((rc = h->tpos.upload(tp))) return rc;
+        std::lock_guard<std::mutex> lk(ga.mu);
+        if (ga.map.empty()) {
+            std::vector<int> hir(h->n + 1), hjc(h->nnz);
+            WT_CUDA(cudaMemcpyAsync(hir.data(), h->irptr.p, sizeof(int) * (h->n + 1), cudaMemcpyDeviceToHost, h->st));
+            WT_CUDA(cudaMemcpyAsync(hjc.data(), h->jcptr.p, sizeof(int) * h->nnz, cudaMemcpyDeviceToHost, h->st));
+            WT_CUDA(cudaStreamSynchronize(h->st));
+            std::vector<long long> map;
+            if ((rc = scatter_map(sym, hir, hjc, map))) return rc;
+            // transposed positions for the adjoint residual
+            std::vector<int> tp(h->nnz), cur(hir.begin(), hir.end() - 1);
+            for (long long r = 0; r < h->n; r++)
+                for (long long k = hir[r]; k < hir[r + 1]; k++) tp[k] = cur[hjc[k]]++;
+            ga.map.swap(map);
+            ga.tpos.swap(tp);
+        }
+        if (precision == WT3D_PREC_MIXED) {
+            if (!(w32 = ga.ws32.lock())) { w32 = std::make_shared<FactorWorkspace<float>>(); ga.ws32 = w32; }
+        } else {
+            if (!(w64 = ga.ws64.lock())) { w64 = std::make_shared<FactorWorkspace<double>>(); ga.ws64 = w64; }
+        }
     }
-    if ((rc = h->perm.upload(h->sym.perm))) return rc;
+    if ((rc = h->tpos.upload(ga.tpos))) return rc;
+    if ((rc = h->perm.upload(sym.perm))) return rc;
     if ((rc = h->Bn.alloc((size_t)h->n * MAXRHS)) || (rc = h->Xn.alloc((size_t)h->n * MAXRHS)) ||
         (rc = h->Rn.alloc((size_t)h->n * MAXRHS)) || (rc = h->norms.alloc(2 * MAXRHS)))
         return rc;
     if (precision == WT3D_PREC_MIXED) {
         h->e32.reset(new Engine<float>());
-        rc = h->e32->init(h->sym, map, h->irptr.p, h->jcptr.p);
+        rc = h->e32->init(sym, ga.map, h->irptr.p, h->jcptr.p, w32);
     } else {
         h->e64.reset(new Engine<double>());
-        rc = h->e64->init(h->sym, map, h->irptr.p, h->jcptr.p);
+        rc = h->e64->init(sym, ga.map, h->irptr.p, h->jcptr.p, w64);
     }
     if (rc) return rc;
     auto t1 = std::chrono::steady_clock::now();
     h->stats.n = h->n;
     h->stats.nnz = h->nnz;
-    h->stats.nfronts = (long long)h->sym.fronts.size();
-    h->stats.factor_entries = h->sym.fac_total;
-    h->stats.factor_flops = h->sym.flops;
-    h->stats.factor_bytes = (double)h->sym.fac_total * (precision == WT3D_PREC_MIXED ? 8.0 : 16.0);
-    h->stats.levels = (int)h->sym.levels.size();
+    h->stats.nfronts = (long long)sym.fronts.size();
+    h->stats.factor_entries = sym.fac_total;
+    h->stats.factor_flops = sym.flops;
+    h->stats.factor_bytes = (double)sym.fac_total * (precision == WT3D_PREC_MIXED ? 8.0 : 16.0);
+    h->stats.levels = (int)sym.levels.size();
     h->stats.t_analyse_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    h->stats.device_bytes = own_bytes(h.get());
+    h->stats.workspace_bytes = (double)(h->e32 ? h->e32->workspace_bytes() : h->e64->workspace_bytes());
     *out = h.release();
     return WT3D_OK;
 }
@@ -450,17 +529,22 @@ int wt3d_set_model(wt3d_solver *h, const float *vp, const float *vs, const float
 static int factor_values(wt3d_solver *h)
 {
     int np = 0, rc;
-    cudaEventRecord(h->ev0, h->st);
-    if (h->e32) rc = h->e32->factor(h->a.p, h->nnz, h->st, &np);
-    else rc = h->e64->factor(h->a.p, h->nnz, h->st, &np);
-    if (rc) return rc;
-    cudaEventRecord(h->ev1, h->st);
-    WT_CUDA(cudaStreamSynchronize(h->st));
+    {
+        // the update buffers are shared by the handles of this grid: one
+        // factorisation at a time, until its kernels have finished
+        std::lock_guard<std::mutex> lk(h->e32 ? h->e32->ws->mu : h->e64->ws->mu);
+        cudaEventRecord(h->ev0, h->st);
+        if (h->e32) rc = h->e32->factor(h->a.p, h->nnz, h->st, &np);
+        else rc = h->e64->factor(h->a.p, h->nnz, h->st, &np);
+        if (rc) return rc;
+        cudaEventRecord(h->ev1, h->st);
+        WT_CUDA(cudaStreamSynchronize(h->st));
+    }
     h->stats.t_factor_ms = ms_between(h->ev0, h->ev1);
     h->stats.perturbed_pivots = np;
     h->stats.kernels_factor = 2 + (h->e32 ? h->e32->fsched->kernels() : h->e64->fsched->kernels());
-    h->stats.device_bytes = (double)(h->e32 ? h->e32->device_bytes() : h->e64->device_bytes()) +
-                            (double)h->nnz * (16 + 4 + 4) + (double)h->n * MAXRHS * 16 * 3;
+    h->stats.device_bytes = own_bytes(h);
+    h->stats.workspace_bytes = (double)(h->e32 ? h->e32->workspace_bytes() : h->e64->workspace_bytes());
     h->have_factor = true;
     return WT3D_OK;
 }
@@ -735,6 +819,19 @@ int wt3d_get_stats(const wt3d_solver *h, wt3d_stats *st)
 {
     if (!h || !st) return WT3D_ERR_ARG;
     *st = h->stats;
+    st->device_bytes = own_bytes(h);
+    st->workspace_bytes = (double)(h->e32 ? h->e32->workspace_bytes() : h->e64->workspace_bytes());
+    return WT3D_OK;
+}
+
+int wt3d_solver_bytes(const wt3d_grid *g, int precision, double *out)
+{
+    if (!out) { set_error("wt3d_solver_bytes: null output"); return WT3D_ERR_ARG; }
+    int rc = check_grid(g);
+    if (rc) return rc;
+    std::shared_ptr<GridAnalysis> ga;
+    if ((rc = grid_analysis(g->nx, g->ny, g->nz, ga))) return rc;
+    handle_bytes(ga->sym, wt3d_pattern_nnz(g->nx, g->ny, g->nz), precision, out);
     return WT3D_OK;
 }
 

@@ -10,6 +10,7 @@
 #include <functional>
 #include <map>
 #include <memory>
+#include <mutex>
 
 namespace wt3d {
 
@@ -49,11 +50,23 @@ struct Schedule {
     }
 };
 
+// Buffers a factorisation needs only while it runs: the two level-parity
+// update buffers and the tensor-core split-operand workspace.  Handles of the
+// same grid and precision share one; `mu` serialises their factorisations.
+template <class T>
+struct FactorWorkspace {
+    DevVec<cx<T>> upd0, upd1;
+    DevVec<float> tcws;
+    std::mutex mu;
+    size_t bytes() const { return (upd0.n + upd1.n) * sizeof(cx<T>) + tcws.n * sizeof(float); }
+};
+
 template <class T>
 class Engine {
 public:
     const Symbolic *S = nullptr;
-    DevVec<cx<T>> fac, upd0, upd1, X, dinv;   // dinv: per KB panel L_D^{-1}, U_D^{-1} (KB x KB each)
+    DevVec<cx<T>> fac, X, dinv;   // dinv: per KB panel L_D^{-1}, U_D^{-1} (KB x KB each)
+    std::shared_ptr<FactorWorkspace<T>> ws;
     DevVec<int> ipiv, border;
     DevVec<int> rel;
     DevVec<FrontDev> fr;
@@ -66,29 +79,40 @@ public:
     double pivot_rel = 1e-20;
     // tcgen05 path for complex64 front updates (WT3D_TC=0 selects the SIMT kernel)
     bool use_tc = std::is_same<T, float>::value && !(getenv("WT3D_TC") && getenv("WT3D_TC")[0] == '0');
-    DevVec<float> tcws;                                 // tensor-core split-operand workspace
+    DevVec<float> own_tcws;   // private split workspace, only if the shared one is too small
     DevVec<int> tc_err;                                 // barrier-timeout flag of the tensor-core kernel
     std::vector<Schedule<T> *> built_tc;   // only (near-)zero pivots are replaced: Dirichlet rows carry unit pivots next to O(1e8) stiffness entries
     bool use_graphs = true;
 
+    // device bytes this engine holds on its own (the shared workspace excluded)
     size_t device_bytes() const
     {
-        return fac.n * sizeof(cx<T>) + (upd0.n + upd1.n + X.n) * sizeof(cx<T>) + (ipiv.n + border.n + rel.n) * 4 +
-               fr.n * sizeof(FrontDev) + map.n * 8;
+        return (fac.n + X.n + dinv.n) * sizeof(cx<T>) + (ipiv.n + border.n + rel.n) * 4 + fr.n * sizeof(FrontDev) +
+               map.n * 8 + scale.n * 8 + own_tcws.n * sizeof(float);
     }
+    size_t workspace_bytes() const { return ws ? ws->bytes() : 0; }
+    // split workspace of the tensor-core launches: private if allocated, else the shared one
+    float *tcws_base() const { return own_tcws.p ? own_tcws.p : ws->tcws.p; }
+    size_t tcws_size() const { return own_tcws.p ? own_tcws.n : ws->tcws.n; }
 
     const int *d_irptr = nullptr, *d_jcptr = nullptr;   // natural 0-based CSR of the operator
     DevVec<double> scale;                              // Jacobi scaling 1/sqrt|a_ii|, natural ordering
 
-    int init(const Symbolic &sym, const std::vector<long long> &hmap, const int *irp, const int *jcp)
+    int init(const Symbolic &sym, const std::vector<long long> &hmap, const int *irp, const int *jcp,
+             std::shared_ptr<FactorWorkspace<T>> w)
     {
         S = &sym;
         d_irptr = irp;
         d_jcptr = jcp;
+        ws = w ? w : std::make_shared<FactorWorkspace<T>>();
         int rc;
         if ((rc = fac.alloc(sym.fac_total))) return rc;
-        if ((rc = upd0.alloc(std::max<long long>(sym.upd_size[0], 1)))) return rc;
-        if ((rc = upd1.alloc(std::max<long long>(sym.upd_size[1], 1)))) return rc;
+        {
+            std::lock_guard<std::mutex> lk(ws->mu);
+            const size_t n0 = std::max<long long>(sym.upd_size[0], 1), n1 = std::max<long long>(sym.upd_size[1], 1);
+            if (ws->upd0.n < n0 && (rc = ws->upd0.alloc(n0))) return rc;
+            if (ws->upd1.n < n1 && (rc = ws->upd1.alloc(n1))) return rc;
+        }
         if ((rc = X.alloc((size_t)sym.n * MAXRHS))) return rc;
         if ((rc = ipiv.alloc(sym.n))) return rc;
         if ((rc = border.upload(sym.border))) return rc;
@@ -116,8 +140,8 @@ public:
         }
         if ((rc = fr.upload(h))) return rc;
         if ((rc = dinv.alloc((size_t)npan * 2 * KB * KB))) return rc;
-        static bool attr_done = false;
-        if (!attr_done) {
+        static std::once_flag attr_once;
+        std::call_once(attr_once, [] {
             size_t sp = sizeof(cx<T>) * (KB * (KB + 1) + 2 * KB * (KB + 1));
             cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp);
             cudaFuncSetAttribute(k_trsm_row<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -126,8 +150,7 @@ public:
                                  (int)(sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1))));
             cudaFuncSetAttribute(k_diag_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1))));
-            attr_done = true;
-        }
+        });
         return build_factor_schedule();
     }
 
@@ -218,15 +241,23 @@ public:
         if constexpr (std::is_same<T, float>::value) {
             long long need = 0;
             for (auto &v : sc.tc_pending) need = std::max(need, tc_workspace_floats(v.data(), (int)v.size()));
-            if (need > (long long)tcws.n) {
-                int rc = tcws.alloc(need);
+            if (need > 0 && tcws_base() == nullptr) {
+                // first user of the shared workspace sizes it
+                std::lock_guard<std::mutex> lk(ws->mu);
+                if (ws->tcws.n == 0) {
+                    int rc = ws->tcws.alloc(need);
+                    if (rc) return rc;
+                }
+            }
+            if (need > (long long)tcws_size()) {
+                int rc = own_tcws.alloc(need);
                 if (rc) return rc;
                 // schedules built earlier point into the old workspace: rebuild their maps
                 for (auto *o : built_tc) {
                     for (size_t i = 0; i < o->tc_pending.size(); i++) {
                         o->tc[i].reset(new TcLaunch());
                         if ((rc = tc_build_launch(*o->tc[i], o->tc_pending[i].data(), (int)o->tc_pending[i].size(),
-                                                  tcws.p)))
+                                                  tcws_base())))
                             return rc;
                     }
                     if (o->graph) { cudaGraphExecDestroy(o->graph); o->graph = nullptr; }
@@ -235,7 +266,7 @@ public:
             sc.tc.clear();
             for (auto &v : sc.tc_pending) {
                 sc.tc.emplace_back(new TcLaunch());
-                int rc = tc_build_launch(*sc.tc.back(), v.data(), (int)v.size(), tcws.p);
+                int rc = tc_build_launch(*sc.tc.back(), v.data(), (int)v.size(), tcws_base());
                 if (rc) return rc;
             }
             built_tc.push_back(&sc);
@@ -254,7 +285,7 @@ public:
         Schedule<T> *psc = sc.get();
         const Symbolic &sym = *S;
         cx<T> *F = fac.p;
-        cx<T> *U[2] = {upd0.p, upd1.p};
+        cx<T> *U[2] = {ws->upd0.p, ws->upd1.p};
         // zero the factor pool, scale and scatter the operator
         {
             cx<T> *fp = F; size_t bytes = fac.n * sizeof(cx<T>);
@@ -298,7 +329,7 @@ public:
                     int nt = (int)(he.size() - b0);
                     sc->launches.push_back({[psc, this, b0, nt, rows](cudaStream_t st) {
                         k_extend_add<T><<<ceil_div(rows * 32, 256), 256, 0, st>>>(
-                            psc->ea.p + b0, nt, rows, fr.p, rel.p, fac.p, upd0.p, upd1.p);
+                            psc->ea.p + b0, nt, rows, fr.p, rel.p, fac.p, ws->upd0.p, ws->upd1.p);
                     }, LK_EXTEND_ADD, 0});
                 }
             }

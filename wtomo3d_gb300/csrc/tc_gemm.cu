@@ -370,15 +370,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // ---------------------------------------------------------------------------
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
+    // thread-safe one-time lookup (function-local static initialisation)
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
+            return (PFN_cuTensorMapEncodeTiled_v12000)p;
+        return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    }();
     return fn;
 }
 
@@ -479,11 +480,9 @@ void tc_mma(const TcLaunch &L, int *err, cudaStream_t st)
 
 int tc_init()
 {
-    static bool done = false;
-    if (done) return WT3D_OK;
+    // idempotent; safe to call from several threads
     WT_CUDA(cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     if (!encode_fn()) { set_error("cuTensorMapEncodeTiled unavailable"); return WT3D_ERR_CUDA; }
-    done = true;
     return WT3D_OK;
 }
 
