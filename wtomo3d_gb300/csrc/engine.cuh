@@ -82,7 +82,8 @@ public:
     DevVec<float> own_tcws;   // private split workspace, only if the shared one is too small
     DevVec<int> tc_err;                                 // barrier-timeout flag of the tensor-core kernel
     std::vector<Schedule<T> *> built_tc;   // only (near-)zero pivots are replaced: Dirichlet rows carry unit pivots next to O(1e8) stiffness entries
-    bool use_graphs = true;
+    // launch schedules as captured CUDA graphs (WT3D_GRAPHS=0: direct launches, for profilers)
+    bool use_graphs = !(getenv("WT3D_GRAPHS") && getenv("WT3D_GRAPHS")[0] == '0');
 
     // device bytes this engine holds on its own (the shared workspace excluded)
     size_t device_bytes() const
