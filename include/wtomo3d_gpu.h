@@ -254,6 +254,14 @@ int wt3d_profile_factor(wt3d_solver *h, double *out);
  * out[11] = ms of one FP64 residual over m columns.  out holds 12 doubles. */
 int wt3d_profile_solve(wt3d_solver *h, int m, double *out);
 
+/* Per-launch profile of the factor schedule (which = 0; factors the current
+ * operator) or of one substitution pass over m <= 32 columns (which = 1):
+ * out[4i..4i+3] = launch kind (0 memset, 1 scatter, 2 extend-add, 3 panel,
+ * 4 trsm, 5 SIMT GEMM, 6 diagonal solve, 7 tensor-core split, 8 tensor-core
+ * GEMM), milliseconds, real flops, operand bytes; at most cap launches are
+ * written and *count receives the number of launches. */
+int wt3d_profile_launches(wt3d_solver *h, int which, int m, double *out, int cap, int *count);
+
 /* Copy internal device state to the host for checks (what = 0: factor pool,
  * complex entries of the handle's precision; 1: pivot indices). */
 int wt3d_debug_fetch(wt3d_solver *h, int what, void *out, long long count);

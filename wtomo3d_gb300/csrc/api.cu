@@ -43,6 +43,11 @@ __global__ void k_rm_to_cm_neg(long long n, int m, const double2 *__restrict__ r
 }
 
 // R = B - op(A) X (op = A or A^H), per-column squared norms of R into nr and of B into nb.
+// One warp per grid node; lane l holds right-hand sides l and l + 32
+// (MAXRHS = 64).  The node's three rows (u, v, w) are contiguous in the CSR
+// and share one column list, so each column index and each row of X is
+// loaded once for the three rows.
+static_assert(MAXRHS == 64, "k_residual maps two right-hand sides to a lane");
 __global__ void __launch_bounds__(256) k_residual(long long n, int m, const int *__restrict__ irptr,
                                                   const int *__restrict__ jcptr, const double2 *__restrict__ a,
                                                   const int *__restrict__ tpos, const double2 *__restrict__ X,
@@ -52,43 +57,52 @@ __global__ void __launch_bounds__(256) k_residual(long long n, int m, const int 
     const int lane = threadIdx.x & 31;
     const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-    double sr0 = 0, sr1 = 0, sb0 = 0, sb1 = 0;
-    const int j0 = lane, j1 = lane + 32;
-    for (long long i = w0; i < n; i += nw) {
-        double2 acc0 = make_double2(0, 0), acc1 = make_double2(0, 0);
-        for (int k = irptr[i]; k < irptr[i + 1]; k++) {
-            double2 av;
-            if (adjoint) { av = a[tpos[k]]; av.y = -av.y; }
-            else av = a[k];
-            const double2 *xr = X + (long long)jcptr[k] * MAXRHS;
-            if (j0 < m) {
-                double2 x = xr[j0];
-                acc0.x += av.x * x.x - av.y * x.y;
-                acc0.y += av.x * x.y + av.y * x.x;
-            }
-            if (j1 < m) {
-                double2 x = xr[j1];
-                acc1.x += av.x * x.x - av.y * x.y;
-                acc1.y += av.x * x.y + av.y * x.x;
+    const long long nnode = n / 3;
+    const bool on[2] = {lane < m, lane + 32 < m};
+    double sr[2] = {0, 0}, sb[2] = {0, 0};
+    for (long long g = w0; g < nnode; g += nw) {
+        const long long r0 = 3 * g;
+        const int k0 = irptr[r0];
+        const int len = irptr[r0 + 1] - k0;
+        double2 acc[3][2];
+#pragma unroll
+        for (int q = 0; q < 3; q++) acc[q][0] = acc[q][1] = make_double2(0, 0);
+#pragma unroll 3
+        for (int t = 0; t < len; t++) {
+            const int k = k0 + t;
+            const double2 *xr = X + (long long)jcptr[k] * MAXRHS + lane;
+            double2 x[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) x[h] = on[h] ? xr[32 * h] : make_double2(0, 0);
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                double2 av;
+                if (adjoint) { av = a[tpos[k + q * len]]; av.y = -av.y; }
+                else av = a[k + q * len];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    acc[q][h].x = fma(av.x, x[h].x, fma(-av.y, x[h].y, acc[q][h].x));
+                    acc[q][h].y = fma(av.x, x[h].y, fma(av.y, x[h].x, acc[q][h].y));
+                }
             }
         }
-        if (j0 < m) {
-            double2 b = B[i * MAXRHS + j0];
-            double2 r = make_double2(b.x - acc0.x, b.y - acc0.y);
-            R[i * MAXRHS + j0] = r;
-            sr0 += r.x * r.x + r.y * r.y;
-            sb0 += b.x * b.x + b.y * b.y;
-        }
-        if (j1 < m) {
-            double2 b = B[i * MAXRHS + j1];
-            double2 r = make_double2(b.x - acc1.x, b.y - acc1.y);
-            R[i * MAXRHS + j1] = r;
-            sr1 += r.x * r.x + r.y * r.y;
-            sb1 += b.x * b.x + b.y * b.y;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if (!on[h]) continue;
+            const int j = lane + 32 * h;
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                const double2 b = B[(r0 + q) * MAXRHS + j];
+                const double2 r = make_double2(b.x - acc[q][h].x, b.y - acc[q][h].y);
+                R[(r0 + q) * MAXRHS + j] = r;
+                sr[h] += r.x * r.x + r.y * r.y;
+                sb[h] += b.x * b.x + b.y * b.y;
+            }
         }
     }
-    if (j0 < m) { atomicAdd(&nr[j0], sr0); atomicAdd(&nb[j0], sb0); }
-    if (j1 < m) { atomicAdd(&nr[j1], sr1); atomicAdd(&nb[j1], sb1); }
+#pragma unroll
+    for (int h = 0; h < 2; h++)
+        if (on[h]) { atomicAdd(&nr[lane + 32 * h], sr[h]); atomicAdd(&nb[lane + 32 * h], sb[h]); }
 }
 
 // Xs = S R (new ordering, engine precision); S the Jacobi scaling of the factor.
@@ -976,6 +990,48 @@ extern "C" int wt3d_profile_solve(wt3d_solver *h, int m, double *out)
     cudaEventRecord(h->ev1, h->st);
     WT_CUDA(cudaStreamSynchronize(h->st));
     out[11] = ms_between(h->ev0, h->ev1);
+    return WT3D_OK;
+}
+
+// Per-launch profile of the factor schedule (which = 0) or of one substitution
+// pass over m columns (which = 1, forward + backward, whatever X holds):
+// out[4i..4i+3] = kind (LaunchKind), ms, real flops, operand bytes; at most
+// cap launches are written, *count receives the schedule's launch count.
+extern "C" int wt3d_profile_launches(wt3d_solver *h, int which, int m, double *out, int cap, int *count)
+{
+    if (!h || !out || !count || !h->have_values || (which == 1 && (!h->have_factor || m < 1 || m > MAXRHS)))
+        return WT3D_ERR_STATE;
+    std::vector<float> ms;
+    const std::vector<LaunchRec> *recs = nullptr;
+    int rc;
+    if (h->e32) {
+        Engine<float> &E = *h->e32;
+        if (which == 0) { rc = E.profile_factor_each(h->a.p, h->nnz, h->st, ms); recs = &E.fsched->launches; }
+        else {
+            Schedule<float> *sc = E.solve_schedule(m, false);
+            if (!sc) return WT3D_ERR_NOMEM;
+            rc = E.profile_each(*sc, h->st, ms);
+            recs = &sc->launches;
+        }
+    } else {
+        Engine<double> &E = *h->e64;
+        if (which == 0) { rc = E.profile_factor_each(h->a.p, h->nnz, h->st, ms); recs = &E.fsched->launches; }
+        else {
+            Schedule<double> *sc = E.solve_schedule(m, false);
+            if (!sc) return WT3D_ERR_NOMEM;
+            rc = E.profile_each(*sc, h->st, ms);
+            recs = &sc->launches;
+        }
+    }
+    if (rc) return rc;
+    if (which == 0) h->have_factor = true;
+    *count = (int)ms.size();
+    for (int i = 0; i < (int)ms.size() && i < cap; i++) {
+        out[4 * i] = (*recs)[i].kind;
+        out[4 * i + 1] = ms[i];
+        out[4 * i + 2] = (*recs)[i].flops;
+        out[4 * i + 3] = (*recs)[i].bytes;
+    }
     return WT3D_OK;
 }
 

@@ -23,7 +23,8 @@ enum LaunchKind { LK_MEMSET = 0, LK_SCATTER, LK_EXTEND_ADD, LK_PANEL, LK_TRSM, L
 struct LaunchRec {
     Launch fn;
     int kind;
-    double flops;   // real-flop count of a GEMM launch (sum of 8 M N K)
+    double flops;        // real-flop count of a GEMM launch (sum of 8 M N K)
+    double bytes = 0;    // operand bytes of a GEMM launch (A, B read; C read and written)
 };
 
 // A list of launches plus the task arrays they read.
@@ -161,7 +162,7 @@ public:
                          const int *crow = nullptr, int conjA = 0)
     {
         if (M <= 0 || N <= 0 || K <= 0) return;
-        GemmTask<T> g;
+        GemmTask<T> g{};
         g.A = A; g.B = B; g.C = C; g.brow = brow; g.crow = crow;
         g.lda = lda; g.ldb = ldb; g.ldc = ldc; g.M = M; g.N = N; g.K = K;
         g.tiles_n = (N + GBN - 1) / GBN;
@@ -169,6 +170,11 @@ public:
         g.conjA = conjA;
         tiles += (long long)((M + GBM - 1) / GBM) * g.tiles_n;
         v.push_back(g);
+    }
+
+    static double gemm_bytes(const GemmTask<T> &g)
+    {
+        return ((double)g.M * g.K + (double)g.K * g.N + 2.0 * g.M * g.N) * sizeof(cx<T>);
     }
 
     // Appends the launches for GEMM tasks [b, end) of `all`: tasks the
@@ -185,14 +191,14 @@ public:
                 else simt.push_back(all[i]);
             }
             if (!tcv.empty()) {
-                double fl = 0;
-                for (auto &g : tcv) fl += 8.0 * g.M * (double)g.N * g.K;
+                double fl = 0, by = 0;
+                for (auto &g : tcv) { fl += 8.0 * g.M * (double)g.N * g.K; by += gemm_bytes(g); }
                 const int idx = (int)sc.tc_pending.size();
                 sc.tc_pending.push_back(std::move(tcv));
                 Schedule<T> *psc = &sc;
                 sc.launches.push_back({[psc, idx](cudaStream_t st) { tc_split(*psc->tc[idx], st); }, LK_SPLIT, 0});
                 sc.launches.push_back({[psc, idx, this](cudaStream_t st) { tc_mma(*psc->tc[idx], tc_err.p, st); },
-                                       LK_TCGEMM, fl});
+                                       LK_TCGEMM, fl, by});
             }
         } else {
             simt.assign(all.begin() + b, all.end());
@@ -204,34 +210,56 @@ public:
         for (auto &g : simt) (g.N <= TSBN ? narrow : wide).push_back(g);
         Schedule<T> *psc = &sc;
         if (!narrow.empty()) {
+            // split-K: tasks whose K exceeds a chunk sized for ~8 CTAs per SM
+            // over the whole launch are cut into K-chunks that subtract their
+            // partial products atomically
+            double work = 0;
+            for (auto &g : narrow) work += (double)((g.M + TSBM - 1) / TSBM) * g.K;
+            const int kchunk = std::max(256, (int)((work / (8.0 * 152) + TSBK - 1) / TSBK) * TSBK);
+            std::vector<GemmTask<T>> split;
+            for (auto &g : narrow) {
+                if (g.K <= kchunk + kchunk / 2) { split.push_back(g); continue; }
+                for (int k0 = 0; k0 < g.K; k0 += kchunk) {
+                    GemmTask<T> c = g;
+                    c.K = std::min(kchunk, g.K - k0);
+                    c.A = g.conjA ? g.A + (long long)k0 * g.lda : g.A + k0;
+                    if (g.brow) c.brow = g.brow + k0;
+                    else c.B = g.B + (long long)k0 * g.ldb;
+                    c.atom = 1;
+                    split.push_back(c);
+                }
+            }
+            narrow.swap(split);
             const size_t b0 = all.size();
             long long tiles = 0;
-            double fl = 0;
+            double fl = 0, by = 0;
             for (auto &g : narrow) {
                 g.tile0 = tiles;
                 tiles += (g.M + TSBM - 1) / TSBM;
                 fl += 8.0 * g.M * (double)g.N * g.K;
+                by += gemm_bytes(g);
                 all.push_back(g);
             }
             const int nt = (int)narrow.size();
             sc.launches.push_back({[psc, b0, nt, tiles](cudaStream_t st) {
                 k_gemm_ts<T><<<(unsigned)tiles, 256, 0, st>>>(psc->gemm.p + b0, nt);
-            }, LK_GEMM, fl});
+            }, LK_GEMM, fl, by});
         }
         if (!wide.empty()) {
             const size_t b0 = all.size();
             long long tiles = 0;
-            double fl = 0;
+            double fl = 0, by = 0;
             for (auto &g : wide) {
                 g.tile0 = tiles;
                 tiles += (long long)((g.M + GBM - 1) / GBM) * g.tiles_n;
                 fl += 8.0 * g.M * (double)g.N * g.K;
+                by += gemm_bytes(g);
                 all.push_back(g);
             }
             const int nt = (int)wide.size();
             sc.launches.push_back({[psc, b0, nt, tiles](cudaStream_t st) {
                 k_gemm<T><<<(unsigned)tiles, 256, 0, st>>>(psc->gemm.p + b0, nt);
-            }, LK_GEMM, fl});
+            }, LK_GEMM, fl, by});
         }
     }
 
@@ -447,7 +475,7 @@ public:
             if (!np) return;
             sc->launches.push_back({[psc, this, p0, np, smd, m, mode, Xp, ldx](cudaStream_t st) {
                 k_diag_solve<T><<<np, 256, smd, st>>>(psc->panel.p + p0, fr.p, dinv.p, ipiv.p, Xp, ldx, m, mode);
-            }, LK_DIAG, 0});
+            }, LK_DIAG, 0, (double)np * (KB * KB + 2.0 * KB * m) * sizeof(cx<T>)});
         };
         // ---- forward sweep: leaves to root ----
         for (int L = nlev - 1; L >= 0; L--) {
@@ -579,6 +607,34 @@ public:
     // Factorisation with one event pair around every launch (no graph):
     // out[k] = milliseconds spent in launches of kind k, out[LK_NKINDS] =
     // GEMM real flops, out[LK_NKINDS+1] = GEMM launches.
+    // Runs a schedule once with an event pair around every launch; ms[i] per launch.
+    int profile_each(Schedule<T> &sc, cudaStream_t st, std::vector<float> &ms)
+    {
+        const size_t nl = sc.launches.size();
+        std::vector<cudaEvent_t> ev(2 * nl);
+        for (auto &e : ev) WT_CUDA(cudaEventCreate(&e));
+        for (size_t i = 0; i < nl; i++) {
+            WT_CUDA(cudaEventRecord(ev[2 * i], st));
+            sc.launches[i].fn(st);
+            WT_CUDA(cudaEventRecord(ev[2 * i + 1], st));
+        }
+        WT_CUDA(cudaStreamSynchronize(st));
+        ms.assign(nl, 0.f);
+        for (size_t i = 0; i < nl; i++) cudaEventElapsedTime(&ms[i], ev[2 * i], ev[2 * i + 1]);
+        for (auto &e : ev) cudaEventDestroy(e);
+        WT_CUDA(cudaGetLastError());
+        return WT3D_OK;
+    }
+
+    // The factor schedule under profile_each (the factorisation is complete afterwards).
+    int profile_factor_each(const double2 *d_a, long long nnz, cudaStream_t st, std::vector<float> &ms)
+    {
+        a_dev = d_a;
+        WT_CUDA(cudaMemsetAsync(maxabs.p, 0, sizeof(unsigned long long), st));
+        k_maxabs<<<1216, 256, 0, st>>>(nnz, d_a, maxabs.p);
+        return profile_each(*fsched, st, ms);
+    }
+
     int profile_factor(const double2 *d_a, long long nnz, cudaStream_t st, double *out)
     {
         a_dev = d_a;

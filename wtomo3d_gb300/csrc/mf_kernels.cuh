@@ -41,6 +41,7 @@ struct GemmTask {
     int tiles_n;
     long long tile0;
     int conjA;         // use conj(A^T): A is read as its conjugate transpose
+    int atom;          // C -= A B with atomics (a K-chunk of a split task)
 };
 
 template <class T>
@@ -518,6 +519,7 @@ __global__ void __launch_bounds__(256) k_gemm_ts(const GemmTask<T> *__restrict__
             const int c = tx + 8 * j;
             if (c >= t.N) continue;
             if (t.crow) atomic_sub(t.C + (long long)t.crow[r] * t.ldc + c, acc[i][j]);
+            else if (t.atom) atomic_sub(t.C + (long long)r * t.ldc + c, acc[i][j]);
             else {
                 cx<T> *p = t.C + (long long)r * t.ldc + c;
                 *p = *p - acc[i][j];
