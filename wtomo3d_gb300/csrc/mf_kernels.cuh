@@ -447,59 +447,82 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmTask<T> *__restrict__ ta
 // side blocks of the substitution passes): 128 x 32 tiles, 4 x 4 complex
 // outputs per thread, every A element read once per tile.
 // ---------------------------------------------------------------------------
-constexpr int TSBM = 128, TSBN = 32, TSBK = 16;
+constexpr int TSBM = 128, TSBN = 32, TSBK = 16;   // TSBK: K granularity of split-K chunks
+template <class T> struct TsCfg { static constexpr int BK = sizeof(T) == 4 ? 32 : 16; };
+
+// 128 x 32 tile per CTA of 256 threads; thread (tx, ty) owns rows 4ty..4ty+3
+// and columns 4tx..4tx+3 (16 complex accumulators).  The K loop stages
+// BK-deep slices of A (transposed in shared memory) and B, prefetching the
+// next slice into registers while the current one is consumed.
 template <class T>
-__global__ void __launch_bounds__(256) k_gemm_ts(const GemmTask<T> *__restrict__ tasks, int ntasks)
+__global__ void __launch_bounds__(256, 2) k_gemm_ts(const GemmTask<T> *__restrict__ tasks, int ntasks)
 {
-    __shared__ cx<T> As[TSBK][TSBM + 1];
-    __shared__ cx<T> Bs[TSBK][TSBN];
+    constexpr int BK = TsCfg<T>::BK;
+    constexpr int AP = TSBM + 1;                       // padded row of the A^T slice
+    constexpr int NA = TSBM * BK / 256, NB = BK * TSBN / 256;
+    __shared__ cx<T> As[BK][AP];
+    __shared__ cx<T> Bs[BK][TSBN];
     const int ti = find_task(tasks, ntasks, (long long)blockIdx.x);
     const GemmTask<T> t = tasks[ti];
     const int m0 = (int)((long long)blockIdx.x - t.tile0) * TSBM;
-    const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3;   // 8 column groups x 32 row groups
+    const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3;
     cx<T> acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; i++)
 #pragma unroll
         for (int j = 0; j < 4; j++) acc[i][j] = cx<T>(0);
-    for (int k0 = 0; k0 < t.K; k0 += TSBK) {
-        if (!t.conjA) {
+    cx<T> pa[NA], pb[NB];
+    // A slice element q of this thread: non-conjugate A is read along K
+    // (row-contiguous), the conjugate transpose along M.
+    auto load = [&](int k0) {
 #pragma unroll
-            for (int q = 0; q < (TSBM * TSBK) / 256; q++) {
-                const int idx = tid + q * 256;
-                const int i = idx / TSBK, kk = idx % TSBK;
-                const int r = m0 + i, c = k0 + kk;
-                As[kk][i] = (r < t.M && c < t.K) ? t.A[(long long)r * t.lda + c] : cx<T>(0);
-            }
-        } else {
-#pragma unroll
-            for (int q = 0; q < (TSBM * TSBK) / 256; q++) {
-                const int idx = tid + q * 256;
-                const int kk = idx / TSBM, i = idx % TSBM;
-                const int r = m0 + i, c = k0 + kk;
-                As[kk][i] = (r < t.M && c < t.K) ? conj(t.A[(long long)c * t.lda + r]) : cx<T>(0);
-            }
+        for (int q = 0; q < NA; q++) {
+            const int idx = tid + q * 256;
+            int i, kk;
+            if (!t.conjA) { i = idx / BK; kk = idx % BK; }
+            else { kk = idx / TSBM; i = idx % TSBM; }
+            const int r = m0 + i, c = k0 + kk;
+            cx<T> v(0);
+            if (r < t.M && c < t.K) v = t.conjA ? conj(t.A[(long long)c * t.lda + r]) : t.A[(long long)r * t.lda + c];
+            pa[q] = v;
         }
 #pragma unroll
-        for (int q = 0; q < (TSBK * TSBN) / 256; q++) {
+        for (int q = 0; q < NB; q++) {
             const int idx = tid + q * 256;
             const int kk = idx / TSBN, j = idx % TSBN;
             const int r = k0 + kk;
             cx<T> v(0);
-            if (r < t.K && j < t.N) {
-                const long long row = t.brow ? (long long)t.brow[r] : (long long)r;
-                v = t.B[row * t.ldb + j];
-            }
-            Bs[kk][j] = v;
+            if (r < t.K && j < t.N) v = t.B[(t.brow ? (long long)t.brow[r] : (long long)r) * t.ldb + j];
+            pb[q] = v;
         }
-        __syncthreads();
+    };
+    auto store = [&]() {
 #pragma unroll
-        for (int kk = 0; kk < TSBK; kk++) {
+        for (int q = 0; q < NA; q++) {
+            const int idx = tid + q * 256;
+            int i, kk;
+            if (!t.conjA) { i = idx / BK; kk = idx % BK; }
+            else { kk = idx / TSBM; i = idx % TSBM; }
+            As[kk][i] = pa[q];
+        }
+#pragma unroll
+        for (int q = 0; q < NB; q++) {
+            const int idx = tid + q * 256;
+            Bs[idx / TSBN][idx % TSBN] = pb[q];
+        }
+    };
+    load(0);
+    for (int k0 = 0; k0 < t.K; k0 += BK) {
+        store();
+        __syncthreads();
+        if (k0 + BK < t.K) load(k0 + BK);
+#pragma unroll
+        for (int kk = 0; kk < BK; kk++) {
             cx<T> a[4], b[4];
 #pragma unroll
-            for (int i = 0; i < 4; i++) a[i] = As[kk][ty + 32 * i];
+            for (int i = 0; i < 4; i++) a[i] = As[kk][4 * ty + i];
 #pragma unroll
-            for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx + 8 * j];
+            for (int j = 0; j < 4; j++) b[j] = Bs[kk][4 * tx + j];
 #pragma unroll
             for (int i = 0; i < 4; i++)
 #pragma unroll
@@ -512,11 +535,11 @@ __global__ void __launch_bounds__(256) k_gemm_ts(const GemmTask<T> *__restrict__
     }
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        const int r = m0 + ty + 32 * i;
+        const int r = m0 + 4 * ty + i;
         if (r >= t.M) continue;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            const int c = tx + 8 * j;
+            const int c = 4 * tx + j;
             if (c >= t.N) continue;
             if (t.crow) atomic_sub(t.C + (long long)t.crow[r] * t.ldc + c, acc[i][j]);
             else if (t.atom) atomic_sub(t.C + (long long)r * t.ldc + c, acc[i][j]);
