@@ -92,8 +92,9 @@ __global__ void __launch_bounds__(256) k_residual(long long n, int m, const int 
             const int j = lane + 32 * h;
 #pragma unroll
             for (int q = 0; q < 3; q++) {
-                const double2 b = B[(r0 + q) * MAXRHS + j];
-                const double2 r = make_double2(b.x - acc[q][h].x, b.y - acc[q][h].y);
+                // B == nullptr: R = op(A) X (the products of the Krylov solver)
+                const double2 b = B ? B[(r0 + q) * MAXRHS + j] : make_double2(0, 0);
+                const double2 r = B ? make_double2(b.x - acc[q][h].x, b.y - acc[q][h].y) : acc[q][h];
                 R[(r0 + q) * MAXRHS + j] = r;
                 sr[h] += r.x * r.x + r.y * r.y;
                 sb[h] += b.x * b.x + b.y * b.y;
@@ -103,6 +104,117 @@ __global__ void __launch_bounds__(256) k_residual(long long n, int m, const int 
 #pragma unroll
     for (int h = 0; h < 2; h++)
         if (on[h]) { atomicAdd(&nr[lane + 32 * h], sr[h]); atomicAdd(&nb[lane + 32 * h], sb[h]); }
+}
+
+// ---- batched Krylov kernels over n x MAXRHS row-major FP64 blocks -------
+// Column c of every block is an independent system; reductions go through
+// per-block partial sums and a second pass, so they do not depend on
+// scheduling.
+constexpr int GM_K = 8;          // restart length of the flexible GMRES
+constexpr int GM_BLOCKS = 304;   // 2 blocks per SM for the reductions
+
+// part[b][i][c] = sum over the rows of block b of conj(V_i[row, c]) W[row, c], i < nv.
+__global__ void __launch_bounds__(256) k_mdot(long long n, int m, int nv, const double2 *__restrict__ V,
+                                              long long vstride, const double2 *__restrict__ W,
+                                              double2 *__restrict__ part)
+{
+    __shared__ double2 red[8][MAXRHS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (int i = 0; i < nv; i++) {
+        const double2 *Vi = V + (long long)i * vstride;
+        double2 acc[2] = {make_double2(0, 0), make_double2(0, 0)};
+        for (long long r = w0; r < n; r += nw) {
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int c = lane + 32 * h;
+                if (c >= m) continue;
+                const double2 v = Vi[r * MAXRHS + c], w = W[r * MAXRHS + c];
+                acc[h].x = fma(v.x, w.x, fma(v.y, w.y, acc[h].x));
+                acc[h].y = fma(v.x, w.y, fma(-v.y, w.x, acc[h].y));
+            }
+        }
+        red[warp][lane] = acc[0];
+        red[warp][lane + 32] = acc[1];
+        __syncthreads();
+        if (threadIdx.x < MAXRHS) {
+            double2 t = make_double2(0, 0);
+            for (int q = 0; q < 8; q++) { t.x += red[q][threadIdx.x].x; t.y += red[q][threadIdx.x].y; }
+            part[((long long)blockIdx.x * (GM_K + 1) + i) * MAXRHS + threadIdx.x] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// h[i][c] = sum_b part[b][i][c]
+__global__ void k_mdot_reduce(int nblocks, int nv, const double2 *__restrict__ part, double2 *__restrict__ h)
+{
+    const int i = blockIdx.x, c = threadIdx.x;
+    if (i >= nv || c >= MAXRHS) return;
+    double2 t = make_double2(0, 0);
+    for (int b = 0; b < nblocks; b++) {
+        const double2 v = part[((long long)b * (GM_K + 1) + i) * MAXRHS + c];
+        t.x += v.x; t.y += v.y;
+    }
+    h[i * MAXRHS + c] = t;
+}
+
+// W[row, c] -= sum_{i < nv} coef[i][c] V_i[row, c]; with part != nullptr also
+// part[b][c] = per-block sum of |W_new[row, c]|^2.
+__global__ void __launch_bounds__(256) k_maxpy(long long n, int m, int nv, const double2 *__restrict__ V,
+                                               long long vstride, const double2 *__restrict__ coef,
+                                               double2 *__restrict__ W, double *__restrict__ part)
+{
+    __shared__ double red[256];
+    const long long tot = n * MAXRHS;
+    const long long stride = (long long)gridDim.x * blockDim.x;   // a multiple of MAXRHS: fixed column per thread
+    const int c = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) % MAXRHS);
+    double2 cf[GM_K + 1];
+#pragma unroll
+    for (int i = 0; i <= GM_K; i++) cf[i] = i < nv ? coef[i * MAXRHS + c] : make_double2(0, 0);
+    double s2 = 0;
+    if (c < m) {
+        for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += stride) {
+            double2 w = W[q];
+#pragma unroll
+            for (int i = 0; i <= GM_K; i++) {
+                if (i >= nv) break;
+                const double2 v = V[(long long)i * vstride + q];
+                w.x -= cf[i].x * v.x - cf[i].y * v.y;
+                w.y -= cf[i].x * v.y + cf[i].y * v.x;
+            }
+            W[q] = w;
+            s2 += w.x * w.x + w.y * w.y;
+        }
+    }
+    if (!part) return;
+    red[threadIdx.x] = s2;
+    __syncthreads();
+    if (threadIdx.x < MAXRHS) {
+        double t = 0;
+        for (int q = threadIdx.x; q < 256; q += MAXRHS) t += red[q];
+        part[(long long)blockIdx.x * MAXRHS + threadIdx.x] = t;
+    }
+}
+
+__global__ void k_norm_reduce(int nblocks, const double *__restrict__ part, double *__restrict__ out)
+{
+    const int c = threadIdx.x;
+    if (c >= MAXRHS) return;
+    double t = 0;
+    for (int b = 0; b < nblocks; b++) t += part[(long long)b * MAXRHS + c];
+    out[c] = t;
+}
+
+// W[row, c] *= s[c]
+__global__ void k_colscale(long long n, const double *__restrict__ sc, double2 *__restrict__ W)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n * MAXRHS) return;
+    const double f = sc[q % MAXRHS];
+    W[q].x *= f;
+    W[q].y *= f;
 }
 
 // Xs = S R (new ordering, engine precision); S the Jacobi scaling of the factor.
@@ -189,6 +301,9 @@ struct wt3d_solver {
     double om_re = 0, om_im = 0;          // omega of the assembled operator
     DevVec<double> norms;
     DevVec<double> gscr;                  // per-row derivative records of the gradient
+    DevVec<double2> gmV, gmZ, gmH;        // flexible GMRES: Krylov basis, preconditioned basis, projections
+    DevVec<double2> gmPart;
+    DevVec<double> gmNorm, gmScale;
     std::unique_ptr<Engine<float>> e32;
     std::unique_ptr<Engine<double>> e64;
     cudaStream_t st = nullptr;
@@ -240,7 +355,159 @@ int have_gpu()
     return WT3D_OK;
 }
 
+// Restarted flexible GMRES in FP64, right-preconditioned by the factorisation
+// (z = M^-1 v is one substitution pass), over m columns.  On entry h->Xn holds
+// the current iterate, h->Rn = B - op(A) Xn and bnorm2/rnorm2 the squared
+// column norms of B and R; on exit Xn is the new iterate.  Classical
+// Gram-Schmidt applied twice; Givens rotations and the small least-squares
+// problems per column on the host.
+template <class T>
+int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, double tol, int maxit,
+           const std::vector<double> &bnorm2, std::vector<double> &rnorm2, double *relres, int &it)
+{
+    cudaStream_t st = h->st;
+    const long long n = h->n, blk = n * MAXRHS;
+    int rc;
+    if (!h->gmV.p) {
+        if ((rc = h->gmV.alloc((size_t)blk * (GM_K + 1))) || (rc = h->gmZ.alloc((size_t)blk * GM_K)) ||
+            (rc = h->gmH.alloc((size_t)(GM_K + 1) * MAXRHS)) ||
+            (rc = h->gmPart.alloc((size_t)GM_BLOCKS * (GM_K + 1) * MAXRHS)) ||
+            (rc = h->gmNorm.alloc(MAXRHS)) || (rc = h->gmScale.alloc(MAXRHS)))
+            return rc;
+    }
+    // the Krylov bases are released with the call: they are not part of a
+    // handle's resident memory
+    struct Release {
+        wt3d_solver *h;
+        ~Release() { h->gmV.free(); h->gmZ.free(); }
+    } release{h};
+    double2 *V = h->gmV.p, *Z = h->gmZ.p;
+    const int th = 256;
+    const unsigned nbm = (unsigned)ceil_div(n * m, th), nbb = (unsigned)ceil_div(blk, th);
+    typedef std::complex<double> C;
+    std::vector<double> sc_h(MAXRHS);
+    std::vector<double2> hb((GM_K + 1) * MAXRHS), hb2((GM_K + 1) * MAXRHS), coef((GM_K + 1) * MAXRHS);
+    std::vector<double> wn(MAXRHS);
+    auto orth = [&](int nv, double2 *W, std::vector<double2> &out, bool norm) -> int {
+        k_mdot<<<GM_BLOCKS, 256, 0, st>>>(n, m, nv, V, blk, W, h->gmPart.p);
+        k_mdot_reduce<<<nv, MAXRHS, 0, st>>>(GM_BLOCKS, nv, h->gmPart.p, h->gmH.p);
+        k_maxpy<<<GM_BLOCKS, 256, 0, st>>>(n, m, nv, V, blk, h->gmH.p, W, norm ? (double *)h->gmPart.p : nullptr);
+        if (norm) k_norm_reduce<<<1, MAXRHS, 0, st>>>(GM_BLOCKS, (const double *)h->gmPart.p, h->gmNorm.p);
+        WT_CUDA(cudaGetLastError());
+        WT_CUDA(cudaMemcpyAsync(out.data(), h->gmH.p, sizeof(double2) * nv * MAXRHS, cudaMemcpyDeviceToHost, st));
+        if (norm) WT_CUDA(cudaMemcpyAsync(wn.data(), h->gmNorm.p, sizeof(double) * MAXRHS, cudaMemcpyDeviceToHost, st));
+        WT_CUDA(cudaStreamSynchronize(st));
+        return WT3D_OK;
+    };
+    for (;;) {
+        // ---- one cycle from the current residual ----
+        std::vector<double> beta(m);
+        std::vector<int> done(m, 0), len(m, 0);
+        for (int c = 0; c < m; c++) {
+            beta[c] = sqrt(rnorm2[c]);
+            const double bn = sqrt(bnorm2[c]);
+            done[c] = !(beta[c] > tol * (bn > 0 ? bn : 1.0));
+            sc_h[c] = done[c] ? 0.0 : 1.0 / beta[c];
+        }
+        for (int c = m; c < MAXRHS; c++) sc_h[c] = 0.0;
+        WT_CUDA(cudaMemcpyAsync(V, h->Rn.p, sizeof(double2) * blk, cudaMemcpyDeviceToDevice, st));
+        WT_CUDA(cudaMemcpyAsync(h->gmScale.p, sc_h.data(), sizeof(double) * MAXRHS, cudaMemcpyHostToDevice, st));
+        k_colscale<<<nbb, th, 0, st>>>(n, h->gmScale.p, V);
+        std::vector<std::vector<C>> H(m, std::vector<C>((GM_K + 1) * GM_K, C(0)));
+        std::vector<std::vector<C>> g(m, std::vector<C>(GM_K + 1, C(0))), cs(m, std::vector<C>(GM_K)),
+            sn(m, std::vector<C>(GM_K));
+        for (int c = 0; c < m; c++) g[c][0] = beta[c];
+        int j = 0;
+        for (; j < GM_K; j++) {
+            bool all = true;
+            for (int c = 0; c < m; c++) all = all && done[c];
+            if (all || it >= maxit) break;
+            // z_j = M^-1 v_j
+            double2 *Vj = V + (long long)j * blk, *Zj = Z + (long long)j * blk, *W = V + (long long)(j + 1) * blk;
+            k_gather_new<T><<<nbm, th, 0, st>>>(n, m, h->perm.p, E.scale.p, Vj, E.X.p);
+            if ((rc = E.run(*sc, st))) return rc;
+            WT_CUDA(cudaMemsetAsync(Zj, 0, sizeof(double2) * blk, st));
+            k_scatter_add_nat<T><<<nbm, th, 0, st>>>(n, m, h->perm.p, E.scale.p, E.X.p, Zj);
+            // w = op(A) z_j
+            WT_CUDA(cudaMemsetAsync(h->norms.p, 0, sizeof(double) * 2 * MAXRHS, st));
+            k_residual<<<152 * 8, 256, 0, st>>>(n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, Zj, nullptr, W,
+                                                h->norms.p, h->norms.p + MAXRHS, adjoint ? 1 : 0);
+            h->kernels_solve += sc->kernels() + 11;
+            if ((rc = orth(j + 1, W, hb, false)) || (rc = orth(j + 1, W, hb2, true))) return rc;
+            it++;
+            for (int c = 0; c < m; c++) {
+                if (done[c]) { sc_h[c] = 0.0; continue; }
+                std::vector<C> &Hc = H[c];
+                for (int i = 0; i <= j; i++)
+                    Hc[i * GM_K + j] = C(hb[i * MAXRHS + c].x + hb2[i * MAXRHS + c].x,
+                                         hb[i * MAXRHS + c].y + hb2[i * MAXRHS + c].y);
+                const double hn = sqrt(wn[c]);
+                // earlier rotations, then a new one zeroing H[j+1][j]
+                for (int i = 0; i < j; i++) {
+                    const C a = Hc[i * GM_K + j], b = Hc[(i + 1) * GM_K + j];
+                    Hc[i * GM_K + j] = std::conj(cs[c][i]) * a + std::conj(sn[c][i]) * b;
+                    Hc[(i + 1) * GM_K + j] = -sn[c][i] * a + cs[c][i] * b;
+                }
+                const C a = Hc[j * GM_K + j];
+                const double den = sqrt(std::norm(a) + hn * hn);
+                cs[c][j] = den > 0 ? a / den : C(1);
+                sn[c][j] = den > 0 ? C(hn / den) : C(0);
+                Hc[j * GM_K + j] = den;
+                g[c][j + 1] = -sn[c][j] * g[c][j];
+                g[c][j] = std::conj(cs[c][j]) * g[c][j];
+                len[c] = j + 1;
+                const double bn = sqrt(bnorm2[c]);
+                const double est = std::abs(g[c][j + 1]) / (bn > 0 ? bn : 1.0);
+                if (relres) relres[c] = est;
+                if (est <= 0.5 * tol || hn <= 1e-300) done[c] = 1;
+                sc_h[c] = done[c] ? 0.0 : 1.0 / hn;
+            }
+            WT_CUDA(cudaMemcpyAsync(h->gmScale.p, sc_h.data(), sizeof(double) * MAXRHS, cudaMemcpyHostToDevice, st));
+            k_colscale<<<nbb, th, 0, st>>>(n, h->gmScale.p, W);
+        }
+        // x += Z y, y = R^-1 g per column
+        const int jmax = j;
+        if (jmax > 0) {
+            std::fill(coef.begin(), coef.end(), make_double2(0, 0));
+            for (int c = 0; c < m; c++) {
+                const int L = len[c];
+                std::vector<C> y(L);
+                for (int i = L - 1; i >= 0; i--) {
+                    C t = g[c][i];
+                    for (int q = i + 1; q < L; q++) t -= H[c][i * GM_K + q] * y[q];
+                    y[i] = t / H[c][i * GM_K + i];
+                }
+                for (int i = 0; i < L; i++) coef[i * MAXRHS + c] = make_double2(-y[i].real(), -y[i].imag());
+            }
+            WT_CUDA(cudaMemcpyAsync(h->gmH.p, coef.data(), sizeof(double2) * jmax * MAXRHS, cudaMemcpyHostToDevice, st));
+            k_maxpy<<<GM_BLOCKS, 256, 0, st>>>(n, m, jmax, Z, blk, h->gmH.p, h->Xn.p, nullptr);
+        }
+        // true residual
+        std::vector<double> hn2(2 * MAXRHS);
+        WT_CUDA(cudaMemsetAsync(h->norms.p, 0, sizeof(double) * 2 * MAXRHS, st));
+        k_residual<<<152 * 8, 256, 0, st>>>(n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, h->Xn.p, h->Bn.p,
+                                            h->Rn.p, h->norms.p, h->norms.p + MAXRHS, adjoint ? 1 : 0);
+        WT_CUDA(cudaGetLastError());
+        WT_CUDA(cudaMemcpyAsync(hn2.data(), h->norms.p, sizeof(double) * 2 * MAXRHS, cudaMemcpyDeviceToHost, st));
+        WT_CUDA(cudaStreamSynchronize(st));
+        double worst = 0;
+        for (int c = 0; c < m; c++) {
+            rnorm2[c] = hn2[c];
+            const double r = hn2[MAXRHS + c] > 0 ? sqrt(hn2[c] / hn2[MAXRHS + c]) : sqrt(hn2[c]);
+            if (relres) relres[c] = r;
+            worst = std::max(worst, r);
+        }
+        if (!(worst == worst)) return WT3D_ERR_NOCONV;
+        if (worst <= tol) return WT3D_OK;
+        if (it >= maxit || jmax == 0) return WT3D_ERR_NOCONV;
+    }
+}
+
 // Refinement driver over m <= MAXRHS columns held in h->Bn; result in h->Xn.
+// Plain iterative refinement while it reduces the worst residual at least
+// fourfold per step; flexible GMRES preconditioned by the same factors
+// otherwise (a few near-singular modes of the preconditioned operator slow
+// refinement down, and the Krylov solver removes them in a few steps).
 template <class T>
 int refine(wt3d_solver *h, Engine<T> &E, int m, bool adjoint, double tol, int maxit, double *relres, int *iters)
 {
@@ -277,9 +544,12 @@ int refine(wt3d_solver *h, Engine<T> &E, int m, bool adjoint, double tol, int ma
         if (!(worst == worst)) { rc = WT3D_ERR_NOCONV; break; }   // NaN
         if (worst <= tol) break;
         if (it >= maxit) { rc = WT3D_ERR_NOCONV; break; }
-        // stop when a step no longer halves the worst residual: the FP64
-        // residual itself has reached its rounding floor (|A||x|/|b| * eps)
-        if (it >= 2 && worst > 0.5 * prev_worst) { rc = WT3D_ERR_NOCONV; break; }
+        if (it >= 1 && worst > 0.25 * prev_worst) {
+            std::vector<double> bn2(hn.begin() + MAXRHS, hn.begin() + MAXRHS + m), rn2(hn.begin(), hn.begin() + m);
+            it++;
+            rc = fgmres<T>(h, E, sc, m, adjoint, tol, maxit, bn2, rn2, relres, it);
+            break;
+        }
         prev_worst = worst;
         it++;
     }
