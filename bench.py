@@ -226,6 +226,33 @@ def run_ours(args, rank, world):
     return out
 
 
+def run_serve(args):
+    """Serving loop (configuration 3): a seeded Poisson stream of requests over
+    grids 48^3, 64^3 and 96x96x64 (weights 0.5/0.35/0.15), model seeds from a
+    pool of 8, frequencies {0.5, 1, 1.5, 2} Hz, 1-64 sources (75% plane
+    waves, 25% point forces); factorisations resident under a 120 GB budget
+    with LRU eviction, right-hand sides batched per factorisation.  Latency =
+    arrival to solution on the host."""
+    from wtomo3d_gb300 import serve
+    be = serve.GpuBackend(dx=20.0, pml_nodes=10, tol=args.tol, maxit=30)
+    grids = ((48, 48, 48), (64, 64, 64), (96, 96, 64))
+    for g in grids:          # host analyses of the three grids, computed once per process
+        be.bytes_needed((g, 0, 1.0))
+    stream = serve.make_stream(args.serve_requests, rate_hz=args.serve_rate, seed=7, grids=grids)
+    srv = serve.Server(be, budget_bytes=120e9, max_batch=64, workers=4)
+    try:
+        summ = srv.run(stream, timeout_s=900)
+    finally:
+        srv.close()
+    summ = {k: (float("%.4g" % v) if isinstance(v, float) else v) for k, v in summ.items()}
+    summ.update({"workload": "config3 serving: Poisson %.2f req/s, %d requests (seed 7), grids 48^3/64^3/96x96x64 "
+                             "(0.5/0.35/0.15), model pool 8, f in {0.5,1,1.5,2} Hz, 1-64 sources (75%% plane, 25%% "
+                             "point), budget 120 GB resident factors, LRU, RHS batched per factor, 4 workers"
+                             % (args.serve_rate, args.serve_requests),
+                 "hit_rate": round(summ["hits"] / max(1, summ["requests"]), 3)})
+    return summ
+
+
 def run_fp64(args):
     """The FP64 GPU factorisation oracle on the same workload: complex128
     fronts (FP64 SIMT kernels), FP64 refinement to the same tolerance.  Only
@@ -300,6 +327,9 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=30)
+    ap.add_argument("--serve-rate", type=float, default=0.3)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -329,6 +359,8 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
     out = run_ours(args, rank, world)
+    if rank == 0 and not args.no_serve:
+        out["serve"] = run_serve(args)
     if rank == 0:
         if not args.no_cpu:
             v, cb = run_cpu(args, 1, 0)

@@ -216,6 +216,19 @@ typedef struct wt3d_stats {
 } wt3d_stats;
 int wt3d_get_stats(const wt3d_solver *h, wt3d_stats *st);
 
+/* Device buffers owned by the handle for ncols right-hand sides and
+ * solutions (complex128, column-major n x ncols), grown on demand and freed
+ * with the handle; counted in wt3d_stats.device_bytes.  For callers that keep
+ * no device memory of their own (the serving loop).  No reference counterpart. */
+int wt3d_batch_buffers(wt3d_solver *h, int ncols, void **d_F, void **d_X);
+
+/* Copy `bytes` between host and device memory in either direction on the
+ * handle's stream, returning when done.  No reference counterpart. */
+int wt3d_memcpy(wt3d_solver *h, void *dst, const void *src, long long bytes);
+
+/* Free and total device memory of the current device. */
+int wt3d_mem_info(double *free_bytes, double *total_bytes);
+
 /* Device memory of a handle for grid g, before creating it (host analysis
  * only, cached per grid): out[0] = bytes a factored handle holds on its own,
  * out[1] = additional bytes once plane-wave sources are built (background

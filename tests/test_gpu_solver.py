@@ -85,7 +85,7 @@ def test_mixed_refinement_converges_in_few_steps(small_case):
 
 def test_many_rhs_batches(small_case):
     g, vp, vs, rho, om, A, lu = small_case
-    B = rand_rhs(g.n, 70, seed=4, g=g)   # two passes of 64 + 6
+    B = rand_rhs(g.n, 70, seed=4, g=g)   # passes of 32 + 32 + 6 columns
     with wt.Solver(g) as s:
         s.set_model(vp, vs, rho)
         s.factor(om)
@@ -185,7 +185,7 @@ def test_slow_refinement_switches_to_gmres():
                         d_F=F.data_ptr())
         for adjoint in (False, True):
             rr = s.solve_device(F.data_ptr(), X.data_ptr(), 4, tol=1e-10, maxit=30, adjoint=adjoint)
-            assert rr.max() <= 1e-10 and s.last_iters <= 16, (adjoint, s.last_iters, rr.max())
+            assert rr.max() <= 1e-10 and s.last_iters <= 20, (adjoint, s.last_iters, rr.max())
             # the reported residual is the true one
             Y = torch.zeros_like(F)
             if not adjoint:

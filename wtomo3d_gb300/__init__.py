@@ -125,6 +125,9 @@ def lib():
         L.wt3d_apply.argtypes = [vp, ctypes.c_int, vp, vp]
         L.wt3d_apply_device.argtypes = [vp, ctypes.c_int, vp, vp]
         L.wt3d_solver_bytes.argtypes = [ctypes.POINTER(Grid), ctypes.c_int, vp]
+        L.wt3d_batch_buffers.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp)]
+        L.wt3d_memcpy.argtypes = [vp, vp, vp, ctypes.c_longlong]
+        L.wt3d_mem_info.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         L.wt3d_update_operator.argtypes = [vp]
         L.wt3d_gradient_contract.argtypes = [vp, ctypes.c_int, vp, vp, vp]
         L.wt3d_misfit_gradient.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, ctypes.c_double,
@@ -186,6 +189,13 @@ def assemble(grid, vp, vs, rho, omega):
     om = complex(omega)
     _check(lib().wt3d_assemble(ctypes.byref(grid), _ptr(vp), _ptr(vs), _ptr(rho), om.real, om.imag, _ptr(a)))
     return a
+
+
+def mem_info():
+    """(free, total) device bytes of the current device."""
+    f, t = ctypes.c_double(), ctypes.c_double()
+    _check(lib().wt3d_mem_info(ctypes.byref(f), ctypes.byref(t)))
+    return f.value, t.value
 
 
 def solver_bytes(grid, precision=PREC_MIXED):
@@ -264,6 +274,16 @@ class Solver:
         Y = np.empty_like(Xf, order="F")
         _check(lib().wt3d_apply(self._h, Xf.shape[1], _ptr(Xf), _ptr(Y)))
         return Y[:, 0] if one else Y
+
+    def batch_buffers(self, ncols):
+        """Device pointers (F, X) of handle-owned n x ncols complex128 buffers."""
+        f, x = ctypes.c_void_p(), ctypes.c_void_p()
+        _check(lib().wt3d_batch_buffers(self._h, int(ncols), ctypes.byref(f), ctypes.byref(x)))
+        return f.value, x.value
+
+    def memcpy(self, dst, src, nbytes):
+        """Copy between host and device addresses (ints) on the handle's stream."""
+        _check(lib().wt3d_memcpy(self._h, ctypes.c_void_p(dst), ctypes.c_void_p(src), int(nbytes)))
 
     def apply_device(self, d_X, d_Y, nrhs):
         """Y = A X on device arrays (column-major n x nrhs complex128)."""

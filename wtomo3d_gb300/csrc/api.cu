@@ -43,11 +43,12 @@ __global__ void k_rm_to_cm_neg(long long n, int m, const double2 *__restrict__ r
 }
 
 // R = B - op(A) X (op = A or A^H), per-column squared norms of R into nr and of B into nb.
-// One warp per grid node; lane l holds right-hand sides l and l + 32
-// (MAXRHS = 64).  The node's three rows (u, v, w) are contiguous in the CSR
-// and share one column list, so each column index and each row of X is
-// loaded once for the three rows.
-static_assert(MAXRHS == 64, "k_residual maps two right-hand sides to a lane");
+// One warp per grid node; lane l holds right-hand sides l, l + 32, ...
+// (NH = MAXRHS / 32 of them).  The node's three rows (u, v, w) are contiguous
+// in the CSR and share one column list, so each column index and each row of
+// X is loaded once for the three rows.
+constexpr int NH = MAXRHS / 32;
+static_assert(MAXRHS % 32 == 0, "k_residual maps right-hand sides to lanes in groups of 32");
 __global__ void __launch_bounds__(256) k_residual(long long n, int m, const int *__restrict__ irptr,
                                                   const int *__restrict__ jcptr, const double2 *__restrict__ a,
                                                   const int *__restrict__ tpos, const double2 *__restrict__ X,
@@ -58,36 +59,40 @@ __global__ void __launch_bounds__(256) k_residual(long long n, int m, const int 
     const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     const long long nnode = n / 3;
-    const bool on[2] = {lane < m, lane + 32 < m};
-    double sr[2] = {0, 0}, sb[2] = {0, 0};
+    bool on[NH];
+    double sr[NH], sb[NH];
+#pragma unroll
+    for (int h = 0; h < NH; h++) { on[h] = lane + 32 * h < m; sr[h] = sb[h] = 0; }
     for (long long g = w0; g < nnode; g += nw) {
         const long long r0 = 3 * g;
         const int k0 = irptr[r0];
         const int len = irptr[r0 + 1] - k0;
-        double2 acc[3][2];
+        double2 acc[3][NH];
 #pragma unroll
-        for (int q = 0; q < 3; q++) acc[q][0] = acc[q][1] = make_double2(0, 0);
+        for (int q = 0; q < 3; q++)
+#pragma unroll
+            for (int h = 0; h < NH; h++) acc[q][h] = make_double2(0, 0);
 #pragma unroll 3
         for (int t = 0; t < len; t++) {
             const int k = k0 + t;
             const double2 *xr = X + (long long)jcptr[k] * MAXRHS + lane;
-            double2 x[2];
+            double2 x[NH];
 #pragma unroll
-            for (int h = 0; h < 2; h++) x[h] = on[h] ? xr[32 * h] : make_double2(0, 0);
+            for (int h = 0; h < NH; h++) x[h] = on[h] ? xr[32 * h] : make_double2(0, 0);
 #pragma unroll
             for (int q = 0; q < 3; q++) {
                 double2 av;
                 if (adjoint) { av = a[tpos[k + q * len]]; av.y = -av.y; }
                 else av = a[k + q * len];
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
+                for (int h = 0; h < NH; h++) {
                     acc[q][h].x = fma(av.x, x[h].x, fma(-av.y, x[h].y, acc[q][h].x));
                     acc[q][h].y = fma(av.x, x[h].y, fma(av.y, x[h].x, acc[q][h].y));
                 }
             }
         }
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < NH; h++) {
             if (!on[h]) continue;
             const int j = lane + 32 * h;
 #pragma unroll
@@ -102,7 +107,7 @@ __global__ void __launch_bounds__(256) k_residual(long long n, int m, const int 
         }
     }
 #pragma unroll
-    for (int h = 0; h < 2; h++)
+    for (int h = 0; h < NH; h++)
         if (on[h]) { atomicAdd(&nr[lane + 32 * h], sr[h]); atomicAdd(&nb[lane + 32 * h], sb[h]); }
 }
 
@@ -124,10 +129,12 @@ __global__ void __launch_bounds__(256) k_mdot(long long n, int m, int nv, const 
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     for (int i = 0; i < nv; i++) {
         const double2 *Vi = V + (long long)i * vstride;
-        double2 acc[2] = {make_double2(0, 0), make_double2(0, 0)};
+        double2 acc[NH];
+#pragma unroll
+        for (int h = 0; h < NH; h++) acc[h] = make_double2(0, 0);
         for (long long r = w0; r < n; r += nw) {
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
+            for (int h = 0; h < NH; h++) {
                 const int c = lane + 32 * h;
                 if (c >= m) continue;
                 const double2 v = Vi[r * MAXRHS + c], w = W[r * MAXRHS + c];
@@ -135,8 +142,8 @@ __global__ void __launch_bounds__(256) k_mdot(long long n, int m, int nv, const 
                 acc[h].y = fma(v.x, w.y, fma(-v.y, w.x, acc[h].y));
             }
         }
-        red[warp][lane] = acc[0];
-        red[warp][lane + 32] = acc[1];
+#pragma unroll
+        for (int h = 0; h < NH; h++) red[warp][lane + 32 * h] = acc[h];
         __syncthreads();
         if (threadIdx.x < MAXRHS) {
             double2 t = make_double2(0, 0);
@@ -301,6 +308,7 @@ struct wt3d_solver {
     double om_re = 0, om_im = 0;          // omega of the assembled operator
     DevVec<double> norms;
     DevVec<double> gscr;                  // per-row derivative records of the gradient
+    DevVec<double2> batF, batX;           // caller batch buffers (wt3d_batch_buffers)
     DevVec<double2> gmV, gmZ, gmH;        // flexible GMRES: Krylov basis, preconditioned basis, projections
     DevVec<double2> gmPart;
     DevVec<double> gmNorm, gmScale;
@@ -627,7 +635,7 @@ double own_bytes(const wt3d_solver *h)
     double b = (double)(h->e32 ? h->e32->device_bytes() : h->e64->device_bytes());
     b += (double)(h->irptr.n + h->jcptr.n + h->tpos.n + h->perm.n) * 4;
     b += (double)(h->a.n + h->da.n + h->mu.n + h->Bn.n + h->Xn.n + h->Rn.n + h->T1.n + h->abg.n + h->bgda.n +
-                  h->bgmu.n) * 16;
+                  h->bgmu.n + h->batF.n + h->batX.n) * 16;
     b += (double)(h->ro.n + h->bgro.n + h->norms.n + h->gscr.n) * 8 + (double)(h->vp.n + h->vs.n + h->rho.n) * 4;
     return b;
 }
@@ -1097,6 +1105,37 @@ int wt3d_misfit_gradient(wt3d_solver *h, int nsrc, const void *d_F, const void *
     if ((rc = wt3d_gradient_contract(h, nsrc, X.p, Lm.p, dg.p))) return rc;
     WT_CUDA(cudaMemcpy(grad, dg.p, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost));
     return rcf ? rcf : rca;
+}
+
+int wt3d_batch_buffers(wt3d_solver *h, int ncols, void **d_F, void **d_X)
+{
+    if (!h || ncols < 1 || !d_F || !d_X) { set_error("wt3d_batch_buffers: bad arguments"); return WT3D_ERR_ARG; }
+    const size_t need = (size_t)h->n * ncols;
+    int rc;
+    if (h->batF.n < need) {
+        WT_CUDA(cudaStreamSynchronize(h->st));
+        if ((rc = h->batF.alloc(need)) || (rc = h->batX.alloc(need))) return rc;
+    }
+    *d_F = h->batF.p;
+    *d_X = h->batX.p;
+    return WT3D_OK;
+}
+
+int wt3d_memcpy(wt3d_solver *h, void *dst, const void *src, long long bytes)
+{
+    if (!h || !dst || !src || bytes < 0) { set_error("wt3d_memcpy: bad arguments"); return WT3D_ERR_ARG; }
+    WT_CUDA(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDefault, h->st));
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    return WT3D_OK;
+}
+
+int wt3d_mem_info(double *free_bytes, double *total_bytes)
+{
+    size_t f = 0, t = 0;
+    WT_CUDA(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = (double)f;
+    if (total_bytes) *total_bytes = (double)t;
+    return WT3D_OK;
 }
 
 int wt3d_get_stats(const wt3d_solver *h, wt3d_stats *st)

@@ -16,6 +16,7 @@ struct DevVec {
         if (count == 0) return WT3D_OK;
         cudaError_t e = cudaMalloc(&p, count * sizeof(T));
         if (e != cudaSuccess) {
+            cudaGetLastError();   // an allocation failure is not sticky: clear it for later checks
             p = nullptr;
             set_error(std::string("cudaMalloc(") + std::to_string(count * sizeof(T)) + " B): " + cudaGetErrorString(e));
             return WT3D_ERR_NOMEM;

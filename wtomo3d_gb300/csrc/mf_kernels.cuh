@@ -15,7 +15,7 @@
 namespace wt3d {
 
 constexpr int KB = 64;        // panel width
-constexpr int MAXRHS = 64;    // right-hand sides per solve pass
+constexpr int MAXRHS = 32;    // right-hand sides per solve pass (a multiple of 32)
 
 struct FrontDev {
     long long fac;     // P block offset in the factor pool (complex elements)

@@ -128,6 +128,16 @@ class Server:
             free += victims[-1].bytes
         if free < need:
             return False                      # wait for running work to finish
+        # the device must also hold the transient memory of the new
+        # factorisation (workspace, Krylov bases) next to everything resident
+        can_open = getattr(self.backend, "can_open", None)
+        if can_open is not None:
+            freeing = sum(v.bytes for v in victims)
+            while not can_open(key, freeing) and idle:
+                victims.append(idle.pop(0))
+                freeing += victims[-1].bytes
+            if not can_open(key, freeing) and self._jobs > 0:
+                return False
         for v in victims:
             del self.entries[v.key]
             self.used -= v.bytes
@@ -187,7 +197,29 @@ class Server:
         for v in victims:
             self.backend.close(v.handle)
             v.handle = None
-        h = self.backend.open(e.key)
+        for attempt in range(6):
+            try:
+                h = self.backend.open(e.key)
+                break
+            except Exception as exc:
+                is_oom = getattr(self.backend, "is_oom", lambda x: False)
+                if attempt == 5 or not is_oom(exc):
+                    raise
+                # out of device memory: release every idle factorisation, then
+                # wait for running work before retrying
+                with self.cv:
+                    idle = [x for x in self.entries.values()
+                            if x is not e and x.state == "ready" and not x.busy and not x.pending]
+                    for x in idle:
+                        del self.entries[x.key]
+                        self.used -= x.bytes
+                        self.log["evictions"] += 1
+                for x in idle:
+                    self.backend.close(x.handle)
+                    x.handle = None
+                with self.cv:
+                    if not idle:
+                        self.cv.wait(timeout=1.0)
         with self.cv:
             e.handle = h
             actual = self.backend.resident_bytes(h)
@@ -281,13 +313,15 @@ class GpuBackend:
     force on component comp.  Solutions (scattered field for plane waves)
     are FP64-refined to `tol`."""
 
-    def __init__(self, dx=20.0, pml_nodes=10, tol=1e-8, maxit=20, keep_results=False, precision=None):
+    def __init__(self, dx=20.0, pml_nodes=10, tol=1e-8, maxit=20, keep_results=False, precision=None, max_batch=64):
         import wtomo3d_gb300 as wt
         self.wt = wt
         self.dx, self.pml_nodes, self.tol, self.maxit = dx, pml_nodes, tol, maxit
         self.keep = keep_results
+        self.max_batch = max_batch
         self.precision = wt.PREC_MIXED if precision is None else precision
         self._models = {}
+        self._open = {}
         self._lock = threading.Lock()
 
     def grid(self, dims):
@@ -305,62 +339,78 @@ class GpuBackend:
             return self._models[k]
 
     def bytes_needed(self, key):
-        r, extra, _ = self.wt.solver_bytes(self.grid(key[0]), self.precision)
-        return r + extra
+        g = self.grid(key[0])
+        r, extra, _ = self.wt.solver_bytes(g, self.precision)
+        return r + extra + 2.0 * g.n * self.max_batch * 16      # + the batch buffers
+
+    def can_open(self, key, freeing):
+        """Free device memory (plus what the evictions release) covers the new
+        handle, the factorisation workspace of its grid unless another handle
+        of that grid holds it, the Krylov bases of a slow solve and a margin."""
+        g = self.grid(key[0])
+        _, _, ws = self.wt.solver_bytes(g, self.precision)
+        with self._lock:
+            shared = self._open.get(tuple(key[0]), 0) > 0
+        transient = (0.0 if shared else 1.25 * ws) + 17.0 * g.n * 32 * 16 + 4e9
+        free, _ = self.wt.mem_info()
+        return free + freeing >= self.bytes_needed(key) + transient
 
     def open(self, key):
         dims, seed, freq = key
         mdl, bg, _ = self.model(dims, seed)
         s = self.wt.Solver(self.grid(dims), self.precision)
-        s.set_model(*mdl)
-        s.set_background(*bg)
-        s.factor(2 * np.pi * freq)
+        try:
+            s.set_model(*mdl)
+            s.set_background(*bg)
+            s.factor(2 * np.pi * freq)
+            s.batch_buffers(self.max_batch)
+        except Exception:
+            s.close()
+            raise
+        with self._lock:
+            self._open[tuple(dims)] = self._open.get(tuple(dims), 0) + 1
         return s
+
+    def is_oom(self, exc):
+        return getattr(exc, "code", None) == self.wt.WT3D_ERR_NOMEM
 
     def resident_bytes(self, s):
         st = s.stats()
         return float(st["device_bytes"])
 
     def close(self, s):
+        dims = (s.grid.nx, s.grid.ny, s.grid.nz)
         s.close()
+        with self._lock:
+            self._open[dims] = self._open.get(dims, 1) - 1
 
     def solve(self, s, key, batch):
-        import torch
         from wtomo3d_gb300 import model
         dims, seed, freq = key
         nx, ny, nz = dims
         _, _, lay = self.model(dims, seed)
         n = s.grid.n
         cols = sum(r.nsrc for r in batch)
-        dev = torch.device("cuda")
-        # torch work of this job on a stream of its own: a device-wide
-        # synchronize would wait for the other handles' batches
-        ts = torch.cuda.Stream()
-        with torch.cuda.stream(ts):
-            F = torch.zeros((cols, n), dtype=torch.complex128, device=dev)
-            X = torch.zeros_like(F)
-            c0 = 0
-            for r in batch:
-                if r.kind == "point":
-                    B = np.stack([model.point_force(nx, ny, nz, self.dx, x * (nx - 1) * self.dx,
-                                                    y * (ny - 1) * self.dx, z * (nz - 1) * self.dx, comp=c)
-                                  for (x, y, z, c) in r.params])
-                    F[c0:c0 + r.nsrc] = torch.from_numpy(B).to(dev)
-                c0 += r.nsrc
-            ts.synchronize()
-            c0 = 0
-            for r in batch:
-                if r.kind == "plane":
-                    ain = np.array([p[0] for p in r.params])
-                    baz = np.array([p[1] for p in r.params])
-                    s.rhs_planewave(lay, ain, baz, d_F=F[c0:].data_ptr())
-                c0 += r.nsrc
-            relres = s.solve_device(F.data_ptr(), X.data_ptr(), cols, tol=self.tol, maxit=self.maxit)
-            out, c0 = [], 0
-            for r in batch:
-                x = X[c0:c0 + r.nsrc].cpu().numpy().T.copy() if self.keep else None
-                out.append((x, relres[c0:c0 + r.nsrc].copy()))
-                c0 += r.nsrc
-            ts.synchronize()
-            del F, X
+        dF, dX = s.batch_buffers(cols)
+        col_bytes = n * 16
+        c0 = 0
+        for r in batch:
+            if r.kind == "plane":
+                s.rhs_planewave(lay, np.array([p[0] for p in r.params]), np.array([p[1] for p in r.params]),
+                                d_F=dF + c0 * col_bytes)
+            else:
+                B = np.asfortranarray(np.stack(
+                    [model.point_force(nx, ny, nz, self.dx, x * (nx - 1) * self.dx, y * (ny - 1) * self.dx,
+                                       z * (nz - 1) * self.dx, comp=c) for (x, y, z, c) in r.params], axis=1))
+                s.memcpy(dF + c0 * col_bytes, B.ctypes.data, B.nbytes)
+            c0 += r.nsrc
+        relres = s.solve_device(dF, dX, cols, tol=self.tol, maxit=self.maxit, allow_noconv=True)
+        out, c0 = [], 0
+        for r in batch:
+            x = None
+            if self.keep:
+                x = np.empty((n, r.nsrc), np.complex128, order="F")
+                s.memcpy(x.ctypes.data, dX + c0 * col_bytes, x.nbytes)
+            out.append((x, relres[c0:c0 + r.nsrc].copy()))
+            c0 += r.nsrc
         return out
