@@ -38,7 +38,8 @@ constexpr int TC_STAGES = 2;
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 4;     // 16 KB
 constexpr int TC_B_BYTES = TC_BNR * TC_BK * 4;    // 32 KB
 constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;
-constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
+constexpr int TC_EPI_BYTES = 4 * 32 * 33 * 4;        // per epilogue warp a 32 x 33 float transpose buffer
+constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256 + TC_EPI_BYTES;
 constexpr int TC_THREADS = 192;
 constexpr unsigned TC_WAIT_LIMIT = 1u << 24;
 constexpr int TC_GROUP = 8;                 // row panels per rasterisation group
@@ -219,42 +220,64 @@ __global__ void __launch_bounds__(256) k_split_b(const TcTask *__restrict__ task
 // ---------------------------------------------------------------------------
 // the tensor-core kernel
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(TC_THREADS, 1)
-    k_tc_gemm(const TcTask *__restrict__ tasks, int ntasks, const CUtensorMap *__restrict__ maps, int *err)
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 {
-    extern __shared__ __align__(1024) uint8_t smem_raw[];
-    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE_BYTES);
-    uint64_t *empty = full + TC_STAGES;
-    uint64_t *accum = empty + TC_STAGES;
-    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(accum + 1);
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long gt = blockIdx.x;
+// Tile gt of a launch: its task and the tile's first complex row and real column.
+// Grouped rasterisation: consecutive tiles sweep a band of TC_GROUP row panels
+// column by column, so the tiles in flight share a compact set of A and B
+// panels in L2 instead of streaming all of B per row panel.
+__device__ __forceinline__ const TcTask *tc_tile(const TcTask *__restrict__ tasks, int ntasks, long long gt, int &m0,
+                                                 int &n0r)
+{
     int lo_t = 0, hi_t = ntasks - 1;
     while (lo_t < hi_t) {
         int mid = (lo_t + hi_t + 1) >> 1;
         if (tasks[mid].tile0 <= gt) lo_t = mid;
         else hi_t = mid - 1;
     }
-    const TcTask &t = tasks[lo_t];
-    const long long lt = gt - t.tile0;
-    // Grouped rasterisation: consecutive CTAs sweep a band of TC_GROUP row
-    // panels column by column, so a wave of resident CTAs shares a compact set
-    // of A and B panels in L2 instead of streaming all of B per row panel.
-    const int tiles_m = (t.M + TC_BM - 1) / TC_BM;
-    const long long per_group = (long long)TC_GROUP * t.tiles_n;
+    const TcTask *t = tasks + lo_t;
+    const long long lt = gt - t->tile0;
+    const int tiles_m = (t->M + TC_BM - 1) / TC_BM;
+    const long long per_group = (long long)TC_GROUP * t->tiles_n;
     const int group = (int)(lt / per_group);
     const int first_m = group * TC_GROUP;
     const int gsize = min(tiles_m - first_m, TC_GROUP);
     const int in_group = (int)(lt % per_group);
-    const int m0 = (first_m + in_group % gsize) * TC_BM;
-    const int n0r = (in_group / gsize) * TC_BNR;
-    const int nk = t.Kr / TC_BK;
+    m0 = (first_m + in_group % gsize) * TC_BM;
+    n0r = (in_group / gsize) * TC_BNR;
+    return t;
+}
 
+// Persistent: one CTA per SM walks the launch's tiles gt = blockIdx.x,
+// blockIdx.x + gridDim.x, ...  Warp 0 (one lane) streams the k-steps of all
+// its tiles through the TC_STAGES-deep TMA pipeline; warp 1 (one lane) issues
+// the MMAs into one of two TMEM accumulators (256 columns each) and commits
+// the finished one; warps 2-5 drain a finished accumulator straight from TMEM
+// into C -= D while the MMAs of the next tile run into the other one.  Every
+// wait is bounded: a role that times out sets *err and stops, the others then
+// time out in turn, and before TMEM is released the MMA lane waits for its
+// issued MMAs and the producer for its issued copies.
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_tc_gemm(const TcTask *__restrict__ tasks, int ntasks, long long ntiles, const CUtensorMap *__restrict__ maps,
+              int *err)
+{
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE_BYTES);
+    uint64_t *empty = full + TC_STAGES;
+    uint64_t *tfull = empty + TC_STAGES;      // accumulator b written (MMA commit)
+    uint64_t *tempty = tfull + 2;             // accumulator b read out (4 epilogue warps)
+    uint64_t *drain = tempty + 2;
+    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(drain + 1);
+    float *epi = reinterpret_cast<float *>(smem + TC_STAGES * TC_STAGE_BYTES + 256);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
-                     "r"(256));
+                     "r"(2 * TC_BNR));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (threadIdx.x == 32) {
@@ -262,7 +285,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(accum, 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 4);
+        }
+        mbar_init(drain, 1);
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -272,96 +299,123 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
     if (warp == 0 && lane == 0) {
         // ---------------- TMA producer ----------------
-        const CUtensorMap *mp = maps + t.map0;
-        for (int ks = 0; ks < nk; ks++) {
-            const int s = ks % TC_STAGES;
-            const uint32_t ph = ((ks / TC_STAGES) & 1) ^ 1;
-            if (!mbar_wait(&empty[s], ph)) atomicCAS(err, 0, 1);
-            uint8_t *st = smem + s * TC_STAGE_BYTES;
-            mbar_expect_tx(&full[s], TC_STAGE_BYTES);
-            tma_load_2d(st, mp + 0, ks * TC_BK, m0, &full[s]);
-            tma_load_2d(st + TC_A_BYTES, mp + 1, ks * TC_BK, m0, &full[s]);
-            tma_load_2d(st + 2 * TC_A_BYTES, mp + 2, ks * TC_BK, n0r, &full[s]);
-            tma_load_2d(st + 2 * TC_A_BYTES + TC_B_BYTES, mp + 3, ks * TC_BK, n0r, &full[s]);
+        long long gks = 0;
+        bool ok = true;
+        for (long long gt = blockIdx.x; gt < ntiles && ok; gt += gridDim.x) {
+            int m0, n0r;
+            const TcTask *t = tc_tile(tasks, ntasks, gt, m0, n0r);
+            const CUtensorMap *mp = maps + t->map0;
+            const int nk = t->Kr / TC_BK;
+            for (int ks = 0; ks < nk; ks++, gks++) {
+                const int s = (int)(gks % TC_STAGES);
+                const uint32_t ph = (uint32_t)((gks / TC_STAGES) & 1) ^ 1u;
+                if (!mbar_wait(&empty[s], ph)) { atomicCAS(err, 0, 1); ok = false; break; }
+                uint8_t *st = smem + s * TC_STAGE_BYTES;
+                mbar_expect_tx(&full[s], TC_STAGE_BYTES);
+                tma_load_2d(st, mp + 0, ks * TC_BK, m0, &full[s]);
+                tma_load_2d(st + TC_A_BYTES, mp + 1, ks * TC_BK, m0, &full[s]);
+                tma_load_2d(st + 2 * TC_A_BYTES, mp + 2, ks * TC_BK, n0r, &full[s]);
+                tma_load_2d(st + 2 * TC_A_BYTES + TC_B_BYTES, mp + 3, ks * TC_BK, n0r, &full[s]);
+            }
+        }
+        // the last copy issued into each stage has landed before the CTA exits
+        for (int s = 0; s < TC_STAGES; s++) {
+            if (gks <= s) continue;
+            const long long last = gks - 1 - ((gks - 1 - s) % TC_STAGES);
+            mbar_wait(&full[s], (uint32_t)((last / TC_STAGES) & 1));
         }
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer ----------------
         constexpr uint32_t idesc = tf32_idesc(TC_BM, TC_BNR);
-        for (int ks = 0; ks < nk; ks++) {
-            const int s = ks % TC_STAGES;
-            const uint32_t ph = (ks / TC_STAGES) & 1;
-            if (!mbar_wait(&full[s], ph)) atomicCAS(err, 0, 2);
+        long long gks = 0;
+        int it = 0;
+        bool ok = true;
+        for (long long gt = blockIdx.x; gt < ntiles && ok; gt += gridDim.x, it++) {
+            int m0, n0r;
+            const TcTask *t = tc_tile(tasks, ntasks, gt, m0, n0r);
+            const int nk = t->Kr / TC_BK;
+            const int b = it & 1;
+            const uint32_t use = (uint32_t)(it >> 1);
+            if (!mbar_wait(&tempty[b], (use & 1u) ^ 1u)) { atomicCAS(err, 0, 4); ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t base = smem_u32(smem + s * TC_STAGE_BYTES);
-            const uint32_t a_hi = base, a_lo = base + TC_A_BYTES;
-            const uint32_t b_hi = base + 2 * TC_A_BYTES, b_lo = b_hi + TC_B_BYTES;
+            const uint32_t dacc = tmem + (uint32_t)(b * TC_BNR);
+            for (int ks = 0; ks < nk; ks++, gks++) {
+                const int s = (int)(gks % TC_STAGES);
+                const uint32_t ph = (uint32_t)((gks / TC_STAGES) & 1);
+                if (!mbar_wait(&full[s], ph)) { atomicCAS(err, 0, 2); ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t base = smem_u32(smem + s * TC_STAGE_BYTES);
+                const uint32_t a_hi = base, a_lo = base + TC_A_BYTES;
+                const uint32_t b_hi = base + 2 * TC_A_BYTES, b_lo = b_hi + TC_B_BYTES;
 #pragma unroll
-            for (int kk = 0; kk < TC_BK / 8; kk++) {
-                const uint32_t off = kk * 32;   // 8 TF32 elements = 32 bytes along K
-                const uint64_t dah = sw128_desc(a_hi + off), dal = sw128_desc(a_lo + off);
-                const uint64_t dbh = sw128_desc(b_hi + off), dbl = sw128_desc(b_lo + off);
-                umma_tf32(tmem, dah, dbh, idesc, (ks | kk) != 0);
-                umma_tf32(tmem, dah, dbl, idesc, 1);
-                umma_tf32(tmem, dal, dbh, idesc, 1);
+                for (int kk = 0; kk < TC_BK / 8; kk++) {
+                    const uint32_t off = kk * 32;   // 8 TF32 elements = 32 bytes along K
+                    const uint64_t dah = sw128_desc(a_hi + off), dal = sw128_desc(a_lo + off);
+                    const uint64_t dbh = sw128_desc(b_hi + off), dbl = sw128_desc(b_lo + off);
+                    umma_tf32(dacc, dah, dbh, idesc, (ks | kk) != 0);
+                    umma_tf32(dacc, dah, dbl, idesc, 1);
+                    umma_tf32(dacc, dal, dbh, idesc, 1);
+                }
+                umma_commit(&empty[s]);
             }
-            umma_commit(&empty[s]);
+            if (!ok) break;
+            umma_commit(&tfull[b]);
         }
-        umma_commit(accum);
+        // no MMA of this CTA is in flight once the drain barrier completes
+        umma_commit(drain);
+        mbar_wait(drain, 0);
     } else if (warp >= 2) {
         // ---------------- epilogue ----------------
-        // The accumulator is staged row-major in the (now idle) pipeline
-        // shared memory, then C is read-modified-written by whole warps on
-        // contiguous 256-byte row segments.
-        if (!mbar_wait(accum, 0)) atomicCAS(err, 0, 3);
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        const int q = warp & 3;                 // TMEM lane quarter this warp may access
-        const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16);
-        float *stage = reinterpret_cast<float *>(smem);     // 128 rows x EP floats
-        constexpr int EP = TC_BNR + 4;
-        float *myrow = stage + (32 * q + lane) * EP;
+        // Lane l of warp w reads accumulator row 32 q + l (TMEM lane quarter
+        // q = w mod 4) in 32-column chunks; each chunk goes through a 32 x 33
+        // transpose buffer so that C is read-modified-written one row segment
+        // (32 floats, 128 bytes) per warp instruction.
+        const int q = warp & 3;
+        float *tb = epi + (warp - 2) * (32 * 33);
+        int it = 0;
+        for (long long gt = blockIdx.x; gt < ntiles; gt += gridDim.x, it++) {
+            int m0, n0r;
+            const TcTask *t = tc_tile(tasks, ntasks, gt, m0, n0r);
+            const int b = it & 1;
+            const uint32_t use = (uint32_t)(it >> 1);
+            if (!mbar_wait(&tfull[b], use & 1u)) { atomicCAS(err, 0, 3); break; }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * TC_BNR);
+            const int row0 = m0 + 32 * q;
 #pragma unroll 1
-        for (int ch = 0; ch < TC_BNR / 32; ch++) {
-            uint32_t v[32];
-            TMEM_LD32(tq + ch * 32, v);
-            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            for (int ch = 0; ch < TC_BNR / 32; ch++) {
+                uint32_t v[32];
+                TMEM_LD32(taddr + ch * 32, v);
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-            for (int i = 0; i < 32; i += 4)
-                *reinterpret_cast<float4 *>(myrow + ch * 32 + i) =
-                    make_float4(__uint_as_float(v[i]), __uint_as_float(v[i + 1]), __uint_as_float(v[i + 2]),
-                                __uint_as_float(v[i + 3]));
-        }
-        asm volatile("bar.sync 1, 128;" ::: "memory");   // the four epilogue warps only
-        const int c0 = n0r / 2;
-        const int ew = warp - 2;                // 0..3
-#pragma unroll 1
-        for (int r = ew; r < TC_BM; r += 4) {
-            const int row = m0 + r;
-            if (row >= t.M) break;
-            cx<float> *crow = t.C + (long long)row * t.ldc + c0;
-            const float *srow = stage + r * EP;
-            cx<float> o[4];
+                for (int i = 0; i < 32; i++) tb[lane * 33 + i] = __uint_as_float(v[i]);
+                __syncwarp();
+                const int cf = n0r + ch * 32 + lane;          // real column = 2 * complex column + (re, im)
+                const int nr = min(32, t->M - row0);
+                if ((cf >> 1) < t->N) {
+                    // all 32 row loads in flight before the first store
+                    float *cp = reinterpret_cast<float *>(t->C + (long long)row0 * t->ldc) + cf;
+                    const long long ldf = 2LL * t->ldc;
+                    float cv[32];
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const int c = lane + 32 * j;
-                if (c0 + c < t.N) o[j] = crow[c];
-            }
+                    for (int r = 0; r < 32; r++) cv[r] = r < nr ? cp[r * ldf] : 0.f;
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const int c = lane + 32 * j;
-                if (c0 + c < t.N) {
-                    const float2 d = *reinterpret_cast<const float2 *>(srow + 2 * c);
-                    o[j].re -= d.x;
-                    o[j].im -= d.y;
-                    crow[c] = o[j];
+                    for (int r = 0; r < 32; r++)
+                        if (r < nr) cp[r * ldf] = cv[r] - tb[r * 33 + lane];
                 }
+                __syncwarp();
             }
+            // accumulator b may be overwritten by the tile after next
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[b]);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_BNR));
     }
 }
 
@@ -471,11 +525,23 @@ void tc_split(const TcLaunch &L, cudaStream_t st)
     k_split_b<<<(unsigned)L.b_tiles, 256, 0, st>>>(L.tasks.p, L.ntasks, L.b_tiles);
 }
 
+static int num_sms()
+{
+    static const int n = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 1;
+    }();
+    return n;
+}
+
 void tc_mma(const TcLaunch &L, int *err, cudaStream_t st)
 {
     if (L.ntasks == 0) return;
-    k_tc_gemm<<<(unsigned)L.tiles, TC_THREADS, TC_SMEM, st>>>(L.tasks.p, L.ntasks,
-                                                              reinterpret_cast<const CUtensorMap *>(L.maps.p), err);
+    const long long grid = std::min<long long>(L.tiles, num_sms());
+    k_tc_gemm<<<(unsigned)grid, TC_THREADS, TC_SMEM, st>>>(L.tasks.p, L.ntasks, L.tiles,
+                                                           reinterpret_cast<const CUtensorMap *>(L.maps.p), err);
 }
 
 int tc_init()
