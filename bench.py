@@ -96,7 +96,36 @@ def plane_wave_sources(nrhs, seed=11):
     return ain, baz
 
 
+def run_pipelined(n_steps, first, work, nlanes):
+    """Runs steps first .. first+n_steps-1; step i on lane i % nlanes, one host
+    thread per lane (the library releases the interpreter lock).  Lanes are
+    separate solver handles of the same grid: their factorisations are
+    serialised by the shared workspace, so one lane's substitution passes
+    overlap the other lane's factorisation."""
+    import threading
+    out = [None] * n_steps
+    errs = []
+
+    def lane(l):
+        try:
+            for i in range(first, first + n_steps):
+                if i % nlanes == l:
+                    out[i - first] = work(l, i)
+        except Exception as exc:   # re-raised below
+            errs.append(exc)
+
+    ths = [threading.Thread(target=lane, args=(l,)) for l in range(nlanes)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    if errs:
+        raise errs[0]
+    return out
+
+
 def run_ours(args, rank, world):
+    import ctypes
     import torch
     import wtomo3d_gb300 as wt
     from wtomo3d_gb300 import Grid, model
@@ -108,31 +137,37 @@ def run_ours(args, rank, world):
     dx = 20.0
     g = Grid(nx, ny, nz, dx, pmld=10 * dx, fst=1, usemin=1)
     vp, vs, rho = model.layered_random(nx, ny, nz, dx, seed=1)
-    t0 = time.perf_counter()
-    s = wt.Solver(g, wt.PREC_MIXED)
-    t_analyse = time.perf_counter() - t0
-    s.set_model(vp, vs, rho)
     vp0, vs0, rho0 = model.layered(nx, ny, nz)
-    s.set_background(vp0, vs0, rho0)
     layers = wt.Layered1D(*model.layered1d(nz, dx))
     nrhs = args.nrhs
     ain, baz = plane_wave_sources(nrhs)
     rhs_desc = ("%d Haskell plane-wave P sources per frequency (incidence U[0,30] deg, back-azimuth U[0,360), "
                 "seed 11), scattered-field f = (A_bg - A) u0 against the unperturbed layered background" % nrhs)
-    dB = torch.zeros((nrhs, g.n), dtype=torch.complex128, device="cuda")   # n x nrhs column-major
-    dX = torch.zeros_like(dB)
-    stream = torch.cuda.ExternalStream(s.stream)
+    # two lanes (handles) of the same grid, pipelined frequencies
+    nl = args.lanes
+    t0 = time.perf_counter()
+    S = [wt.Solver(g, wt.PREC_MIXED) for _ in range(nl)]
+    t_analyse = time.perf_counter() - t0
+    dB, dX = [], []
+    for s in S:
+        s.set_model(vp, vs, rho)
+        s.set_background(vp0, vs0, rho0)
+        dB.append(torch.zeros((nrhs, g.n), dtype=torch.complex128, device="cuda"))   # n x nrhs column-major
+        dX.append(torch.zeros_like(dB[-1]))
+    stream = torch.cuda.ExternalStream(S[0].stream)
 
-    def step(i):
+    def step(l, i):
+        s = S[l]
         f = FREQS[(i + rank) % len(FREQS)]
         s.factor(2 * np.pi * f)
-        s.rhs_planewave(layers, ain, baz, d_F=dB.data_ptr())
-        rr = s.solve_device(dB.data_ptr(), dX.data_ptr(), nrhs, tol=args.tol, maxit=30)
+        s.rhs_planewave(layers, ain, baz, d_F=dB[l].data_ptr())
+        rr = s.solve_device(dB[l].data_ptr(), dX[l].data_ptr(), nrhs, tol=args.tol, maxit=30)
         st = s.stats()
-        return f, float(rr.max()), s.last_iters, st
+        return dict(freq=f, relres=float(rr.max()), iters=s.last_iters, factor_ms=st["t_factor_ms"],
+                    solve_ms=st["t_solve_ms"], assemble_ms=st["t_assemble_ms"],
+                    launches=st["kernels_factor"] + st["kernels_solve"] + 4)   # + background, expansion, source
 
-    for i in range(args.warmup):
-        step(i)
+    run_pipelined(args.warmup, 0, step, nl)
     clocks = Clocks(dev)
     if world > 1:
         torch.distributed.barrier()
@@ -141,17 +176,13 @@ def run_ours(args, rank, world):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    recs = []
-    launches = 0
-    for i in range(args.steps):
-        f, rr, it, st = step(args.warmup + i)
-        recs.append(dict(freq=f, relres=rr, iters=it, factor_ms=st["t_factor_ms"], solve_ms=st["t_solve_ms"],
-                         assemble_ms=st["t_assemble_ms"]))
-        launches += st["kernels_factor"] + st["kernels_solve"] + 4   # + background assembly, expansion, source
+    recs = run_pipelined(args.steps, args.warmup, step, nl)
+    torch.cuda.synchronize()
     e1.record(stream)
     torch.cuda.synchronize()
     ck = clocks.stop()
     ms = e0.elapsed_time(e1)
+    launches = sum(r.pop("launches") for r in recs)
     if world > 1:
         t = torch.tensor([ms], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -160,24 +191,28 @@ def run_ours(args, rank, world):
 
     # ---- end to end through the public API: host model, background and source
     # parameters in, solutions back to pinned host memory ----
-    Xh = torch.empty((nrhs, g.n), dtype=torch.complex128).pin_memory()
+    Xh = [torch.empty((nrhs, g.n), dtype=torch.complex128).pin_memory() for _ in range(nl)]
     host_models = [[torch.from_numpy(np.ascontiguousarray(a.reshape(-1, order="F"))).pin_memory()
                     for a in arrs] for arrs in ((vp, vs, rho), (vp0, vs0, rho0))]
-    import ctypes
     L = wt.lib()
+
+    def e2e_step(l, i):
+        s = S[l]
+        f = FREQS[(i + rank) % len(FREQS)]
+        L.wt3d_set_model(s._h, *[ctypes.c_void_p(a.data_ptr()) for a in host_models[0]])
+        L.wt3d_set_background(s._h, *[ctypes.c_void_p(a.data_ptr()) for a in host_models[1]])
+        s.factor(2 * np.pi * f)
+        s.rhs_planewave(layers, ain, baz, d_F=dB[l].data_ptr())
+        s.solve_device(dB[l].data_ptr(), dX[l].data_ptr(), nrhs, tol=args.tol, maxit=30)   # returns synchronised
+        s.memcpy(Xh[l].data_ptr(), dX[l].data_ptr(), Xh[l].numel() * 16)
+        return None
+
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for i in range(args.steps):
-        f = FREQS[(args.warmup + i + rank) % len(FREQS)]
-        L.wt3d_set_model(s._h, *[ctypes.c_void_p(a.data_ptr()) for a in host_models[0]])
-        L.wt3d_set_background(s._h, *[ctypes.c_void_p(a.data_ptr()) for a in host_models[1]])
-        s.factor(2 * np.pi * f)
-        s.rhs_planewave(layers, ain, baz, d_F=dB.data_ptr())
-        s.solve_device(dB.data_ptr(), dX.data_ptr(), nrhs, tol=args.tol, maxit=30)   # returns synchronised
-        Xh.copy_(dX, non_blocking=True)
-        torch.cuda.synchronize()
+    run_pipelined(args.steps, args.warmup, e2e_step, nl)
+    torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     if world > 1:
         t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
@@ -185,7 +220,8 @@ def run_ours(args, rank, world):
         e2e_s = float(t.item())
     e2e = world * nrhs * args.steps / e2e_s
     h2d = 2 * sum(a.nbytes for a in (vp, vs, rho)) + ain.nbytes + baz.nbytes
-    d2h = Xh.numel() * 16
+    d2h = Xh[0].numel() * 16
+    s = S[0]
 
     # ---- roofline of the dominant kernel (one profiled factorisation) ----
     prof = s.profile_factor()
@@ -205,7 +241,9 @@ def run_ours(args, rank, world):
                    "model": "4 flat layers Vp 3000-6000, Vs=Vp/1.73, 5% Gaussian-correlated 200 m (seed 1), Gardner rho",
                    "freqs_hz": FREQS, "sources_per_step": nrhs, "rhs": rhs_desc, "tol": args.tol,
                    "l2": "inputs larger than L2 (factors %.1f GB)" % (st["factor_bytes"] / 1e9),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "pipelining": "%d solver handles of the same grid, alternate frequencies from %d host threads: "
+                                 "one frequency's substitution passes overlap the next one's factorisation" % (nl, nl)},
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "tensor", "kernel": "k_tc_gemm (tcgen05 3xTF32 front Schur/trailing updates)",
@@ -218,11 +256,12 @@ def run_ours(args, rank, world):
         "solve_pass_profile_ms": sprof,
         "clocks": ck,
     }
-    # release torch's handles on the library stream before the handle (and its
-    # stream) is destroyed
+    # release torch's handles on the library stream before the handles (and
+    # their streams) are destroyed
     del stream, e0, e1, dB, dX, Xh
     torch.cuda.synchronize()
-    s.close()
+    for h in S:
+        h.close()
     return out
 
 
@@ -328,6 +367,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--lanes", type=int, default=2, help="pipelined solver handles (1 = sequential steps)")
     ap.add_argument("--serve-requests", type=int, default=30)
     ap.add_argument("--serve-rate", type=float, default=0.3)
     args = ap.parse_args()
