@@ -42,7 +42,7 @@ constexpr int TC_EPI_BYTES = 4 * 32 * 33 * 4;        // per epilogue warp a 32 x
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256 + TC_EPI_BYTES;
 constexpr int TC_THREADS = 192;
 constexpr unsigned TC_WAIT_LIMIT = 1u << 24;
-constexpr int TC_GROUP = 8;                 // row panels per rasterisation group
+constexpr int TC_GROUP = 8;                 // column panels per rasterisation group
 
 // ---------------------------------------------------------------------------
 // PTX helpers
@@ -226,9 +226,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 }
 
 // Tile gt of a launch: its task and the tile's first complex row and real column.
-// Grouped rasterisation: consecutive tiles sweep a band of TC_GROUP row panels
-// column by column, so the tiles in flight share a compact set of A and B
-// panels in L2 instead of streaming all of B per row panel.
+// Grouped rasterisation: consecutive tiles sweep a band of TC_GROUP column
+// panels row panel by row panel, so the tiles in flight share a compact set of
+// A and B panels in L2.  The expanded B operand (2N x 2K real) is twice the
+// size of A, so B is the one kept resident while A panels stream.
 __device__ __forceinline__ const TcTask *tc_tile(const TcTask *__restrict__ tasks, int ntasks, long long gt, int &m0,
                                                  int &n0r)
 {
@@ -241,13 +242,13 @@ __device__ __forceinline__ const TcTask *tc_tile(const TcTask *__restrict__ task
     const TcTask *t = tasks + lo_t;
     const long long lt = gt - t->tile0;
     const int tiles_m = (t->M + TC_BM - 1) / TC_BM;
-    const long long per_group = (long long)TC_GROUP * t->tiles_n;
+    const long long per_group = (long long)TC_GROUP * tiles_m;
     const int group = (int)(lt / per_group);
-    const int first_m = group * TC_GROUP;
-    const int gsize = min(tiles_m - first_m, TC_GROUP);
+    const int first_n = group * TC_GROUP;
+    const int gsize = min(t->tiles_n - first_n, TC_GROUP);
     const int in_group = (int)(lt % per_group);
-    m0 = (first_m + in_group % gsize) * TC_BM;
-    n0r = (in_group / gsize) * TC_BNR;
+    n0r = (first_n + in_group % gsize) * TC_BNR;
+    m0 = (in_group / gsize) * TC_BM;
     return t;
 }
 
