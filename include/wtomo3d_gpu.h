@@ -197,6 +197,30 @@ int wt3d_misfit_gradient(wt3d_solver *h, int nsrc, const void *d_F, const void *
                          const long long *rec_node, const double _Complex *dobs, double tol, int maxit,
                          double *chi, double *grad, double _Complex *dpred);
 
+/* ---- sources and receivers between nodes --------------------------------
+ * Weights of a point at (x, y, z) metres from node 1 on the grid, as
+ * SRCSETUP/SRCREG spread a source or sample a receiver (srcsetup.f:50-211,
+ * srcreg.f:77-304): ireg = 0 nearest node; ireg > 0 Kaiser-windowed sinc of
+ * half-width ireg nodes (sprd <= 0.5) or the normalised discrete Dirac of
+ * half-width sprd nodes (sprd > 0.5); terms beyond a free top (g->fst) are
+ * mirrored with a sign change, terms beyond the other faces dropped.  FP64,
+ * I0 from std::cyl_bessel_i (the reference: REAL, rational I0; ~1e-7).
+ * Writes up to cap (0-based node, weight) pairs; *count = pairs produced. */
+int wt3d_source_weights(const wt3d_grid *g, double x, double y, double z, int ireg, double sprd, int cap,
+                        long long *node, double *weight, int *count);
+
+/* Point-force right-hand sides on the device: column j of d_F (complex128,
+ * column-major n x nsrc) = the source sterm[j] (NULL: 1) spread by the
+ * weights above onto component comp[j] (0 u, 1 v, 2 w) at xyz[3j..3j+2]. */
+int wt3d_rhs_sources(wt3d_solver *h, int nsrc, const double *xyz, const int *comp, const double _Complex *sterm,
+                     int ireg, double sprd, void *d_F);
+
+/* Three-component receiver samples of device wavefields d_U (n x nrhs):
+ * out[(j*nrec + r)*3 + c] = sum of weight * u_j(node, c) over receiver r's
+ * weights (SRCSETUP with lsetup = .false., srcsetup.f:192-206). */
+int wt3d_sample_receivers(wt3d_solver *h, int nrhs, const void *d_U, int nrec, const double *xyz, int ireg,
+                          double sprd, double _Complex *out);
+
 /* Statistics of the last factorisation. */
 typedef struct wt3d_stats {
     long long n, nnz;              /* unknowns, operator nonzeros             */

@@ -145,6 +145,105 @@ long long ora_point_source(const ora_grid *g, double xloc, double yloc, double z
 #undef FN
 
 /* ---------------------------------------------------------------------- */
+/* SRCSETUP with ireg > 0 (srcsetup.f:78-211) over SRCREG (srcreg.f:77-304) */
+/* in FP64.  I0 from its power series sum_k ((x/2)^k / k!)^2; the         */
+/* reference evaluates it by a rational approximation in REAL.            */
+/* ---------------------------------------------------------------------- */
+static double ora_i0(double x)
+{
+    double t = 1.0, s = 1.0, q = 0.25 * x * x;
+    for (int k = 1; k < 200; k++) {
+        t *= q / ((double)k * (double)k);
+        s += t;
+        if (t < 1e-17 * s) break;
+    }
+    return s;
+}
+
+static double ora_sinc(int ireg, double x)
+{
+    const double pi = 3.141592653589793;
+    double a, lx, v = (x <= 1e-10) ? 1.0 : sin(pi * x) / (pi * x);
+    switch (ireg) {   /* srcreg.f:206-226 */
+    case 1: a = 1.24; break;
+    case 2: a = 2.94; break;
+    case 3: a = 4.53; break;
+    case 4: a = 6.31; break;
+    case 5: a = 7.91; break;
+    case 6: a = 9.42; break;
+    case 7: a = 10.95; break;
+    case 8: a = 12.53; break;
+    case 9: a = 14.09; break;
+    default: a = 14.18;
+    }
+    lx = x / (double)ireg;
+    if (lx < 1.0) return v * ora_i0(a * sqrt(1.0 - lx * lx)) / ora_i0(a);
+    return 0.0;
+}
+
+static double ora_dirac(double h, double x)
+{
+    if (x < h) return (1.0 - x * x / (2.0 * h * h)) / (2.0 * h);
+    if (x < 2.0 * h) return (1.0 + (x * x - 4.0 * x * h) / (4.0 * h * h)) / h;
+    return 0.0;
+}
+
+int ora_source_weights(const ora_grid *g, double xloc, double yloc, double zloc, int ireg, double sprd,
+                       double complex sterm, double complex *swave)
+{
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+    const double dx = g->dx;
+    double fs[17][17][17];   /* (iz, ix, iy), 1-based as srcreg */
+    int ixs, iys, izs, half, lenw, ix, iy, iz;
+    double xoff, yoff, zoff, xs, ys, zs, amp = 1.0;
+    if (ireg <= 0) return 1;
+    ixs = (int)(xloc / dx) + 1; iys = (int)(yloc / dx) + 1; izs = (int)(zloc / dx) + 1;
+    xoff = xloc - (ixs - 1) * dx; yoff = yloc - (iys - 1) * dx; zoff = zloc - (izs - 1) * dx;
+    if (sprd <= 0.5) { half = ireg; lenw = 2 * ireg + 1; }
+    else { if (sprd <= 1e-10) return 1; half = (int)(2 * sprd); lenw = (int)(4 * sprd) + 1; }
+    if (lenw > 16) return 1;
+    xs = half + 1 + xoff / dx; ys = half + 1 + yoff / dx; zs = half + 1 + zoff / dx;
+    if (sprd > 0.5) amp = 0.0;
+    for (iy = 1; iy <= lenw; iy++)
+        for (ix = 1; ix <= lenw; ix++)
+            for (iz = 1; iz <= lenw; iz++) {
+                double v;
+                if (sprd <= 0.5)
+                    v = ora_sinc(ireg, fabs(iz - zs)) * ora_sinc(ireg, fabs(iy - ys)) * ora_sinc(ireg, fabs(ix - xs));
+                else
+                    v = ora_dirac(sprd, fabs(iz - zs)) * ora_dirac(sprd, fabs(iy - ys)) * ora_dirac(sprd, fabs(ix - xs));
+                fs[iz][ix][iy] = v;
+                if (sprd > 0.5) amp += v;
+            }
+    {
+        int izmins = izs - half, izmaxs = izs + half, ixmins = ixs - half, ixmaxs = ixs + half;
+        int iymins = iys - half, iymaxs = iys + half;
+        int izmin = izmins, izmax = izmaxs, ixmin = ixmins, ixmax = ixmaxs, iymin = iymins, iymax = iymaxs;
+        if (izmin < 1 && !g->fst) izmin = 1;   /* freesurf(1): top; other faces absorbing */
+        if (izmax > nz) izmax = nz;
+        if (ixmin < 1) ixmin = 1;
+        if (ixmax > nx) ixmax = nx;
+        if (iymin < 1) iymin = 1;
+        if (iymax > ny) iymax = ny;
+        for (iz = izmin; iz <= izmax; iz++) {
+            int izsrg = iz - izmins + 1, izfs = iz < 1 ? 2 - iz : (iz > nz ? 2 * nz - iz : iz);
+            if (izfs < 1 || izfs > nz) continue;
+            for (ix = ixmin; ix <= ixmax; ix++) {
+                int ixsrg = ix - ixmins + 1;
+                for (iy = iymin; iy <= iymax; iy++) {
+                    int iysrg = iy - iymins + 1;
+                    long long off = (long long)(izfs - 1) + (long long)nz * (ix - 1) + (long long)nz * nx * (iy - 1);
+                    double f = fs[izsrg][ixsrg][iysrg] / amp;
+                    if (iz == izfs) swave[off] += f * sterm;
+                    else swave[off] -= f * sterm;
+                }
+            }
+        }
+    }
+    return 0;
+}
+
+/* ---------------------------------------------------------------------- */
 /* Adjoint-state gradient in FP64 by central differences of node blocks.  */
 /* The reference has no gradient code on this path; this differentiates   */
 /* the restated ASMBLE operator numerically, independently of the GPU's    */

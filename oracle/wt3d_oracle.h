@@ -85,6 +85,15 @@ void ora_spmv_c128(int n, const int *irptr, const int *jcptr, const double compl
 long long ora_point_source(const ora_grid *g, double xloc, double yloc, double zloc,
                            int comp, double complex sterm, double complex *rhs);
 
+/* SRCSETUP with ireg > 0 (srcsetup.f:78-211) and SRCREG (srcreg.f:77-304):
+ * adds the spread source sterm at (xloc, yloc, zloc) (metres from node 1)
+ * into the node field swave[nz*nx*ny] (model order).  Kaiser-windowed sinc
+ * of half-width ireg nodes when sprd <= 0.5, normalised discrete Dirac of
+ * half-width sprd nodes otherwise; mirrored with a sign change above a free
+ * top (g->fst), dropped beyond the other faces.  Returns 0 on success. */
+int ora_source_weights(const ora_grid *g, double xloc, double yloc, double zloc, int ireg, double sprd,
+                       double complex sterm, double complex *swave);
+
 /* HASKGRN (haskgrn.f:31-672) in FP64: ugrn[nz], wgrn[nz] for a unit incident
  * P (s_wave = 0) or S plane wave with incidence angle ain (radians) at angular
  * frequency omega, nl layers with tops h1d[] (h1d[0] = 0; layer nl = half-space). */

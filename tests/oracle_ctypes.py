@@ -35,6 +35,8 @@ class Oracle:
         L.ora_node_blocks_c128.argtypes = [ctypes.POINTER(OGrid), vp, vp, vp, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp]
         L.ora_spmv_c128.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp]
+        L.ora_source_weights.argtypes = [ctypes.POINTER(OGrid)] + [ctypes.c_double] * 3 + [ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
         L.ora_gradient_c128.argtypes = [ctypes.POINTER(OGrid), vp, vp, vp, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_int, vp, vp, vp]
         L.ora_haskgrn.argtypes = [ctypes.c_int, vp, vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
@@ -79,6 +81,15 @@ class Oracle:
         ierr = self.L.ora_node_blocks_c128(ctypes.byref(og), _p(vp), _p(vs), _p(rho), om.real, om.imag,
                                            iz, ix, iy, _p(blk), _p(act))
         return blk.reshape(27, 3, 3), act, ierr
+
+    def source_field(self, g, x, y, z, ireg, sprd, sterm=1.0):
+        """Node field (model order, complex) of a spread source (ireg > 0)."""
+        og = self.grid(g)
+        f = np.zeros(g.nx * g.ny * g.nz, np.complex128)
+        st = complex(sterm)
+        rc = self.L.ora_source_weights(ctypes.byref(og), x, y, z, int(ireg), float(sprd), st.real, st.imag, _p(f))
+        assert rc == 0, rc
+        return f
 
     def gradient(self, g, vp, vs, rho, omega, U, Lam):
         """FP64 gradient (dchi/dVp, dchi/dVs, dchi/drho), each (nz, nx, ny),

@@ -128,6 +128,10 @@ def lib():
         L.wt3d_batch_buffers.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp)]
         L.wt3d_memcpy.argtypes = [vp, vp, vp, ctypes.c_longlong]
         L.wt3d_mem_info.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        L.wt3d_source_weights.argtypes = [ctypes.POINTER(Grid)] + [ctypes.c_double] * 3 + [ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_int, vp, vp, ctypes.POINTER(ctypes.c_int)]
+        L.wt3d_rhs_sources.argtypes = [vp, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_double, vp]
+        L.wt3d_sample_receivers.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, vp, ctypes.c_int, ctypes.c_double, vp]
         L.wt3d_update_operator.argtypes = [vp]
         L.wt3d_gradient_contract.argtypes = [vp, ctypes.c_int, vp, vp, vp]
         L.wt3d_misfit_gradient.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, ctypes.c_double,
@@ -189,6 +193,19 @@ def assemble(grid, vp, vs, rho, omega):
     om = complex(omega)
     _check(lib().wt3d_assemble(ctypes.byref(grid), _ptr(vp), _ptr(vs), _ptr(rho), om.real, om.imag, _ptr(a)))
     return a
+
+
+def source_weights(grid, x, y, z, ireg=0, sprd=0.5):
+    """(0-based nodes, weights) with which a point at (x, y, z) metres spreads
+    onto the grid (SRCSETUP/SRCREG)."""
+    cnt = ctypes.c_int(0)
+    _check(lib().wt3d_source_weights(ctypes.byref(grid), x, y, z, int(ireg), float(sprd), 0, None, None,
+                                     ctypes.byref(cnt)))
+    node = np.zeros(cnt.value, np.int64)
+    w = np.zeros(cnt.value)
+    _check(lib().wt3d_source_weights(ctypes.byref(grid), x, y, z, int(ireg), float(sprd), cnt.value, _ptr(node),
+                                     _ptr(w), ctypes.byref(cnt)))
+    return node, w
 
 
 def mem_info():
@@ -284,6 +301,22 @@ class Solver:
     def memcpy(self, dst, src, nbytes):
         """Copy between host and device addresses (ints) on the handle's stream."""
         _check(lib().wt3d_memcpy(self._h, ctypes.c_void_p(dst), ctypes.c_void_p(src), int(nbytes)))
+
+    def rhs_sources(self, xyz, comp, d_F, sterm=None, ireg=0, sprd=0.5):
+        """Point-force RHS columns on the device (d_F: n x nsrc, column-major)."""
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+        comp = np.ascontiguousarray(comp, np.int32).reshape(-1)
+        st = None if sterm is None else np.ascontiguousarray(sterm, np.complex128).reshape(-1)
+        _check(lib().wt3d_rhs_sources(self._h, len(comp), _ptr(xyz), _ptr(comp), None if st is None else _ptr(st),
+                                      int(ireg), float(sprd), ctypes.c_void_p(d_F)))
+
+    def sample_receivers(self, d_U, nrhs, xyz, ireg=0, sprd=0.5):
+        """Three-component receiver samples, shape (nrhs, nrec, 3)."""
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+        out = np.zeros((nrhs, len(xyz), 3), np.complex128)
+        _check(lib().wt3d_sample_receivers(self._h, int(nrhs), ctypes.c_void_p(d_U), len(xyz), _ptr(xyz), int(ireg),
+                                           float(sprd), _ptr(out)))
+        return out
 
     def apply_device(self, d_X, d_Y, nrhs):
         """Y = A X on device arrays (column-major n x nrhs complex128)."""

@@ -224,6 +224,38 @@ __global__ void k_colscale(long long n, const double *__restrict__ sc, double2 *
     W[q].y *= f;
 }
 
+// Spread sources: F[src_col[e] * n + 3 node[e] + comp[e]] += w[e] * sterm[e]
+// (one thread per (source, weight) entry; entries of one source are distinct).
+__global__ void k_put_sources(long long n, long long ne, const int *__restrict__ col, const long long *__restrict__ node,
+                              const int *__restrict__ comp, const double *__restrict__ w,
+                              const double2 *__restrict__ sterm, double2 *__restrict__ F)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const double2 s = sterm[col[e]];
+    double2 *p = F + (long long)col[e] * n + 3 * node[e] + comp[e];
+    p->x += w[e] * s.x;
+    p->y += w[e] * s.y;
+}
+
+// Receivers: out[(j nrec + r) 3 + c] = sum_e w[e] U_j[3 node[e] + c] over the
+// entries e of receiver r (rec_start[r] .. rec_start[r+1]).
+__global__ void k_get_receivers(long long n, int m, int nrec, const int *__restrict__ rec_start,
+                                const long long *__restrict__ node, const double *__restrict__ w,
+                                const double2 *__restrict__ U, double2 *__restrict__ out)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long long)m * nrec * 3) return;
+    const int c = (int)(q % 3), r = (int)((q / 3) % nrec), j = (int)(q / (3LL * nrec));
+    double2 acc = make_double2(0, 0);
+    for (int e = rec_start[r]; e < rec_start[r + 1]; e++) {
+        const double2 u = U[(long long)j * n + 3 * node[e] + c];
+        acc.x += w[e] * u.x;
+        acc.y += w[e] * u.y;
+    }
+    out[q] = acc;
+}
+
 // Xs = S R (new ordering, engine precision); S the Jacobi scaling of the factor.
 template <class T>
 __global__ void k_gather_new(long long n, int m, const int *__restrict__ perm, const double *__restrict__ s,
@@ -1125,6 +1157,76 @@ int wt3d_memcpy(wt3d_solver *h, void *dst, const void *src, long long bytes)
 {
     if (!h || !dst || !src || bytes < 0) { set_error("wt3d_memcpy: bad arguments"); return WT3D_ERR_ARG; }
     WT_CUDA(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDefault, h->st));
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    return WT3D_OK;
+}
+
+int wt3d_rhs_sources(wt3d_solver *h, int nsrc, const double *xyz, const int *comp, const double _Complex *sterm,
+                     int ireg, double sprd, void *d_F)
+{
+    if (!h || nsrc < 1 || !xyz || !comp || !d_F) { set_error("wt3d_rhs_sources: bad arguments"); return WT3D_ERR_ARG; }
+    const long long n = h->n;
+    std::vector<int> col, cmp;
+    std::vector<long long> nd;
+    std::vector<double> w;
+    std::vector<double2> st(nsrc);
+    for (int j = 0; j < nsrc; j++) {
+        if (comp[j] < 0 || comp[j] > 2) { set_error("wt3d_rhs_sources: component must be 0, 1 or 2"); return WT3D_ERR_ARG; }
+        std::vector<long long> a;
+        std::vector<double> b;
+        int rc = source_weights(h->grid, xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2], ireg, sprd, a, b);
+        if (rc) return rc;
+        // merge repeated nodes (mirrored terms) so that the kernel's entries are distinct
+        std::map<long long, double> acc;
+        for (size_t e = 0; e < a.size(); e++) acc[a[e]] += b[e];
+        for (auto &kv : acc) { col.push_back(j); nd.push_back(kv.first); w.push_back(kv.second); cmp.push_back(comp[j]); }
+        const std::complex<double> v = sterm ? reinterpret_cast<const std::complex<double> *>(sterm)[j] : 1.0;
+        st[j] = make_double2(v.real(), v.imag());
+    }
+    DevVec<int> dcol, dcmp;
+    DevVec<long long> dnd;
+    DevVec<double> dw;
+    DevVec<double2> dst;
+    int rc;
+    if ((rc = dcol.upload(col)) || (rc = dcmp.upload(cmp)) || (rc = dnd.upload(nd)) || (rc = dw.upload(w)) ||
+        (rc = dst.upload(st)))
+        return rc;
+    WT_CUDA(cudaMemsetAsync(d_F, 0, sizeof(double2) * n * nsrc, h->st));
+    const long long ne = (long long)col.size();
+    if (ne) k_put_sources<<<ceil_div(ne, 256), 256, 0, h->st>>>(n, ne, dcol.p, dnd.p, dcmp.p, dw.p, dst.p,
+                                                                (double2 *)d_F);
+    WT_CUDA(cudaGetLastError());
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    return WT3D_OK;
+}
+
+int wt3d_sample_receivers(wt3d_solver *h, int nrhs, const void *d_U, int nrec, const double *xyz, int ireg,
+                          double sprd, double _Complex *out)
+{
+    if (!h || nrhs < 1 || !d_U || nrec < 1 || !xyz || !out) { set_error("wt3d_sample_receivers: bad arguments"); return WT3D_ERR_ARG; }
+    std::vector<int> start(1, 0);
+    std::vector<long long> nd;
+    std::vector<double> w;
+    for (int r = 0; r < nrec; r++) {
+        std::vector<long long> a;
+        std::vector<double> b;
+        int rc = source_weights(h->grid, xyz[3 * r], xyz[3 * r + 1], xyz[3 * r + 2], ireg, sprd, a, b);
+        if (rc) return rc;
+        nd.insert(nd.end(), a.begin(), a.end());
+        w.insert(w.end(), b.begin(), b.end());
+        start.push_back((int)nd.size());
+    }
+    DevVec<int> dstart;
+    DevVec<long long> dnd;
+    DevVec<double> dw;
+    DevVec<double2> dout;
+    const long long tot = (long long)nrhs * nrec * 3;
+    int rc;
+    if ((rc = dstart.upload(start)) || (rc = dnd.upload(nd)) || (rc = dw.upload(w)) || (rc = dout.alloc(tot))) return rc;
+    k_get_receivers<<<ceil_div(tot, 256), 256, 0, h->st>>>(h->n, nrhs, nrec, dstart.p, dnd.p, dw.p,
+                                                            (const double2 *)d_U, dout.p);
+    WT_CUDA(cudaGetLastError());
+    WT_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(double2) * tot, cudaMemcpyDeviceToHost, h->st));
     WT_CUDA(cudaStreamSynchronize(h->st));
     return WT3D_OK;
 }

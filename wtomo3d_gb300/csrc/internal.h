@@ -18,6 +18,10 @@ int device_lame(long long nn, const float *d_vp, const float *d_vs, const float 
 int device_assemble(const wt3d_grid &g, const void *d_da, const void *d_mu, const double *d_ro, double om_re,
                     double om_im, const int *d_irptr, void *d_a, cudaStream_t st);
 
+// ---- sources and receivers between nodes (sources.cpp) --------------------
+int source_weights(const wt3d_grid &g, double x, double y, double z, int ireg, double sprd,
+                   std::vector<long long> &node, std::vector<double> &w);
+
 // ---- adjoint gradient (gradient.cu) --------------------------------------
 long long gradient_scratch_doubles(long long nn);
 int device_gradient(const wt3d_grid &g, const void *d_da, const void *d_mu, const double *d_ro, const float *d_vp,
