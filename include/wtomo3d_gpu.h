@@ -112,7 +112,19 @@ int wt3d_solver_destroy(wt3d_solver *h);
 /* Model (host arrays, (nz,nx,ny) floats). */
 int wt3d_set_model(wt3d_solver *h, const float *vp, const float *vs, const float *rho);
 
-/* Assemble A(omega) on the device and factor it (precision from create). */
+/* Attenuation (the Q model of DISPERSION, dispersion.f:78-114): qp_inv,
+ * qs_inv = 1/Qp, 1/Qs per node ((nz,nx,ny) floats), freqbase the frequency
+ * (Hz) at which vp and vs are given (model:freqbase, readini.f90:65, default
+ * 20).  Each wt3d_factor then disperses the Lame arrays to Re(omega):
+ * c = c1 max(1 + ln(Re omega / 2 pi freqbase)/(pi Q), 0.1), complex velocity
+ * (c, -c/(2Q)).  NULL pointers return to the elastic model.  The background
+ * of the plane-wave sources stays elastic, as in the reference.  The
+ * gradient entry points reject attenuating models. */
+int wt3d_set_attenuation(wt3d_solver *h, const float *qp_inv, const float *qs_inv, double freqbase);
+
+/* Assemble A(omega) on the device and factor it (precision from create).
+ * omega may be complex: the anti-alias frequency 2 pi f + i/tau of
+ * elwave.f90:164 (the mass terms keep only REAL(omega^2), pfdfd3d.f:140-142). */
 int wt3d_factor(wt3d_solver *h, double omega_re, double omega_im);
 
 /* Set caller-assembled operator values (complex64, host, CSR order of

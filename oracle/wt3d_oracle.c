@@ -329,6 +329,43 @@ int ora_gradient_c128(const ora_grid *g, const float *vp, const float *vs, const
     return 0;
 }
 
+/* DISPERSION (dispersion.f:78-114) in FP64, then ASMBLE.  qp, qs hold 1/Q.
+ * At omega1 = Re(omega) > eps and omegabase = 2 pi freqbase > 0:
+ *   c = c1 * max(1 + (1/Q)/pi * ln(omega1/omegabase), 0.1),
+ *   vc = (c, -c (1/Q) / 2),  mu = vcs^2 rho,  lambda = vcp^2 rho - 2 mu. */
+int ora_assemble_q_c128(const ora_grid *g, const float *vp, const float *vs, const float *rho, const float *qp,
+                        const float *qs, double freqbase, double omega_re, double omega_im, const int *irptr,
+                        double complex *a)
+{
+    const double pi = 3.141592653589793, eps = 10.0 * 1.1920929e-07;
+    long long nn = (long long)g->nx * g->ny * g->nz, i;
+    double complex *da = (double complex *)malloc(sizeof(double complex) * nn);
+    double complex *mu = (double complex *)malloc(sizeof(double complex) * nn);
+    double *ro = (double *)malloc(sizeof(double) * nn);
+    const double omegabase = freqbase * 2.0 * pi;
+    int rc;
+    if (!da || !mu || !ro) { free(da); free(mu); free(ro); return 1; }
+    lame_c128(nn, vp, vs, rho, da, mu, ro);
+    if (omega_re > eps && omegabase > 0.0) {
+        const double fac1 = log(omega_re / omegabase);
+        for (i = 0; i < nn; i++) {
+            double fs = 1.0 + (qs[i] / pi) * fac1, fp = 1.0 + (qp[i] / pi) * fac1, cs, cp;
+            double complex vc;
+            if (fs < 0.1) fs = 0.1;
+            if (fp < 0.1) fp = 0.1;
+            cs = vs[i] * fs;
+            vc = cs - I * (cs * qs[i] / 2.0);
+            mu[i] = vc * vc * (double)rho[i];
+            cp = vp[i] * fp;
+            vc = cp - I * (cp * qp[i] / 2.0);
+            da[i] = vc * vc * (double)rho[i] - 2.0 * mu[i];
+        }
+    }
+    rc = assemble_lame_c128(g, da, mu, ro, omega_re, omega_im, irptr, a);
+    free(da); free(mu); free(ro);
+    return rc;
+}
+
 int ora_assemble_c128(const ora_grid *g, const float *vp, const float *vs, const float *rho,
                       double omega_re, double omega_im, const int *irptr, double complex *a)
 {

@@ -61,6 +61,12 @@ int ora_assemble_c64(const ora_grid *g, const float *vp, const float *vs, const 
                      double omega_re, double omega_im, const int *irptr,
                      float complex *a);
 
+/* DISPERSION (dispersion.f:78-114) then ASMBLE, complex128: qp, qs are 1/Q
+ * per node, freqbase the reference frequency (Hz) of vp and vs. */
+int ora_assemble_q_c128(const ora_grid *g, const float *vp, const float *vs, const float *rho, const float *qp,
+                        const float *qs, double freqbase, double omega_re, double omega_im, const int *irptr,
+                        double complex *a);
+
 /* One node's 27 3x3 blocks (slot s = 9(dy+1)+3(dx+1)+(dz+1), rows/cols u,v,w),
  * and a mask of the slots present in the pattern.  1-based node indices. */
 int ora_node_blocks_c128(const ora_grid *g, const float *vp, const float *vs, const float *rho,

@@ -32,6 +32,8 @@ class Oracle:
         L.ora_pattern.argtypes = [ctypes.c_int] * 3 + [vp, vp]
         for f in (L.ora_assemble_c128, L.ora_assemble_c64):
             f.argtypes = [ctypes.POINTER(OGrid), vp, vp, vp, ctypes.c_double, ctypes.c_double, vp, vp]
+        L.ora_assemble_q_c128.argtypes = [ctypes.POINTER(OGrid), vp, vp, vp, vp, vp, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_double, vp, vp]
         L.ora_node_blocks_c128.argtypes = [ctypes.POINTER(OGrid), vp, vp, vp, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp]
         L.ora_spmv_c128.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp]
@@ -70,6 +72,16 @@ class Oracle:
         f = self.L.ora_assemble_c128 if precision == "c128" else self.L.ora_assemble_c64
         om = complex(omega)
         ierr = f(ctypes.byref(og), _p(vp), _p(vs), _p(rho), om.real, om.imag, _p(irptr), _p(a))
+        return a, ierr
+
+    def assemble_q(self, g, vp, vs, rho, qp, qs, freqbase, omega, irptr):
+        """complex128 ASMBLE after DISPERSION (qp, qs = 1/Q per node)."""
+        og = self.grid(g)
+        arrs = [np.ascontiguousarray(np.asarray(x, np.float32).reshape(-1, order="F")) for x in (vp, vs, rho, qp, qs)]
+        a = np.zeros(irptr[-1] - 1, np.complex128)
+        om = complex(omega)
+        ierr = self.L.ora_assemble_q_c128(ctypes.byref(og), *[_p(x) for x in arrs], float(freqbase), om.real,
+                                          om.imag, _p(irptr), _p(a))
         return a, ierr
 
     def node_blocks(self, g, vp, vs, rho, omega, iz, ix, iy):

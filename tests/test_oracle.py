@@ -183,3 +183,23 @@ def test_golden_fixtures(oracle, name):
     a, ierr = oracle.assemble(g, vp, vs, rho, om, ir)
     assert ierr == 0
     np.testing.assert_allclose(a, z["a"], rtol=0, atol=1e-13 * np.abs(z["a"]).max())
+
+
+def test_dispersion_oracle_limits(oracle):
+    """DISPERSION (dispersion.f:78-114): 1/Q = 0 leaves the elastic operator;
+    at Re(omega) = 2 pi freqbase only the imaginary velocity part appears, so
+    the operator's real part is that of the elastic one up to O(1/Q^2)."""
+    import numpy as np
+    from wtomo3d_gb300 import Grid, model
+    g = Grid(10, 9, 8, 25.0, pmld=50.0, fst=1)
+    vp, vs, rho = model.layered_random(10, 9, 8, 25.0, seed=2, corr_len=50.0)
+    ir, jc = oracle.pattern(10, 9, 8)
+    zero = np.zeros_like(vp)
+    om = 2 * np.pi * 3.0
+    a0, _ = oracle.assemble(g, vp, vs, rho, om, ir)
+    aq0, _ = oracle.assemble_q(g, vp, vs, rho, zero, zero, 20.0, om, ir)
+    assert np.abs(aq0 - a0).max() <= 1e-12 * np.abs(a0).max()
+    q = np.full_like(vp, 0.01)
+    aq, _ = oracle.assemble_q(g, vp, vs, rho, q, q, 3.0, om, ir)
+    assert np.abs(aq.imag).max() > 1e-4 * np.abs(a0).max()          # attenuation present
+    assert np.abs(aq.real - a0.real).max() <= 1e-3 * np.abs(a0).max()  # (1 - i q/2)^2: real part 1 - q^2/4

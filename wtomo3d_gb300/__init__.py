@@ -145,6 +145,7 @@ def lib():
         L.wt3d_haskgrn.argtypes = [ctypes.POINTER(Layered1D), ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                    ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, vp]
         L.wt3d_set_background.argtypes = [vp, vp, vp, vp]
+        L.wt3d_set_attenuation.argtypes = [vp, vp, vp, ctypes.c_double]
         L.wt3d_rhs_planewave.argtypes = [vp, ctypes.POINTER(Layered1D), ctypes.c_int, vp, vp, vp, vp, vp]
         ip = ctypes.POINTER(ctypes.c_int)
         L.strumpack_serial_finter.argtypes = [ip, ip, ip, vp, vp, vp, vp, vp, ip]
@@ -388,6 +389,16 @@ class Solver:
         d["gemm_flops"] = float(out[len(kinds)])
         d["gemm_launches"] = int(out[len(kinds) + 1])
         return d
+
+    def set_attenuation(self, qp_inv, qs_inv, freqbase=20.0):
+        """1/Qp, 1/Qs per node (None, None: elastic); dispersion at every factor()."""
+        n = self.grid.nnodes
+        if qp_inv is None:
+            _check(lib().wt3d_set_attenuation(self._h, None, None, 0.0))
+            self._q = None
+            return
+        self._q = (_f32(qp_inv, n), _f32(qs_inv, n))
+        _check(lib().wt3d_set_attenuation(self._h, _ptr(self._q[0]), _ptr(self._q[1]), float(freqbase)))
 
     def set_background(self, vp, vs, rho):
         n = self.grid.nnodes

@@ -333,6 +333,8 @@ struct wt3d_solver {
     DevVec<double2> da, mu;
     DevVec<double> ro;
     DevVec<float> vp, vs, rho;
+    DevVec<float> qp, qs;                 // 1/Q per node (attenuation), optional
+    double freqbase = 0;
     DevVec<double2> Bn, Xn, Rn, T1;
     DevVec<double2> abg, bgda, bgmu;      // background operator and Lame arrays
     DevVec<double> bgro;
@@ -668,7 +670,8 @@ double own_bytes(const wt3d_solver *h)
     b += (double)(h->irptr.n + h->jcptr.n + h->tpos.n + h->perm.n) * 4;
     b += (double)(h->a.n + h->da.n + h->mu.n + h->Bn.n + h->Xn.n + h->Rn.n + h->T1.n + h->abg.n + h->bgda.n +
                   h->bgmu.n + h->batF.n + h->batX.n) * 16;
-    b += (double)(h->ro.n + h->bgro.n + h->norms.n + h->gscr.n) * 8 + (double)(h->vp.n + h->vs.n + h->rho.n) * 4;
+    b += (double)(h->ro.n + h->bgro.n + h->norms.n + h->gscr.n) * 8 +
+         (double)(h->vp.n + h->vs.n + h->rho.n + h->qp.n + h->qs.n) * 4;
     return b;
 }
 
@@ -879,7 +882,12 @@ int wt3d_factor(wt3d_solver *h, double omega_re, double omega_im)
     if (!h->have_model) { set_error("wt3d_factor: no model set"); return WT3D_ERR_STATE; }
     h->have_factor = false;
     cudaEventRecord(h->ev0, h->st);
-    int rc = device_assemble(h->grid, h->da.p, h->mu.p, h->ro.p, omega_re, omega_im, h->irptr.p, h->a.p, h->st);
+    int rc;
+    // attenuation: Lame arrays dispersed to this frequency
+    if (h->qp.p && (rc = device_lame_q(h->n / 3, h->vp.p, h->vs.p, h->rho.p, h->qp.p, h->qs.p, omega_re, h->freqbase,
+                                       h->da.p, h->mu.p, h->ro.p, h->st)))
+        return rc;
+    rc = device_assemble(h->grid, h->da.p, h->mu.p, h->ro.p, omega_re, omega_im, h->irptr.p, h->a.p, h->st);
     if (rc) return rc;
     cudaEventRecord(h->ev1, h->st);
     WT_CUDA(cudaStreamSynchronize(h->st));
@@ -890,6 +898,29 @@ int wt3d_factor(wt3d_solver *h, double omega_re, double omega_im)
     rc = factor_values(h);
     h->stats.kernels_factor += 1;   // the assembly kernel
     return rc;
+}
+
+int wt3d_set_attenuation(wt3d_solver *h, const float *qp_inv, const float *qs_inv, double freqbase)
+{
+    if (!h) { set_error("null handle"); return WT3D_ERR_ARG; }
+    if (!qp_inv || !qs_inv) {   // back to an elastic model
+        h->qp.free();
+        h->qs.free();
+        if (h->have_model) {
+            int rc = device_lame(h->n / 3, h->vp.p, h->vs.p, h->rho.p, h->da.p, h->mu.p, h->ro.p, h->st);
+            if (rc) return rc;
+            WT_CUDA(cudaStreamSynchronize(h->st));
+        }
+        return WT3D_OK;
+    }
+    const long long nn = h->n / 3;
+    int rc;
+    if ((!h->qp.p && (rc = h->qp.alloc(nn))) || (!h->qs.p && (rc = h->qs.alloc(nn)))) return rc;
+    WT_CUDA(cudaMemcpyAsync(h->qp.p, qp_inv, sizeof(float) * nn, cudaMemcpyHostToDevice, h->st));
+    WT_CUDA(cudaMemcpyAsync(h->qs.p, qs_inv, sizeof(float) * nn, cudaMemcpyHostToDevice, h->st));
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    h->freqbase = freqbase;
+    return WT3D_OK;
 }
 
 int wt3d_set_background(wt3d_solver *h, const float *vp, const float *vs, const float *rho)
@@ -1072,7 +1103,11 @@ int wt3d_update_operator(wt3d_solver *h)
 {
     if (!h) { set_error("null handle"); return WT3D_ERR_ARG; }
     if (!h->have_model || !h->have_values) { set_error("wt3d_update_operator: needs a model and a factored operator"); return WT3D_ERR_STATE; }
-    int rc = device_assemble(h->grid, h->da.p, h->mu.p, h->ro.p, h->om_re, h->om_im, h->irptr.p, h->a.p, h->st);
+    int rc;
+    if (h->qp.p && (rc = device_lame_q(h->n / 3, h->vp.p, h->vs.p, h->rho.p, h->qp.p, h->qs.p, h->om_re, h->freqbase,
+                                       h->da.p, h->mu.p, h->ro.p, h->st)))
+        return rc;
+    rc = device_assemble(h->grid, h->da.p, h->mu.p, h->ro.p, h->om_re, h->om_im, h->irptr.p, h->a.p, h->st);
     if (rc) return rc;
     WT_CUDA(cudaStreamSynchronize(h->st));
     return WT3D_OK;
@@ -1082,6 +1117,7 @@ int wt3d_gradient_contract(wt3d_solver *h, int nrhs, const void *d_U, const void
 {
     if (!h || nrhs < 1 || !d_U || !d_Lam || !d_grad) { set_error("wt3d_gradient_contract: bad arguments"); return WT3D_ERR_ARG; }
     if (!h->have_model || !h->have_values) { set_error("wt3d_gradient_contract: needs a model and an assembled operator"); return WT3D_ERR_STATE; }
+    if (h->qp.p) { set_error("wt3d_gradient_contract: the gradient is built for elastic models (no attenuation)"); return WT3D_ERR_STATE; }
     const long long nn = h->n / 3;
     int rc;
     if (!h->gscr.p && (rc = h->gscr.alloc((size_t)gradient_scratch_doubles(nn)))) return rc;

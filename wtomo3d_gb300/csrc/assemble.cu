@@ -43,6 +43,30 @@ __global__ void k_lame(long long n, const float *__restrict__ vp, const float *_
     ro[i] = r;
 }
 
+// DISPERSION (dispersion.f:78-114) in FP64: qp, qs hold 1/Q.  At
+// omega1 = Re(omega) and omegabase = 2 pi freqbase,
+//   c = c1 * max(1 + (1/Q)/pi * ln(omega1/omegabase), 0.1),  vc = (c, -c (1/Q)/2),
+//   mu = vcs^2 rho,  lambda = vcp^2 rho - 2 mu.
+__global__ void k_lame_q(long long n, const float *__restrict__ vp, const float *__restrict__ vs,
+                         const float *__restrict__ rho, const float *__restrict__ qp, const float *__restrict__ qs,
+                         double fac1, cx<double> *__restrict__ da, cx<double> *__restrict__ mu,
+                         double *__restrict__ ro)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double pi = 3.141592653589793;
+    const double r = rho[i];
+    double fs = 1.0 + ((double)qs[i] / pi) * fac1, fp = 1.0 + ((double)qp[i] / pi) * fac1;
+    fs = fs < 0.1 ? 0.1 : fs;
+    fp = fp < 0.1 ? 0.1 : fp;
+    const double cs = vs[i] * fs, cp = vp[i] * fp;
+    const cx<double> vcs(cs, -cs * (double)qs[i] / 2.0), vcp(cp, -cp * (double)qp[i] / 2.0);
+    const cx<double> m = vcs * vcs * r;
+    mu[i] = m;
+    da[i] = vcp * vcp * r - 2.0 * m;
+    ro[i] = r;
+}
+
 template <int S, class R, class OutT>
 __device__ __forceinline__ void emit_slot(int region, const NodeCoefs<R> &c, const Stretch<R> &f, R m2, R m3,
                                           R m4, cx<R> m1, cx<R> r1x, cx<R> r1y, R dxo8, unsigned mask,
@@ -198,6 +222,20 @@ int device_lame(long long nn, const float *d_vp, const float *d_vs, const float 
 {
     int th = 256;
     k_lame<<<ceil_div(nn, th), th, 0, st>>>(nn, d_vp, d_vs, d_rho, (cx<double> *)d_da, (cx<double> *)d_mu, d_ro);
+    WT_CUDA(cudaGetLastError());
+    return WT3D_OK;
+}
+
+int device_lame_q(long long nn, const float *d_vp, const float *d_vs, const float *d_rho, const float *d_qp,
+                  const float *d_qs, double omega_re, double freqbase, void *d_da, void *d_mu, double *d_ro,
+                  cudaStream_t st)
+{
+    const double omegabase = freqbase * 2.0 * 3.141592653589793;
+    const double eps = 10.0 * 1.1920929e-07;   // 10 EPSILON(1.0) (dispersion.f:49)
+    if (!(omega_re > eps && omegabase > 0.0))  // no dispersion (dispersion.f:78-80)
+        return device_lame(nn, d_vp, d_vs, d_rho, d_da, d_mu, d_ro, st);
+    k_lame_q<<<ceil_div(nn, 256), 256, 0, st>>>(nn, d_vp, d_vs, d_rho, d_qp, d_qs, std::log(omega_re / omegabase),
+                                                (cx<double> *)d_da, (cx<double> *)d_mu, d_ro);
     WT_CUDA(cudaGetLastError());
     return WT3D_OK;
 }

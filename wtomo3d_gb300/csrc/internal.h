@@ -15,6 +15,9 @@ void grid_pml(const wt3d_grid &g, double &pmld, double &pmlf, int &ipml);
 int device_pattern(int nx, int ny, int nz, int base, int *d_irptr, int *d_jcptr, cudaStream_t st);
 int device_lame(long long nn, const float *d_vp, const float *d_vs, const float *d_rho, void *d_da, void *d_mu,
                 double *d_ro, cudaStream_t st);
+int device_lame_q(long long nn, const float *d_vp, const float *d_vs, const float *d_rho, const float *d_qp,
+                  const float *d_qs, double omega_re, double freqbase, void *d_da, void *d_mu, double *d_ro,
+                  cudaStream_t st);
 int device_assemble(const wt3d_grid &g, const void *d_da, const void *d_mu, const double *d_ro, double om_re,
                     double om_im, const int *d_irptr, void *d_a, cudaStream_t st);
 
