@@ -233,6 +233,15 @@ int wt3d_rhs_sources(wt3d_solver *h, int nsrc, const double *xyz, const int *com
 int wt3d_sample_receivers(wt3d_solver *h, int nrhs, const void *d_U, int nrec, const double *xyz, int ireg,
                           double sprd, double _Complex *out);
 
+/* Hydrophone pressure of device wavefields d_U (n x nrhs), makeuh.f:113-167:
+ * p = (lambda + 2 mu / 3) (du/dx + dv/dy + dw/dz) with lambda, mu of the
+ * node INT(1.5 + x/dx) (clamped) and each derivative the centred difference
+ * of receiver samples at +-dx, divided by (-i omega) and negated as written
+ * there.  out[j*nrec + r].  A receiver response (recin, makeuh.f:92-97) is a
+ * per-receiver factor the caller applies. */
+int wt3d_sample_pressure(wt3d_solver *h, int nrhs, const void *d_U, int nrec, const double *xyz, int ireg,
+                         double sprd, double _Complex *out);
+
 /* Statistics of the last factorisation. */
 typedef struct wt3d_stats {
     long long n, nnz;              /* unknowns, operator nonzeros             */

@@ -38,3 +38,38 @@ def test_rhs_sources_and_receivers():
                     for c in range(3):
                         assert abs(smp[j, r, c] - np.dot(w, U[j, 3 * node + c])) < 1e-12
             del F, dU
+
+
+def test_pressure_matches_makeuh_restatement():
+    """Hydrophone pressure (makeuh.f:113-167) against a numpy restatement on
+    the same receiver weights and the model's Lame parameters."""
+    g = Grid(24, 22, 20, 20.0, pmld=80.0, fst=1)
+    vp, vs, rho = model.layered_random(24, 22, 20, 20.0, seed=4, corr_len=80.0)
+    om = 2 * np.pi * 2.0
+    xyz = np.array([[207.3, 181.9, 63.1], [120.0, 200.0, 13.1]])
+    rng = np.random.default_rng(5)
+    U = rng.standard_normal((2, g.n)) + 1j * rng.standard_normal((2, g.n))
+    with wt.Solver(g) as s:
+        s.set_model(vp, vs, rho)
+        s.factor(om)
+        dU = torch.from_numpy(U).cuda()
+        for ireg in (0, 3):
+            got = s.sample_pressure(dU.data_ptr(), 2, xyz, ireg, 0.5)
+            for j in range(2):
+                for r in range(2):
+                    x, y, z = xyz[r]
+                    div = 0
+                    for a in range(3):
+                        pm = []
+                        for sgn in (-1, 1):
+                            q = [x, y, z]
+                            q[a] += sgn * g.dx
+                            node, w = wt.source_weights(g, *q, ireg, 0.5)
+                            pm.append(np.dot(w, U[j, 3 * node + a]))
+                        div += -(pm[1] - pm[0]) / (2 * g.dx * (-1j * om))
+                    ix, iy, iz = [min(max(int(1.5 + c / g.dx), 1), m) for c, m in ((x, 24), (y, 22), (z, 20))]
+                    P, S, R = [float(t[iz - 1, ix - 1, iy - 1]) for t in (vp, vs, rho)]
+                    mu = S * S * R
+                    lam = P * P * R - 2 * mu
+                    assert abs(got[j, r] - (lam + 2 * mu / 3) * div) <= 1e-10 * abs((lam + 2 * mu / 3) * div)
+        del dU

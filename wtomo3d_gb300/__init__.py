@@ -132,6 +132,7 @@ def lib():
                                           ctypes.c_double, ctypes.c_int, vp, vp, ctypes.POINTER(ctypes.c_int)]
         L.wt3d_rhs_sources.argtypes = [vp, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_double, vp]
         L.wt3d_sample_receivers.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, vp, ctypes.c_int, ctypes.c_double, vp]
+        L.wt3d_sample_pressure.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, vp, ctypes.c_int, ctypes.c_double, vp]
         L.wt3d_update_operator.argtypes = [vp]
         L.wt3d_gradient_contract.argtypes = [vp, ctypes.c_int, vp, vp, vp]
         L.wt3d_misfit_gradient.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, ctypes.c_double,
@@ -317,6 +318,14 @@ class Solver:
         out = np.zeros((nrhs, len(xyz), 3), np.complex128)
         _check(lib().wt3d_sample_receivers(self._h, int(nrhs), ctypes.c_void_p(d_U), len(xyz), _ptr(xyz), int(ireg),
                                            float(sprd), _ptr(out)))
+        return out
+
+    def sample_pressure(self, d_U, nrhs, xyz, ireg=0, sprd=0.5):
+        """Hydrophone pressure (makeuh.f), shape (nrhs, nrec)."""
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+        out = np.zeros((nrhs, len(xyz)), np.complex128)
+        _check(lib().wt3d_sample_pressure(self._h, int(nrhs), ctypes.c_void_p(d_U), len(xyz), _ptr(xyz), int(ireg),
+                                          float(sprd), _ptr(out)))
         return out
 
     def apply_device(self, d_X, d_Y, nrhs):

@@ -1267,6 +1267,54 @@ int wt3d_sample_receivers(wt3d_solver *h, int nrhs, const void *d_U, int nrec, c
     return WT3D_OK;
 }
 
+int wt3d_sample_pressure(wt3d_solver *h, int nrhs, const void *d_U, int nrec, const double *xyz, int ireg,
+                         double sprd, double _Complex *out)
+{
+    if (!h || nrhs < 1 || !d_U || nrec < 1 || !xyz || !out) { set_error("wt3d_sample_pressure: bad arguments"); return WT3D_ERR_ARG; }
+    if (!h->have_model || !h->have_values) { set_error("wt3d_sample_pressure: needs a model and an assembled operator"); return WT3D_ERR_STATE; }
+    const wt3d_grid &g = h->grid;
+    const double d = g.dx;
+    // six sampling points per hydrophone: x -+ dx (u), y -+ dy (v), z -+ dz (w) (makeuh.f:137-153)
+    std::vector<double> pts((size_t)nrec * 6 * 3);
+    for (int r = 0; r < nrec; r++)
+        for (int a = 0; a < 3; a++)
+            for (int sgn = 0; sgn < 2; sgn++) {
+                double *q = &pts[((size_t)r * 6 + a * 2 + sgn) * 3];
+                q[0] = xyz[3 * r]; q[1] = xyz[3 * r + 1]; q[2] = xyz[3 * r + 2];
+                q[a] += sgn ? d : -d;
+            }
+    std::vector<std::complex<double>> smp((size_t)nrhs * nrec * 6 * 3);
+    int rc = wt3d_sample_receivers(h, nrhs, d_U, nrec * 6, pts.data(), ireg, sprd,
+                                   reinterpret_cast<double _Complex *>(smp.data()));
+    if (rc) return rc;
+    // Lame parameters at the hydrophone node INT(1.5 + x/dx), clamped (makeuh.f:130-136)
+    std::vector<double2> lam(nrec), muv(nrec);
+    for (int r = 0; r < nrec; r++) {
+        int ix = (int)(1.5 + xyz[3 * r] / d), iy = (int)(1.5 + xyz[3 * r + 1] / d), iz = (int)(1.5 + xyz[3 * r + 2] / d);
+        ix = std::min(std::max(ix, 1), g.nx);
+        iy = std::min(std::max(iy, 1), g.ny);
+        iz = std::min(std::max(iz, 1), g.nz);
+        const long long node = (iz - 1) + (long long)g.nz * ((ix - 1) + (long long)g.nx * (iy - 1));
+        WT_CUDA(cudaMemcpyAsync(&lam[r], h->da.p + node, sizeof(double2), cudaMemcpyDeviceToHost, h->st));
+        WT_CUDA(cudaMemcpyAsync(&muv[r], h->mu.p + node, sizeof(double2), cudaMemcpyDeviceToHost, h->st));
+    }
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    const std::complex<double> cfact = std::complex<double>(0.0, -1.0) * std::complex<double>(h->om_re, h->om_im);
+    std::complex<double> *o = reinterpret_cast<std::complex<double> *>(out);
+    for (int j = 0; j < nrhs; j++)
+        for (int r = 0; r < nrec; r++) {
+            std::complex<double> div = 0;
+            for (int a = 0; a < 3; a++) {
+                const std::complex<double> um = smp[(((size_t)j * nrec + r) * 6 + a * 2) * 3 + a];
+                const std::complex<double> up = smp[(((size_t)j * nrec + r) * 6 + a * 2 + 1) * 3 + a];
+                div += -(up - um) / (2.0 * d * cfact);
+            }
+            const std::complex<double> L(lam[r].x, lam[r].y), M(muv[r].x, muv[r].y);
+            o[(size_t)j * nrec + r] = (L + 2.0 * M / 3.0) * div;
+        }
+    return WT3D_OK;
+}
+
 int wt3d_mem_info(double *free_bytes, double *total_bytes)
 {
     size_t f = 0, t = 0;
