@@ -26,6 +26,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "solves/s @96x96x64 mixed vs FP64 GPU at resid<=1e-8; serve p50/p99 ms"
+# ncu capture of one k_tc_gemm launch (profiles/k_tc_gemm_8192x8192.md):
+# dram__bytes_read.sum + dram__bytes_write.sum, and the launch's algorithmic
+# bytes (split operands once + C read and written once)
+TC_CAPTURE = {"launch": "M=N=8192, K=512 (python -m wtomo3d_gb300.gemm_bench 8192 8192 512)",
+              "dram_bytes": 1.684584e9 + 0.504824e9, "algorithmic_bytes": 0.201e9 + 2 * 0.5369e9}
 FREQS = [0.5, 1.0, 1.5, 2.0]
 
 
@@ -249,7 +254,13 @@ def run_ours(args, rank, world):
         "roofline": {"bound": "tensor", "kernel": "k_tc_gemm (tcgen05 3xTF32 front Schur/trailing updates)",
                      "achieved": gemm_tflops, "peak": peak, "unit": "TFLOP/s", "frac": gemm_tflops / peak,
                      "peak_source": "%s bf16_tflops_sustained" % pk_src,
-                     "gemm_time_share": gemm_ms / total_ms, "traffic": None},
+                     "gemm_time_share": gemm_ms / total_ms,
+                     # DRAM bytes of one captured launch of this kernel: a whole
+                     # factorisation's DRAM capture takes several ncu passes, which
+                     # the capture rules allow only on a small case
+                     "traffic": TC_CAPTURE["dram_bytes"],
+                     "traffic_launch": TC_CAPTURE["launch"],
+                     "traffic_algorithmic": TC_CAPTURE["algorithmic_bytes"]},
         "steps_detail": recs,
         "factor": {"flops": st["factor_flops"], "entries": st["factor_entries"], "fronts": st["nfronts"],
                    "analyse_s": t_analyse, "profile_ms": prof},
