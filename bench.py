@@ -26,7 +26,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "solves/s @96x96x64 mixed vs FP64 GPU at resid<=1e-8; serve p50/p99 ms"
-# ncu capture of one k_tc_gemm launch (profiles/k_tc_gemm_8192x8192.md):
+# ncu capture (--set full) of one k_tc_gemm launch of the GEMM microbenchmark:
 # dram__bytes_read.sum + dram__bytes_write.sum, and the launch's algorithmic
 # bytes (split operands once + C read and written once)
 TC_CAPTURE = {"launch": "M=N=8192, K=512 (python -m wtomo3d_gb300.gemm_bench 8192 8192 512)",
@@ -48,9 +48,10 @@ class Clocks:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, dev):
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % dev)
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+    def __init__(self, dev, path=None):
+        import tempfile
+        self.path = path or os.path.join(tempfile.gettempdir(), "wt3d_clocks_%d_%d.csv" % (dev, os.getpid()))
+        os.makedirs(os.path.dirname(os.path.abspath(self.path)), exist_ok=True)
         self.dev = dev
         self.p = None
 
@@ -173,7 +174,7 @@ def run_ours(args, rank, world):
                     launches=st["kernels_factor"] + st["kernels_solve"] + 4)   # + background, expansion, source
 
     run_pipelined(args.warmup, 0, step, nl)
-    clocks = Clocks(dev)
+    clocks = Clocks(dev, args.clocks_log)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -378,6 +379,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--clocks-log", default=None, help="file for the nvidia-smi samples of the timed region")
     ap.add_argument("--lanes", type=int, default=2, help="pipelined solver handles (1 = sequential steps)")
     ap.add_argument("--serve-requests", type=int, default=30)
     ap.add_argument("--serve-rate", type=float, default=0.3)
