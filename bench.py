@@ -134,7 +134,7 @@ def run_ours(args, rank, world):
     import ctypes
     import torch
     import wtomo3d_gb300 as wt
-    from wtomo3d_gb300 import Grid, model
+    from wtomo3d_gb300 import Grid, model, replicas
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
@@ -164,7 +164,7 @@ def run_ours(args, rank, world):
 
     def step(l, i):
         s = S[l]
-        f = FREQS[(i + rank) % len(FREQS)]
+        f = replicas.rank_frequency(i, rank, FREQS)
         s.factor(2 * np.pi * f)
         s.rhs_planewave(layers, ain, baz, d_F=dB[l].data_ptr())
         rr = s.solve_device(dB[l].data_ptr(), dX[l].data_ptr(), nrhs, tol=args.tol, maxit=30)
@@ -189,11 +189,8 @@ def run_ours(args, rank, world):
     ck = clocks.stop()
     ms = e0.elapsed_time(e1)
     launches = sum(r.pop("launches") for r in recs)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * nrhs * args.steps / (ms / 1e3)
+    ms = replicas.max_over_ranks(ms, world, "cuda")
+    value = replicas.job_rate(world, nrhs * args.steps, ms / 1e3)
 
     # ---- end to end through the public API: host model, background and source
     # parameters in, solutions back to pinned host memory ----
@@ -204,7 +201,7 @@ def run_ours(args, rank, world):
 
     def e2e_step(l, i):
         s = S[l]
-        f = FREQS[(i + rank) % len(FREQS)]
+        f = replicas.rank_frequency(i, rank, FREQS)
         L.wt3d_set_model(s._h, *[ctypes.c_void_p(a.data_ptr()) for a in host_models[0]])
         L.wt3d_set_background(s._h, *[ctypes.c_void_p(a.data_ptr()) for a in host_models[1]])
         s.factor(2 * np.pi * f)
@@ -219,12 +216,8 @@ def run_ours(args, rank, world):
     t0 = time.perf_counter()
     run_pipelined(args.steps, args.warmup, e2e_step, nl)
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = world * nrhs * args.steps / e2e_s
+    e2e_s = replicas.max_over_ranks(time.perf_counter() - t0, world, "cuda")
+    e2e = replicas.job_rate(world, nrhs * args.steps, e2e_s)
     h2d = 2 * sum(a.nbytes for a in (vp, vs, rho)) + ain.nbytes + baz.nbytes
     d2h = Xh[0].numel() * 16
     s = S[0]

@@ -558,6 +558,7 @@ int tc_init()
 // ---------------------------------------------------------------------------
 // C ABI check entry: one GEMM C -= A B on host complex64 arrays (row-major),
 // through the tensor-core path (path = 1) or the SIMT path (path = 0).
+// wt3d_bench_gemm also times path 2, the tall-skinny kernel of the solves.
 // ---------------------------------------------------------------------------
 using namespace wt3d;
 extern "C" int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int lda, const void *B, int ldb, void *C,
@@ -641,15 +642,16 @@ extern "C" int wt3d_bench_gemm(int path, int M, int N, int K, int iters, double 
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     const long long tiles = (long long)((M + GBM - 1) / GBM) * g.tiles_n;
-    for (int w = 0; w < 2; w++) {   // warm-up
+    const long long ts_tiles = (M + TSBM - 1) / TSBM;   // path 2: tall-skinny kernel (N <= 32)
+    if (path == 2 && N > TSBN) { set_error("wt3d_bench_gemm: path 2 needs N <= 32"); return WT3D_ERR_ARG; }
+    auto launch = [&]() {
         if (path == 1) tc_mma(L, err.p, 0);
+        else if (path == 2) k_gemm_ts<float><<<(unsigned)ts_tiles, 256>>>(dt.p, 1);
         else k_gemm<float><<<(unsigned)tiles, 256>>>(dt.p, 1);
-    }
+    };
+    for (int w = 0; w < 2; w++) launch();   // warm-up
     cudaEventRecord(e0);
-    for (int i = 0; i < iters; i++) {
-        if (path == 1) tc_mma(L, err.p, 0);
-        else k_gemm<float><<<(unsigned)tiles, 256>>>(dt.p, 1);
-    }
+    for (int i = 0; i < iters; i++) launch();
     cudaEventRecord(e1);
     WT_CUDA(cudaEventSynchronize(e1));
     float ms = 0;

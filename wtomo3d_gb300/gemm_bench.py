@@ -1,6 +1,7 @@
 """Microbenchmark of the front-update GEMM C -= A B (complex64, row-major)
-through the tcgen05 kernel (path 1) or the SIMT kernel (path 0), on random
-operands resident on the device:
+through the tcgen05 kernel (path 1), the SIMT kernel (path 0) or the
+tall-skinny SIMT kernel of the solves (path 2, N <= 32), on random operands
+resident on the device:
 
     python -m wtomo3d_gb300.gemm_bench M N K [--path 1] [--reps 5]
 
@@ -22,7 +23,7 @@ def main():
     ap.add_argument("M", type=int)
     ap.add_argument("N", type=int)
     ap.add_argument("K", type=int)
-    ap.add_argument("--path", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--path", type=int, default=1, choices=[0, 1, 2])
     ap.add_argument("--reps", type=int, default=5)
     a = ap.parse_args()
     import wtomo3d_gb300 as wt
@@ -33,7 +34,7 @@ def main():
     if rc:
         raise SystemExit("wt3d_bench_gemm failed (%d): %s" % (rc, L.wt3d_last_error().decode()))
     fl = 8.0 * a.M * a.N * a.K
-    print(json.dumps({"M": a.M, "N": a.N, "K": a.K, "path": "tcgen05" if a.path else "simt", "ms": ms.value,
+    print(json.dumps({"M": a.M, "N": a.N, "K": a.K, "path": ["simt", "tcgen05", "simt-tall-skinny"][a.path], "ms": ms.value,
                       "tflops": fl / ms.value / 1e9}))
 
 
