@@ -149,8 +149,11 @@ def run_ours(args, rank, world):
     ain, baz = plane_wave_sources(nrhs)
     rhs_desc = ("%d Haskell plane-wave P sources per frequency (incidence U[0,30] deg, back-azimuth U[0,360), "
                 "seed 11), scattered-field f = (A_bg - A) u0 against the unperturbed layered background" % nrhs)
-    # two lanes (handles) of the same grid, pipelined frequencies
+    # two lanes (handles) of the same grid, pipelined frequencies; the
+    # factorisations' tensor-core GEMM leaves sm_reserve SMs to the other
+    # lane's substitution passes
     nl = args.lanes
+    wt.set_sm_reserve(args.sm_reserve if nl > 1 else 0)
     t0 = time.perf_counter()
     S = [wt.Solver(g, wt.PREC_MIXED) for _ in range(nl)]
     t_analyse = time.perf_counter() - t0
@@ -242,7 +245,8 @@ def run_ours(args, rank, world):
                    "l2": "inputs larger than L2 (factors %.1f GB)" % (st["factor_bytes"] / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "pipelining": "%d solver handles of the same grid, alternate frequencies from %d host threads: "
-                                 "one frequency's substitution passes overlap the next one's factorisation" % (nl, nl)},
+                                 "one frequency's substitution passes overlap the next one's factorisation; "
+                                 "tensor-core GEMM on %d SMs less" % (nl, nl, args.sm_reserve if nl > 1 else 0)},
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "tensor", "kernel": "k_tc_gemm (tcgen05 3xTF32 front Schur/trailing updates)",
@@ -267,6 +271,7 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     for h in S:
         h.close()
+    wt.set_sm_reserve(0)
     return out
 
 
@@ -374,6 +379,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--clocks-log", default=None, help="file for the nvidia-smi samples of the timed region")
     ap.add_argument("--lanes", type=int, default=2, help="pipelined solver handles (1 = sequential steps)")
+    ap.add_argument("--sm-reserve", type=int, default=0, help="SMs the factorisation GEMM leaves to the other lane")
     ap.add_argument("--serve-requests", type=int, default=30)
     ap.add_argument("--serve-rate", type=float, default=0.3)
     args = ap.parse_args()

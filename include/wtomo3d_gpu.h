@@ -242,6 +242,12 @@ int wt3d_sample_receivers(wt3d_solver *h, int nrhs, const void *d_U, int nrec, c
 int wt3d_sample_pressure(wt3d_solver *h, int nrhs, const void *d_U, int nrec, const double *xyz, int ireg,
                          double sprd, double _Complex *out);
 
+/* Number of SMs the persistent tensor-core GEMM of the factorisations leaves
+ * idle, process-wide (default 0).  A nonzero reserve lets the substitution
+ * passes of another handle run during a factorisation (two handles pipelining
+ * frequencies).  No reference counterpart. */
+int wt3d_set_sm_reserve(int n);
+
 /* Statistics of the last factorisation. */
 typedef struct wt3d_stats {
     long long n, nnz;              /* unknowns, operator nonzeros             */

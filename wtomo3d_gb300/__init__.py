@@ -125,6 +125,7 @@ def lib():
         L.wt3d_apply.argtypes = [vp, ctypes.c_int, vp, vp]
         L.wt3d_apply_device.argtypes = [vp, ctypes.c_int, vp, vp]
         L.wt3d_solver_bytes.argtypes = [ctypes.POINTER(Grid), ctypes.c_int, vp]
+        L.wt3d_set_sm_reserve.argtypes = [ctypes.c_int]
         L.wt3d_batch_buffers.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp)]
         L.wt3d_memcpy.argtypes = [vp, vp, vp, ctypes.c_longlong]
         L.wt3d_mem_info.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
@@ -170,6 +171,11 @@ def _f32(a, n):
     if a.size != n:
         raise ValueError("model array has %d entries, expected %d" % (a.size, n))
     return a
+
+
+def set_sm_reserve(n):
+    """SMs the factorisations' persistent tensor-core GEMM leaves to other work."""
+    _check(lib().wt3d_set_sm_reserve(int(n)))
 
 
 def set_device(dev):

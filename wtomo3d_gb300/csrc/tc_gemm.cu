@@ -27,6 +27,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include "tc_gemm.h"
+#include <atomic>
 #include <cstring>
 
 namespace wt3d {
@@ -537,10 +538,15 @@ static int num_sms()
     return n;
 }
 
+// SMs the persistent tensor-core kernel leaves to concurrent work (other
+// handles' substitution passes): set through wt3d_set_sm_reserve.
+static std::atomic<int> g_sm_reserve{0};
+
 void tc_mma(const TcLaunch &L, int *err, cudaStream_t st)
 {
     if (L.ntasks == 0) return;
-    const long long grid = std::min<long long>(L.tiles, num_sms());
+    const int sms = std::max(1, num_sms() - g_sm_reserve.load());
+    const long long grid = std::min<long long>(L.tiles, sms);
     k_tc_gemm<<<(unsigned)grid, TC_THREADS, TC_SMEM, st>>>(L.tasks.p, L.ntasks, L.tiles,
                                                            reinterpret_cast<const CUtensorMap *>(L.maps.p), err);
 }
@@ -561,6 +567,13 @@ int tc_init()
 // wt3d_bench_gemm also times path 2, the tall-skinny kernel of the solves.
 // ---------------------------------------------------------------------------
 using namespace wt3d;
+extern "C" int wt3d_set_sm_reserve(int n)
+{
+    if (n < 0) { set_error("wt3d_set_sm_reserve: negative"); return WT3D_ERR_ARG; }
+    g_sm_reserve.store(n);
+    return WT3D_OK;
+}
+
 extern "C" int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int lda, const void *B, int ldb, void *C,
                                int ldc)
 {
