@@ -275,6 +275,60 @@ def run_ours(args, rank, world):
     return out
 
 
+def assembly_rate(dims, reps=3):
+    """Device assembly of A (complex128 CSR values) at 1 Hz on a grid, in HBM
+    bytes per second: algorithmic bytes = nnz x 16 written + 3 x 4 bytes of
+    model per node read + (n + 1) x 4 bytes of row pointers read."""
+    import ctypes
+    import torch
+    import wtomo3d_gb300 as wt
+    from wtomo3d_gb300 import Grid, model
+    nx, ny, nz = dims
+    g = Grid(nx, ny, nz, 20.0, pmld=(12 if nx >= 128 else 10) * 20.0, fst=1, usemin=1)
+    # row pointers from the closed form: 3 rows per node of 3 * (3x3x3 box clipped) entries
+    def cnt(n):
+        c = np.full(n, 3)
+        c[0] -= 1
+        c[-1] -= 1
+        return c
+    cz, cx, cy = cnt(nz), cnt(nx), cnt(ny)
+    per_node = 3 * (cz[:, None, None] * cx[None, :, None] * cy[None, None, :]).reshape(-1, order="F")
+    rows = np.repeat(per_node, 3)
+    irptr = np.zeros(3 * nx * ny * nz + 1, np.int32)
+    irptr[1:] = np.cumsum(rows)
+    nnz = int(irptr[-1])
+    vp, vs, rho = [torch.from_numpy(np.ascontiguousarray(a.reshape(-1, order="F"))).cuda()
+                   for a in model.layered_random(nx, ny, nz, 20.0, seed=1)]
+    dir_ = torch.from_numpy(irptr).cuda()
+    da = torch.empty(nnz, dtype=torch.complex128, device="cuda")
+    st = torch.cuda.Stream()
+    L = wt.lib()
+    L.wt3d_assemble_device.argtypes = [ctypes.POINTER(Grid), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p]
+    args = (ctypes.byref(g), ctypes.c_void_p(vp.data_ptr()), ctypes.c_void_p(vs.data_ptr()),
+            ctypes.c_void_p(rho.data_ptr()), 2 * np.pi, 0.0, ctypes.c_void_p(dir_.data_ptr()),
+            ctypes.c_void_p(da.data_ptr()), ctypes.c_void_p(st.cuda_stream))
+    torch.cuda.synchronize()
+    if L.wt3d_assemble_device(*args):
+        raise RuntimeError(L.wt3d_last_error().decode())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        L.wt3d_assemble_device(*args)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nbytes = nnz * 16 + nx * ny * nz * 12 + (3 * nx * ny * nz + 1) * 4
+    pk, src = peaks()
+    out = {"dims": list(dims), "nnz": nnz, "bytes": nbytes, "ms": ms, "gb_per_s": nbytes / ms / 1e6,
+           "frac": nbytes / ms / 1e6 / pk["hbm_gbs"], "peak_source": "%s hbm_gbs" % src,
+           "note": "includes the per-node Lame conversion of the model (one small kernel)"}
+    del vp, vs, rho, dir_, da, st
+    torch.cuda.synchronize()
+    return out
+
+
 def run_serve(args):
     """Serving loop (configuration 3): a seeded Poisson stream of requests over
     grids 48^3, 64^3 and 96x96x64 (weights 0.5/0.35/0.15), model seeds from a
@@ -411,6 +465,10 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
     out = run_ours(args, rank, world)
+    if rank == 0:
+        # assembly throughput at the benchmark grid and at the largest grid
+        # (128x128x96, 12-node PML), whose factors do not fit one GPU
+        out["assembly"] = [assembly_rate(tuple(args.dims)), assembly_rate((128, 128, 96))]
     if rank == 0 and not args.no_serve:
         out["serve"] = run_serve(args)
     if rank == 0:
