@@ -73,3 +73,17 @@ def test_job1_rejects_non_grid_pattern():
     a = np.ones(len(jc), np.complex64)
     b = np.zeros(n, np.complex64)
     assert wt.strumpack_serial_finter(1, n, len(jc), ir, jc, a, b, b.copy()) == 1
+
+
+def test_too_large_grid_is_rejected_before_any_device_work():
+    """nnz must fit int32 CSR indices (the reference's INTEGER pattern)."""
+    import ctypes
+    import pytest
+    import wtomo3d_gb300 as wt
+    g = wt.Grid(400, 400, 400, 10.0)
+    with pytest.raises(wt.WT3DError) as e:
+        wt.solver_bytes(g)
+    assert e.value.code == wt.WT3D_ERR_ARG
+    with pytest.raises(wt.WT3DError) as e:
+        wt.Solver(wt.Grid(1, 5, 5, 10.0))
+    assert e.value.code == wt.WT3D_ERR_ARG

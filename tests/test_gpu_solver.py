@@ -193,3 +193,23 @@ def test_slow_refinement_switches_to_gmres():
                 res = torch.linalg.norm(F - Y, dim=1) / torch.linalg.norm(F, dim=1)
                 assert float(res.max()) <= 2e-10
         del F, X, Y
+
+
+def test_degenerate_grids_and_zero_columns():
+    """Smallest grids (every row Dirichlet or one interior node), and a zero
+    right-hand side next to nonzero ones: the zero column stays exactly zero
+    and the others converge."""
+    for dims in ((2, 2, 2), (3, 3, 3), (3, 4, 5)):
+        g = Grid(*dims, 20.0, pmld=20.0, fst=0)
+        with wt.Solver(g) as s:
+            s.set_model(*model.homogeneous(*dims))
+            s.factor(2 * np.pi)
+            rng = np.random.default_rng(1)
+            B = np.zeros((g.n, 3), complex)
+            B[:, 0] = rng.standard_normal(g.n)
+            B[:, 2] = 1j
+            X = s.solve(B, tol=1e-10)
+            assert np.all(X[:, 1] == 0)
+            Y = s.apply(X)
+            for j in (0, 2):
+                assert np.linalg.norm(Y[:, j] - B[:, j]) <= 1e-9 * np.linalg.norm(B[:, j])

@@ -142,8 +142,11 @@ public:
         }
         if ((rc = fr.upload(h))) return rc;
         if ((rc = dinv.alloc((size_t)npan * 2 * KB * KB))) return rc;
-        static std::once_flag attr_once;
-        std::call_once(attr_once, [] {
+        // kernel attributes are per device: once for each device this process uses
+        static std::once_flag attr_once[64];
+        int dev = 0;
+        cudaGetDevice(&dev);
+        std::call_once(attr_once[dev & 63], [] {
             size_t sp = sizeof(cx<T>) * (KB * (KB + 1) + 2 * KB * (KB + 1));
             cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp);
             cudaFuncSetAttribute(k_trsm_row<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
