@@ -162,7 +162,14 @@ int wt3d_solve(wt3d_solver *h, int nrhs, const double _Complex *B, double _Compl
 int wt3d_solve_adjoint(wt3d_solver *h, int nrhs, const double _Complex *B, double _Complex *X,
                        double tol, int maxit, double *relres, int *iters);
 
-/* Device-pointer solve: d_B, d_X device complex128, column-major n x nrhs. */
+/* Device-pointer solve: d_B, d_X device complex128, column-major n x nrhs.
+ *
+ * Calls that take caller device buffers (wt3d_*_device, wt3d_rhs_*,
+ * wt3d_sample_*, wt3d_gradient_contract, wt3d_misfit_gradient, wt3d_memcpy)
+ * first wait for all work already queued on the legacy default stream (where
+ * PyTorch runs unless told otherwise), so buffers filled there need no
+ * synchronisation; work on other streams must be complete before the call.
+ * Each call synchronises before it returns, so its outputs are ready. */
 int wt3d_solve_device(wt3d_solver *h, int nrhs, const void *d_B, void *d_X,
                       double tol, int maxit, double *relres, int *iters, int adjoint);
 
@@ -302,8 +309,10 @@ int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *perm, int *
 /* Select the CUDA device of the calling thread (one process per GPU). */
 int wt3d_set_device(int dev);
 
-/* The CUDA stream (cudaStream_t) every call on this handle runs on, for
- * callers that time or order work against it. */
+/* The CUDA stream (cudaStream_t) the factorisation and operator calls of this
+ * handle run on.  Solves and refinement run on a second stream of the
+ * handle, created with the greatest priority, so that they are scheduled
+ * ahead of other handles' factorisations. */
 void *wt3d_get_stream(wt3d_solver *h);
 
 /* Factor the current operator once with an event pair around every launch

@@ -198,7 +198,10 @@ def test_slow_refinement_switches_to_gmres():
 def test_degenerate_grids_and_zero_columns():
     """Smallest grids (every row Dirichlet or one interior node), and a zero
     right-hand side next to nonzero ones: the zero column stays exactly zero
-    and the others converge."""
+    and the others converge.  Dirichlet rows (diagonal 1) sit next to interior
+    rows of ~3e8 here, so FP64 rounding in r = b - A x alone bounds the
+    attainable relative residual near eps * |A| |x| / |b| ~ 1e-9 (refinement
+    in FP64 with an exact solve stalls there too): the tolerance is 1e-8."""
     for dims in ((2, 2, 2), (3, 3, 3), (3, 4, 5)):
         g = Grid(*dims, 20.0, pmld=20.0, fst=0)
         with wt.Solver(g) as s:
@@ -208,8 +211,8 @@ def test_degenerate_grids_and_zero_columns():
             B = np.zeros((g.n, 3), complex)
             B[:, 0] = rng.standard_normal(g.n)
             B[:, 2] = 1j
-            X = s.solve(B, tol=1e-10)
+            X = s.solve(B, tol=1e-8)
             assert np.all(X[:, 1] == 0)
             Y = s.apply(X)
             for j in (0, 2):
-                assert np.linalg.norm(Y[:, j] - B[:, j]) <= 1e-9 * np.linalg.norm(B[:, j])
+                assert np.linalg.norm(Y[:, j] - B[:, j]) <= 2e-8 * np.linalg.norm(B[:, j])

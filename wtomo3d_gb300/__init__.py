@@ -381,7 +381,7 @@ class Solver:
 
     @property
     def stream(self):
-        """cudaStream_t (as an int) every call on this handle runs on."""
+        """cudaStream_t (as an int) of the handle's factorisation and operator calls."""
         return lib().wt3d_get_stream(self._h) or 0
 
     def solve_device(self, d_B, d_X, nrhs, tol=1e-8, maxit=20, adjoint=False, allow_noconv=False):

@@ -7,6 +7,7 @@
 #include <chrono>
 #include <map>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -115,7 +116,7 @@ __global__ void __launch_bounds__(256) k_residual(long long n, int m, const int 
 // Column c of every block is an independent system; reductions go through
 // per-block partial sums and a second pass, so they do not depend on
 // scheduling.
-constexpr int GM_K = 8;          // restart length of the flexible GMRES
+constexpr int GM_KMAX = 16;      // longest restart of the flexible GMRES (per-call length gmres_restart())
 constexpr int GM_BLOCKS = 304;   // 2 blocks per SM for the reductions
 
 // part[b][i][c] = sum over the rows of block b of conj(V_i[row, c]) W[row, c], i < nv.
@@ -148,7 +149,7 @@ __global__ void __launch_bounds__(256) k_mdot(long long n, int m, int nv, const 
         if (threadIdx.x < MAXRHS) {
             double2 t = make_double2(0, 0);
             for (int q = 0; q < 8; q++) { t.x += red[q][threadIdx.x].x; t.y += red[q][threadIdx.x].y; }
-            part[((long long)blockIdx.x * (GM_K + 1) + i) * MAXRHS + threadIdx.x] = t;
+            part[((long long)blockIdx.x * (GM_KMAX + 1) + i) * MAXRHS + threadIdx.x] = t;
         }
         __syncthreads();
     }
@@ -161,7 +162,7 @@ __global__ void k_mdot_reduce(int nblocks, int nv, const double2 *__restrict__ p
     if (i >= nv || c >= MAXRHS) return;
     double2 t = make_double2(0, 0);
     for (int b = 0; b < nblocks; b++) {
-        const double2 v = part[((long long)b * (GM_K + 1) + i) * MAXRHS + c];
+        const double2 v = part[((long long)b * (GM_KMAX + 1) + i) * MAXRHS + c];
         t.x += v.x; t.y += v.y;
     }
     h[i * MAXRHS + c] = t;
@@ -177,15 +178,15 @@ __global__ void __launch_bounds__(256) k_maxpy(long long n, int m, int nv, const
     const long long tot = n * MAXRHS;
     const long long stride = (long long)gridDim.x * blockDim.x;   // a multiple of MAXRHS: fixed column per thread
     const int c = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) % MAXRHS);
-    double2 cf[GM_K + 1];
+    double2 cf[GM_KMAX + 1];
 #pragma unroll
-    for (int i = 0; i <= GM_K; i++) cf[i] = i < nv ? coef[i * MAXRHS + c] : make_double2(0, 0);
+    for (int i = 0; i <= GM_KMAX; i++) cf[i] = i < nv ? coef[i * MAXRHS + c] : make_double2(0, 0);
     double s2 = 0;
     if (c < m) {
         for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += stride) {
             double2 w = W[q];
 #pragma unroll
-            for (int i = 0; i <= GM_K; i++) {
+            for (int i = 0; i <= GM_KMAX; i++) {
                 if (i >= nv) break;
                 const double2 v = V[(long long)i * vstride + q];
                 w.x -= cf[i].x * v.x - cf[i].y * v.y;
@@ -349,18 +350,23 @@ struct wt3d_solver {
     std::unique_ptr<Engine<float>> e32;
     std::unique_ptr<Engine<double>> e64;
     cudaStream_t st = nullptr;
+    cudaStream_t sts = nullptr;           // substitution and refinement work, highest priority
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t evl = nullptr;            // marks the legacy default stream at entry to a device-buffer call
     bool have_model = false, have_values = false, have_factor = false;
     long long kernels_solve = 0;
     wt3d_stats stats{};
     ~wt3d_solver()
     {
         if (st) cudaStreamSynchronize(st);
+        if (sts) cudaStreamSynchronize(sts);
         e32.reset();
         e64.reset();
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (evl) cudaEventDestroy(evl);
         if (st) cudaStreamDestroy(st);
+        if (sts) cudaStreamDestroy(sts);
     }
 };
 
@@ -402,18 +408,31 @@ int have_gpu()
 // the current iterate, h->Rn = B - op(A) Xn and bnorm2/rnorm2 the squared
 // column norms of B and R; on exit Xn is the new iterate.  Classical
 // Gram-Schmidt applied twice; Givens rotations and the small least-squares
-// problems per column on the host.
+// problems per column on the host.  The restart length is 8 unless the
+// WT3D_GMRES_RESTART environment variable sets another (1..16); each Arnoldi
+// vector costs 2 blocks of n x 32 complex128 while the call runs.
+static int gmres_restart()
+{
+    static const int k = [] {
+        const char *e = getenv("WT3D_GMRES_RESTART");
+        const int v = e ? atoi(e) : 8;
+        return v < 1 ? 1 : (v > GM_KMAX ? GM_KMAX : v);
+    }();
+    return k;
+}
+
 template <class T>
 int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, double tol, int maxit,
            const std::vector<double> &bnorm2, std::vector<double> &rnorm2, double *relres, int &it)
 {
-    cudaStream_t st = h->st;
+    cudaStream_t st = h->sts;
     const long long n = h->n, blk = n * MAXRHS;
+    const int kr = gmres_restart();
     int rc;
     if (!h->gmV.p) {
-        if ((rc = h->gmV.alloc((size_t)blk * (GM_K + 1))) || (rc = h->gmZ.alloc((size_t)blk * GM_K)) ||
-            (rc = h->gmH.alloc((size_t)(GM_K + 1) * MAXRHS)) ||
-            (rc = h->gmPart.alloc((size_t)GM_BLOCKS * (GM_K + 1) * MAXRHS)) ||
+        if ((rc = h->gmV.alloc((size_t)blk * (kr + 1))) || (rc = h->gmZ.alloc((size_t)blk * kr)) ||
+            (rc = h->gmH.alloc((size_t)(GM_KMAX + 1) * MAXRHS)) ||
+            (rc = h->gmPart.alloc((size_t)GM_BLOCKS * (GM_KMAX + 1) * MAXRHS)) ||
             (rc = h->gmNorm.alloc(MAXRHS)) || (rc = h->gmScale.alloc(MAXRHS)))
             return rc;
     }
@@ -428,7 +447,7 @@ int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, d
     const unsigned nbm = (unsigned)ceil_div(n * m, th), nbb = (unsigned)ceil_div(blk, th);
     typedef std::complex<double> C;
     std::vector<double> sc_h(MAXRHS);
-    std::vector<double2> hb((GM_K + 1) * MAXRHS), hb2((GM_K + 1) * MAXRHS), coef((GM_K + 1) * MAXRHS);
+    std::vector<double2> hb((kr + 1) * MAXRHS), hb2((kr + 1) * MAXRHS), coef((kr + 1) * MAXRHS);
     std::vector<double> wn(MAXRHS);
     auto orth = [&](int nv, double2 *W, std::vector<double2> &out, bool norm) -> int {
         k_mdot<<<GM_BLOCKS, 256, 0, st>>>(n, m, nv, V, blk, W, h->gmPart.p);
@@ -455,12 +474,12 @@ int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, d
         WT_CUDA(cudaMemcpyAsync(V, h->Rn.p, sizeof(double2) * blk, cudaMemcpyDeviceToDevice, st));
         WT_CUDA(cudaMemcpyAsync(h->gmScale.p, sc_h.data(), sizeof(double) * MAXRHS, cudaMemcpyHostToDevice, st));
         k_colscale<<<nbb, th, 0, st>>>(n, h->gmScale.p, V);
-        std::vector<std::vector<C>> H(m, std::vector<C>((GM_K + 1) * GM_K, C(0)));
-        std::vector<std::vector<C>> g(m, std::vector<C>(GM_K + 1, C(0))), cs(m, std::vector<C>(GM_K)),
-            sn(m, std::vector<C>(GM_K));
+        std::vector<std::vector<C>> H(m, std::vector<C>((kr + 1) * kr, C(0)));
+        std::vector<std::vector<C>> g(m, std::vector<C>(kr + 1, C(0))), cs(m, std::vector<C>(kr)),
+            sn(m, std::vector<C>(kr));
         for (int c = 0; c < m; c++) g[c][0] = beta[c];
         int j = 0;
-        for (; j < GM_K; j++) {
+        for (; j < kr; j++) {
             bool all = true;
             for (int c = 0; c < m; c++) all = all && done[c];
             if (all || it >= maxit) break;
@@ -481,20 +500,20 @@ int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, d
                 if (done[c]) { sc_h[c] = 0.0; continue; }
                 std::vector<C> &Hc = H[c];
                 for (int i = 0; i <= j; i++)
-                    Hc[i * GM_K + j] = C(hb[i * MAXRHS + c].x + hb2[i * MAXRHS + c].x,
+                    Hc[i * kr + j] = C(hb[i * MAXRHS + c].x + hb2[i * MAXRHS + c].x,
                                          hb[i * MAXRHS + c].y + hb2[i * MAXRHS + c].y);
                 const double hn = sqrt(wn[c]);
                 // earlier rotations, then a new one zeroing H[j+1][j]
                 for (int i = 0; i < j; i++) {
-                    const C a = Hc[i * GM_K + j], b = Hc[(i + 1) * GM_K + j];
-                    Hc[i * GM_K + j] = std::conj(cs[c][i]) * a + std::conj(sn[c][i]) * b;
-                    Hc[(i + 1) * GM_K + j] = -sn[c][i] * a + cs[c][i] * b;
+                    const C a = Hc[i * kr + j], b = Hc[(i + 1) * kr + j];
+                    Hc[i * kr + j] = std::conj(cs[c][i]) * a + std::conj(sn[c][i]) * b;
+                    Hc[(i + 1) * kr + j] = -sn[c][i] * a + cs[c][i] * b;
                 }
-                const C a = Hc[j * GM_K + j];
+                const C a = Hc[j * kr + j];
                 const double den = sqrt(std::norm(a) + hn * hn);
                 cs[c][j] = den > 0 ? a / den : C(1);
                 sn[c][j] = den > 0 ? C(hn / den) : C(0);
-                Hc[j * GM_K + j] = den;
+                Hc[j * kr + j] = den;
                 g[c][j + 1] = -sn[c][j] * g[c][j];
                 g[c][j] = std::conj(cs[c][j]) * g[c][j];
                 len[c] = j + 1;
@@ -516,8 +535,8 @@ int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, d
                 std::vector<C> y(L);
                 for (int i = L - 1; i >= 0; i--) {
                     C t = g[c][i];
-                    for (int q = i + 1; q < L; q++) t -= H[c][i * GM_K + q] * y[q];
-                    y[i] = t / H[c][i * GM_K + i];
+                    for (int q = i + 1; q < L; q++) t -= H[c][i * kr + q] * y[q];
+                    y[i] = t / H[c][i * kr + i];
                 }
                 for (int i = 0; i < L; i++) coef[i * MAXRHS + c] = make_double2(-y[i].real(), -y[i].imag());
             }
@@ -553,7 +572,7 @@ int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, d
 template <class T>
 int refine(wt3d_solver *h, Engine<T> &E, int m, bool adjoint, double tol, int maxit, double *relres, int *iters)
 {
-    cudaStream_t st = h->st;
+    cudaStream_t st = h->sts;
     const long long n = h->n;
     Schedule<T> *sc = E.solve_schedule(m, adjoint);
     if (!sc) return WT3D_ERR_NOMEM;
@@ -600,17 +619,31 @@ int refine(wt3d_solver *h, Engine<T> &E, int m, bool adjoint, double tol, int ma
     return rc;
 }
 
+// Entry points that take caller device buffers run on the handle's own
+// non-blocking streams.  Callers (PyTorch among them) commonly fill or consume
+// those buffers on the legacy default stream without synchronising, so each
+// such entry point first makes its stream wait for everything already queued
+// there.  Work the caller queued on other streams must be complete before the
+// call.  Every entry point synchronises its stream before it returns.
+static int after_legacy(wt3d_solver *h, cudaStream_t s)
+{
+    WT_CUDA(cudaEventRecord(h->evl, cudaStreamLegacy));
+    WT_CUDA(cudaStreamWaitEvent(s, h->evl, 0));
+    return WT3D_OK;
+}
+
 int solve_dev_cm(wt3d_solver *h, int nrhs, const double2 *d_B, double2 *d_X, double tol, int maxit, double *relres,
                  int *iters, bool adjoint)
 {
     if (!h->have_factor) { set_error("solve before factor"); return WT3D_ERR_STATE; }
+    if (int rc = after_legacy(h, h->sts)) return rc;
     const long long n = h->n;
     int worst_rc = WT3D_OK, maxits = 0;
     h->kernels_solve = 0;
-    cudaEventRecord(h->ev0, h->st);
+    cudaEventRecord(h->ev0, h->sts);
     for (int c0 = 0; c0 < nrhs; c0 += MAXRHS) {
         int m = std::min(MAXRHS, nrhs - c0);
-        k_cm_to_rm<<<ceil_div(n, 256), 256, 0, h->st>>>(n, m, d_B + (long long)c0 * n, h->Bn.p);
+        k_cm_to_rm<<<ceil_div(n, 256), 256, 0, h->sts>>>(n, m, d_B + (long long)c0 * n, h->Bn.p);
         h->kernels_solve += 2;   // layout conversions in and out
         int its = 0, rc;
         if (h->e32) rc = refine<float>(h, *h->e32, m, adjoint, tol, maxit, relres ? relres + c0 : nullptr, &its);
@@ -618,10 +651,10 @@ int solve_dev_cm(wt3d_solver *h, int nrhs, const double2 *d_B, double2 *d_X, dou
         if (rc && rc != WT3D_ERR_NOCONV) return rc;
         if (rc) worst_rc = rc;
         maxits = std::max(maxits, its);
-        k_rm_to_cm<<<ceil_div(n, 256), 256, 0, h->st>>>(n, m, h->Xn.p, d_X + (long long)c0 * n);
+        k_rm_to_cm<<<ceil_div(n, 256), 256, 0, h->sts>>>(n, m, h->Xn.p, d_X + (long long)c0 * n);
     }
-    cudaEventRecord(h->ev1, h->st);
-    WT_CUDA(cudaStreamSynchronize(h->st));
+    cudaEventRecord(h->ev1, h->sts);
+    WT_CUDA(cudaStreamSynchronize(h->sts));
     h->stats.t_solve_ms = ms_between(h->ev0, h->ev1);
     h->stats.kernels_solve = (int)h->kernels_solve;
     if (iters) *iters = maxits;
@@ -772,8 +805,16 @@ int wt3d_solver_create(wt3d_solver **out, const wt3d_grid *g, int precision)
     h->n = sym.n;
     h->nnz = wt3d_pattern_nnz(g->nx, g->ny, g->nz);
     WT_CUDA(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    {
+        // solves run ahead of other handles' factorisations: their kernels are
+        // short and latency-bound, a factorisation's are long
+        int least = 0, greatest = 0;
+        WT_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        WT_CUDA(cudaStreamCreateWithPriority(&h->sts, cudaStreamNonBlocking, greatest));
+    }
     WT_CUDA(cudaEventCreate(&h->ev0));
     WT_CUDA(cudaEventCreate(&h->ev1));
+    WT_CUDA(cudaEventCreateWithFlags(&h->evl, cudaEventDisableTiming));
     if ((rc = h->irptr.alloc(h->n + 1)) || (rc = h->jcptr.alloc(h->nnz)) || (rc = h->a.alloc(h->nnz))) return rc;
     if ((rc = device_pattern(g->nx, g->ny, g->nz, 0, h->irptr.p, h->jcptr.p, h->st))) return rc;
     std::shared_ptr<FactorWorkspace<float>> w32;
@@ -952,6 +993,7 @@ int wt3d_rhs_planewave(wt3d_solver *h, const wt3d_layered1d *m, int nsrc, const 
                        const int *s_wave, void *d_F, void *d_U0)
 {
     if (!h || !m || nsrc < 1 || !ain || !baz || !d_F) { set_error("wt3d_rhs_planewave: bad arguments"); return WT3D_ERR_ARG; }
+    if (int rc0 = after_legacy(h, h->st)) return rc0;
     if (!h->have_values || !h->have_bg) { set_error("wt3d_rhs_planewave: needs a factored operator and a background"); return WT3D_ERR_STATE; }
     const int nx = h->grid.nx, ny = h->grid.ny, nz = h->grid.nz;
     const long long n = h->n;
@@ -1033,7 +1075,7 @@ static int solve_host(wt3d_solver *h, int nrhs, const double _Complex *B, double
     DevVec<double2> dB, dX;
     int rc;
     if ((rc = dB.alloc((size_t)h->n * nrhs)) || (rc = dX.alloc((size_t)h->n * nrhs))) return rc;
-    WT_CUDA(cudaMemcpyAsync(dB.p, B, sizeof(double2) * h->n * nrhs, cudaMemcpyHostToDevice, h->st));
+    WT_CUDA(cudaMemcpyAsync(dB.p, B, sizeof(double2) * h->n * nrhs, cudaMemcpyHostToDevice, h->sts));
     rc = solve_dev_cm(h, nrhs, dB.p, dX.p, tol, maxit, relres, iters, adjoint);
     if (rc && rc != WT3D_ERR_NOCONV) return rc;
     WT_CUDA(cudaMemcpy(X, dX.p, sizeof(double2) * h->n * nrhs, cudaMemcpyDeviceToHost));
@@ -1082,6 +1124,7 @@ int wt3d_apply(wt3d_solver *h, int nrhs, const double _Complex *X, double _Compl
 int wt3d_apply_device(wt3d_solver *h, int nrhs, const void *d_X, void *d_Y)
 {
     if (!h || nrhs < 1 || !d_X || !d_Y) { set_error("wt3d_apply_device: bad arguments"); return WT3D_ERR_ARG; }
+    if (int rc0 = after_legacy(h, h->st)) return rc0;
     if (!h->have_values) { set_error("no operator"); return WT3D_ERR_STATE; }
     const long long n = h->n;
     for (int c0 = 0; c0 < nrhs; c0 += MAXRHS) {
@@ -1116,6 +1159,7 @@ int wt3d_update_operator(wt3d_solver *h)
 int wt3d_gradient_contract(wt3d_solver *h, int nrhs, const void *d_U, const void *d_Lam, void *d_grad)
 {
     if (!h || nrhs < 1 || !d_U || !d_Lam || !d_grad) { set_error("wt3d_gradient_contract: bad arguments"); return WT3D_ERR_ARG; }
+    if (int rc0 = after_legacy(h, h->st)) return rc0;
     if (!h->have_model || !h->have_values) { set_error("wt3d_gradient_contract: needs a model and an assembled operator"); return WT3D_ERR_STATE; }
     if (h->qp.p) { set_error("wt3d_gradient_contract: the gradient is built for elastic models (no attenuation)"); return WT3D_ERR_STATE; }
     const long long nn = h->n / 3;
@@ -1140,6 +1184,7 @@ int wt3d_misfit_gradient(wt3d_solver *h, int nsrc, const void *d_F, const void *
         return WT3D_ERR_ARG;
     }
     if (!h->have_factor || !h->have_model) { set_error("wt3d_misfit_gradient: needs a model and a factor"); return WT3D_ERR_STATE; }
+    if (int rc0 = after_legacy(h, h->st)) return rc0;
     const long long n = h->n, nn = n / 3;
     for (int r = 0; r < nrec; r++)
         if (rec_node[r] < 0 || rec_node[r] >= nn) { set_error("wt3d_misfit_gradient: receiver node out of range"); return WT3D_ERR_ARG; }
@@ -1192,6 +1237,7 @@ int wt3d_batch_buffers(wt3d_solver *h, int ncols, void **d_F, void **d_X)
 int wt3d_memcpy(wt3d_solver *h, void *dst, const void *src, long long bytes)
 {
     if (!h || !dst || !src || bytes < 0) { set_error("wt3d_memcpy: bad arguments"); return WT3D_ERR_ARG; }
+    if (int rc0 = after_legacy(h, h->st)) return rc0;
     WT_CUDA(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDefault, h->st));
     WT_CUDA(cudaStreamSynchronize(h->st));
     return WT3D_OK;
@@ -1201,6 +1247,7 @@ int wt3d_rhs_sources(wt3d_solver *h, int nsrc, const double *xyz, const int *com
                      int ireg, double sprd, void *d_F)
 {
     if (!h || nsrc < 1 || !xyz || !comp || !d_F) { set_error("wt3d_rhs_sources: bad arguments"); return WT3D_ERR_ARG; }
+    if (int rc0 = after_legacy(h, h->st)) return rc0;
     const long long n = h->n;
     std::vector<int> col, cmp;
     std::vector<long long> nd;
@@ -1240,6 +1287,7 @@ int wt3d_sample_receivers(wt3d_solver *h, int nrhs, const void *d_U, int nrec, c
                           double sprd, double _Complex *out)
 {
     if (!h || nrhs < 1 || !d_U || nrec < 1 || !xyz || !out) { set_error("wt3d_sample_receivers: bad arguments"); return WT3D_ERR_ARG; }
+    if (int rc0 = after_legacy(h, h->st)) return rc0;
     std::vector<int> start(1, 0);
     std::vector<long long> nd;
     std::vector<double> w;
