@@ -340,13 +340,17 @@ int wt3d_profile_launches(wt3d_solver *h, int which, int m, double *out, int cap
 int wt3d_debug_fetch(wt3d_solver *h, int what, void *out, long long count);
 
 /* One complex64 GEMM C -= A B on host row-major arrays through the tensor-core
- * kernel (path 1) or the SIMT kernel (path 0); for checks of the kernels. */
+ * kernel (path 1), the SIMT kernel (path 0) or the tall-skinny tensor-core
+ * kernel of the substitution passes (path 3, N <= 32; path 4 also gathers B
+ * rows K-1-k and scatters C rows M-1-r); for checks of the kernels. */
 int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int lda, const void *B, int ldb, void *C,
                     int ldc);
 
 /* Device-resident timing of the GEMM kernels: average ms of `iters`
  * launches of C -= A B (M x K by K x N complex64, device-filled operands);
- * path 1 = tensor-core kernel (operand split excluded), 0 = SIMT kernel. */
+ * path 1 = tensor-core kernel (operand split excluded), 0 = SIMT kernel,
+ * 2 = tall-skinny SIMT kernel, 3 = tall-skinny tensor-core kernel (B
+ * expansion excluded); paths 2 and 3 need N <= 32. */
 int wt3d_bench_gemm(int path, int M, int N, int K, int iters, double *ms_out);
 
 /* ---- allocation-free entry point ----------------------------------------

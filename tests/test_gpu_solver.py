@@ -216,3 +216,42 @@ def test_degenerate_grids_and_zero_columns():
             Y = s.apply(X)
             for j in (0, 2):
                 assert np.linalg.norm(Y[:, j] - B[:, j]) <= 2e-8 * np.linalg.norm(B[:, j])
+
+
+def test_tensor_core_substitution_matches_simt():
+    """40^3 (the configuration-1 grid), complex64 factors: the substitution
+    passes with their large blocks on the tall-skinny tensor-core kernel
+    (WT3D_TS unset) and on the SIMT kernel (WT3D_TS=0) reach the same refined
+    solution in the same number of passes, and the tensor-core launches are in
+    the schedule."""
+    import ctypes
+    import os
+    g = Grid(40, 40, 40, 25.0, pmld=10 * 25.0, fst=0)
+    rng = np.random.default_rng(3)
+    # point forces inside the PML-free core, random positions and components
+    pos = rng.uniform(11 * 25.0, 28 * 25.0, size=(8, 3))
+    B = np.stack([model.point_force(40, 40, 40, 25.0, *pos[j], comp=j % 3) for j in range(8)], axis=1)
+    out = {}
+    for ts in ("1", "0"):
+        os.environ["WT3D_TS"] = ts
+        try:
+            with wt.Solver(g) as s:
+                s.set_model(*model.homogeneous(40, 40, 40))
+                s.factor(2 * np.pi)
+                X = s.solve(B, tol=1e-10, maxit=20)
+                L = wt.lib()
+                L.wt3d_profile_launches.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                    ctypes.c_int, ctypes.c_void_p]
+                cap = 200000
+                rec = np.zeros(4 * cap)
+                cnt = ctypes.c_int(0)
+                assert L.wt3d_profile_launches(s._h, 1, 8, ctypes.c_void_p(rec.ctypes.data), cap,
+                                               ctypes.byref(cnt)) == 0
+                kinds = rec[:4 * min(cnt.value, cap)].reshape(-1, 4)[:, 0]
+                out[ts] = (X, s.last_iters, int(np.sum(kinds == 8)))
+        finally:
+            os.environ.pop("WT3D_TS", None)
+    (X1, it1, n1), (X0, it0, n0) = out["1"], out["0"]
+    assert n1 > 0 and n0 == 0, (n1, n0)
+    assert it1 <= it0 + 1, (it1, it0)
+    assert np.linalg.norm(X1 - X0) <= 1e-6 * np.linalg.norm(X0)

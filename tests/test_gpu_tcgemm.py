@@ -54,3 +54,45 @@ def test_gemm_strided_views():
     out = gemm(1, A, B, C)
     scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64) + np.abs(C)
     assert (np.abs(out - ref) / scale).max() < 2e-6
+
+
+def gemm_ld(path, A, lda, B, C):
+    """C -= A B with A passed as the first A.shape[1] columns of rows lda apart."""
+    L = wt.lib()
+    L.wt3d_debug_gemm.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                       ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    M, K = A.shape
+    N = B.shape[1]
+    Abuf = np.zeros((M, lda), np.complex64)
+    Abuf[:, :K] = A
+    Abuf[:, K:] = np.nan     # never read
+    B = np.ascontiguousarray(B, np.complex64)
+    C = np.ascontiguousarray(C, np.complex64).copy()
+    p = lambda a: ctypes.c_void_p(a.ctypes.data)
+    rc = L.wt3d_debug_gemm(path, M, N, K, p(Abuf), lda, p(B), B.shape[1], p(C), C.shape[1])
+    assert rc == 0, L.wt3d_last_error()
+    return C
+
+
+@pytest.mark.parametrize("shape", [(128, 32, 256), (130, 32, 300), (1000, 17, 777), (300, 1, 4099),
+                                   (2048, 32, 5000)])
+@pytest.mark.parametrize("path", [3, 4])
+def test_tall_skinny_tensor_core_gemm(shape, path):
+    """The substitution passes' tensor-core kernel (A read and split on the fly,
+    odd leading dimension so rows start off 16-byte boundaries, ragged M and K,
+    fewer than 32 columns, K split across CTAs); path 4 gathers B rows K-1-k and
+    scatters C rows M-1-r."""
+    M, N, K = shape
+    r = np.random.default_rng(M + 5 * N + 11 * K + path)
+    A = (r.standard_normal((M, K)) + 1j * r.standard_normal((M, K))).astype(np.complex64)
+    B = (r.standard_normal((K, N)) + 1j * r.standard_normal((K, N))).astype(np.complex64)
+    C = (r.standard_normal((M, N)) + 1j * r.standard_normal((M, N))).astype(np.complex64)
+    Bq = B[::-1] if path == 4 else B
+    prod = A.astype(np.complex128) @ Bq.astype(np.complex128)
+    scale = np.abs(A).astype(np.float64) @ np.abs(Bq).astype(np.float64)
+    if path == 4:
+        prod, scale = prod[::-1], scale[::-1]
+    ref = C.astype(np.complex128) - prod
+    out = gemm_ld(path, A, K + 3 if K % 2 == 0 else K, B, C)
+    err = (np.abs(out - ref) / (scale + np.abs(C))).max()
+    assert err < 1e-6 + 3e-7 * np.sqrt(K), err

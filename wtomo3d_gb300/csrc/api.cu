@@ -655,6 +655,7 @@ int solve_dev_cm(wt3d_solver *h, int nrhs, const double2 *d_B, double2 *d_X, dou
     }
     cudaEventRecord(h->ev1, h->sts);
     WT_CUDA(cudaStreamSynchronize(h->sts));
+    if (int rc = h->e32 ? h->e32->check_tc_err() : h->e64->check_tc_err()) return rc;
     h->stats.t_solve_ms = ms_between(h->ev0, h->ev1);
     h->stats.kernels_solve = (int)h->kernels_solve;
     if (iters) *iters = maxits;
@@ -908,6 +909,7 @@ static int factor_values(wt3d_solver *h)
         cudaEventRecord(h->ev1, h->st);
         WT_CUDA(cudaStreamSynchronize(h->st));
     }
+    if ((rc = h->e32 ? h->e32->check_tc_err() : h->e64->check_tc_err())) return rc;
     h->stats.t_factor_ms = ms_between(h->ev0, h->ev1);
     h->stats.perturbed_pivots = np;
     h->stats.kernels_factor = 2 + (h->e32 ? h->e32->fsched->kernels() : h->e64->fsched->kernels());

@@ -44,6 +44,9 @@ struct Schedule {
     DevVec<EATask> ea;
     std::vector<std::vector<GemmTask<float>>> tc_pending;   // tensor-core task lists, built after allocation
     std::vector<std::unique_ptr<TcLaunch>> tc;
+    std::vector<std::vector<GemmTask<float>>> ts_pending;   // tall-skinny tensor-core task lists (solves)
+    std::vector<std::unique_ptr<TsLaunch>> ts;
+    DevVec<float> tsws;                                       // their expanded right-hand sides
     cudaGraphExec_t graph = nullptr;
     ~Schedule()
     {
@@ -80,6 +83,9 @@ public:
     double pivot_rel = 1e-20;
     // tcgen05 path for complex64 front updates (WT3D_TC=0 selects the SIMT kernel)
     bool use_tc = std::is_same<T, float>::value && !(getenv("WT3D_TC") && getenv("WT3D_TC")[0] == '0');
+    // tcgen05 path for the large blocks of complex64 substitution passes (WT3D_TS=0: SIMT)
+    bool use_ts = std::is_same<T, float>::value && !(getenv("WT3D_TS") && getenv("WT3D_TS")[0] == '0');
+    bool building_solve = false;   // set while a solve schedule is built: only those route to the TS kernel
     DevVec<float> own_tcws;   // private split workspace, only if the shared one is too small
     DevVec<int> tc_err;                                 // barrier-timeout flag of the tensor-core kernel
     std::vector<Schedule<T> *> built_tc;   // only (near-)zero pivots are replaced: Dirichlet rows carry unit pivots next to O(1e8) stiffness entries
@@ -89,8 +95,23 @@ public:
     // device bytes this engine holds on its own (the shared workspace excluded)
     size_t device_bytes() const
     {
+        size_t sw = 0;   // the solve schedules' tall-skinny workspaces
+        for (const auto &m : ssched)
+            for (const auto &kv : m) sw += kv.second->tsws.n * sizeof(float);
         return (fac.n + X.n + dinv.n) * sizeof(cx<T>) + (ipiv.n + border.n + rel.n) * 4 + fr.n * sizeof(FrontDev) +
-               map.n * 8 + scale.n * 8 + own_tcws.n * sizeof(float);
+               map.n * 8 + scale.n * 8 + own_tcws.n * sizeof(float) + sw;
+    }
+
+    // Reads (and clears) the barrier-timeout flag of the tensor-core kernels;
+    // call after the stream that ran them is synchronised.
+    int check_tc_err()
+    {
+        int e = 0;
+        WT_CUDA(cudaMemcpy(&e, tc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (!e) return WT3D_OK;
+        WT_CUDA(cudaMemset(tc_err.p, 0, sizeof(int)));
+        set_error("tensor-core kernel: mbarrier wait expired (code " + std::to_string(e) + ")");
+        return WT3D_ERR_CUDA;
     }
     size_t workspace_bytes() const { return ws ? ws->bytes() : 0; }
     // split workspace of the tensor-core launches: private if allocated, else the shared one
@@ -126,6 +147,7 @@ public:
         if ((rc = tc_err.alloc(1))) return rc;
         WT_CUDA(cudaMemset(tc_err.p, 0, sizeof(int)));
         if (use_tc && (rc = tc_init())) return rc;
+        if (use_ts && (rc = ts_init())) return rc;
         std::vector<FrontDev> h(sym.fronts.size());
         long long npan = 0;
         for (size_t f = 0; f < h.size(); f++) {
@@ -203,6 +225,21 @@ public:
                 sc.launches.push_back({[psc, idx, this](cudaStream_t st) { tc_mma(*psc->tc[idx], tc_err.p, st); },
                                        LK_TCGEMM, fl, by});
             }
+            if (use_ts && building_solve) {
+                std::vector<GemmTask<float>> tsv, rest;
+                for (auto &g : simt) (ts_eligible(g) ? tsv : rest).push_back(g);
+                if (!tsv.empty()) {
+                    double fl = 0, by = 0;
+                    for (auto &g : tsv) { fl += 8.0 * g.M * (double)g.N * g.K; by += gemm_bytes(g); }
+                    const int idx = (int)sc.ts_pending.size();
+                    sc.ts_pending.push_back(std::move(tsv));
+                    Schedule<T> *psc = &sc;
+                    sc.launches.push_back({[psc, idx](cudaStream_t st) { ts_expand(*psc->ts[idx], st); }, LK_SPLIT, 0});
+                    sc.launches.push_back({[psc, idx, this](cudaStream_t st) { ts_mma(*psc->ts[idx], tc_err.p, st); },
+                                           LK_TCGEMM, fl, by});
+                }
+                simt.swap(rest);
+            }
         } else {
             simt.assign(all.begin() + b, all.end());
         }
@@ -264,6 +301,26 @@ public:
                 k_gemm<T><<<(unsigned)tiles, 256, 0, st>>>(psc->gemm.p + b0, nt);
             }, LK_GEMM, fl, by});
         }
+    }
+
+    // Allocates a solve schedule's own B~ workspace (sized for its largest
+    // tall-skinny launch; launches run one after another) and builds the
+    // tensor maps of its tall-skinny tensor-core launches.
+    int finish_ts(Schedule<T> &sc)
+    {
+        if constexpr (std::is_same<T, float>::value) {
+            long long need = 0;
+            for (auto &v : sc.ts_pending) need = std::max(need, ts_workspace_floats(v.data(), (int)v.size()));
+            if (need == 0) return WT3D_OK;
+            int rc;
+            if ((rc = sc.tsws.alloc(need))) return rc;
+            sc.ts.clear();
+            for (auto &v : sc.ts_pending) {
+                sc.ts.emplace_back(new TsLaunch());
+                if ((rc = ts_build_launch(*sc.ts.back(), v.data(), (int)v.size(), sc.tsws.p))) return rc;
+            }
+        }
+        return WT3D_OK;
     }
 
     // Allocates the shared tensor-core workspace and builds the tensor maps of
@@ -470,6 +527,11 @@ public:
         const Symbolic &sym = *S;
         cx<T> *F = fac.p;
         cx<T> *Xp = X.p;
+        struct Flag {
+            bool &f;
+            Flag(bool &x) : f(x) { f = true; }
+            ~Flag() { f = false; }
+        } building(building_solve);
         const int ldx = MAXRHS;
         const int nlev = (int)sym.levels.size();
         size_t smd = sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1));
@@ -575,7 +637,7 @@ public:
                 }
             }
         }
-        if (sc->panel.upload(hp) || sc->gemm.upload(hg) || finish_tc(*sc)) return nullptr;
+        if (sc->panel.upload(hp) || sc->gemm.upload(hg) || finish_tc(*sc) || finish_ts(*sc)) return nullptr;
         Schedule<T> *ret = sc.get();
         ssched[adjoint][m] = std::move(sc);
         return ret;

@@ -27,6 +27,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include "tc_gemm.h"
+#include "tc_ptx.cuh"
 #include <atomic>
 #include <cstring>
 
@@ -42,114 +43,11 @@ constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;
 constexpr int TC_EPI_BYTES = 4 * 32 * 33 * 4;        // per epilogue warp a 32 x 33 float transpose buffer
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256 + TC_EPI_BYTES;
 constexpr int TC_THREADS = 192;
-constexpr unsigned TC_WAIT_LIMIT = 1u << 24;
 constexpr int TC_GROUP = 8;                 // column panels per rasterisation group
-
-// ---------------------------------------------------------------------------
-// PTX helpers
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-// Bounded wait for the phase with the given parity; returns false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
-{
-    const uint32_t a = smem_u32(bar);
-    for (unsigned it = 0; it < TC_WAIT_LIMIT; it++) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            smem_u32(dst)),
-        "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
-        : "memory");
-}
-
-// K-major operand tile in the 128-byte-swizzle canonical layout: 8-row atoms
-// of 128-byte rows, atoms 1024 bytes apart along M/N.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
-{
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);        // start address
-    d |= (uint64_t)1 << 16;                           // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;                 // stride byte offset between 8-row atoms
-    d |= (uint64_t)1 << 46;                           // descriptor version (sm_100 family)
-    d |= (uint64_t)2 << 61;                           // swizzle: 128B
-    return d;
-}
-
-// kind::tf32 instruction descriptor: FP32 accumulate, TF32 A and B, both
-// K-major, M = 128, N = 256.
-__host__ __device__ constexpr uint32_t tf32_idesc(int M, int N)
-{
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc)
-{
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-        "l"(da), "l"(db), "r"(idesc), "r"(acc));
-}
-
-__device__ __forceinline__ void umma_commit(uint64_t *bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-
-#define TMEM_LD32(taddr, v)                                                                                       \
-    asm volatile(                                                                                                 \
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18," \
-        "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"                                            \
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),          \
-          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),   \
-          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), \
-          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])  \
-        : "r"(taddr))
 
 // ---------------------------------------------------------------------------
 // operand split / expansion pre-pass
 // ---------------------------------------------------------------------------
-// Round to the nearest TF32 value (10 explicit mantissa bits), ties to even.
-__device__ __forceinline__ float rn_tf32(float x)
-{
-    uint32_t u = __float_as_uint(x);
-    if ((u & 0x7F800000u) == 0x7F800000u) return x;          // inf / nan unchanged
-    u += 0xFFFu + ((u >> 13) & 1u);
-    return __uint_as_float(u & 0xFFFFE000u);
-}
-
-// x = hi + lo + O(2^-24 |x|) with hi and lo both exact TF32 values, so the
-// tensor core's reading of the operands loses nothing.
-__device__ __forceinline__ void split_tf32(float x, float &hi, float &lo)
-{
-    hi = rn_tf32(x);
-    lo = rn_tf32(x - hi);
-}
-
 // One thread per (row, complex k) of A: Ahi/Alo rows of Kr floats.
 __global__ void k_split_a(const TcTask *__restrict__ tasks, int ntasks, long long total)
 {
@@ -221,11 +119,6 @@ __global__ void __launch_bounds__(256) k_split_b(const TcTask *__restrict__ task
 // ---------------------------------------------------------------------------
 // the tensor-core kernel
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
 // Tile gt of a launch: its task and the tile's first complex row and real column.
 // Grouped rasterisation: consecutive tiles sweep a band of TC_GROUP column
 // panels row panel by row panel, so the tiles in flight share a compact set of
@@ -424,41 +317,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
-{
-    // thread-safe one-time lookup (function-local static initialisation)
-    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            return (PFN_cuTensorMapEncodeTiled_v12000)p;
-        return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
-    }();
-    return fn;
-}
-
-static int make_map(CUtensorMap *m, float *base, long long rows, int Kr, int box_rows)
-{
-    auto fn = encode_fn();
-    if (!fn) { set_error("cuTensorMapEncodeTiled unavailable"); return WT3D_ERR_CUDA; }
-    cuuint64_t gdim[2] = {(cuuint64_t)Kr, (cuuint64_t)rows};
-    cuuint64_t gstr[1] = {(cuuint64_t)Kr * 4};
-    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
-    cuuint32_t es[2] = {1, 1};
-    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, gdim, gstr, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) {
-        set_error("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
-        return WT3D_ERR_CUDA;
-    }
-    return WT3D_OK;
-}
-
-static long long align_up(long long x, long long a) { return (x + a - 1) / a * a; }
-
 long long tc_workspace_floats(const GemmTask<float> *g, int n)
 {
     long long w = 0;
@@ -563,8 +421,10 @@ int tc_init()
 
 // ---------------------------------------------------------------------------
 // C ABI check entry: one GEMM C -= A B on host complex64 arrays (row-major),
-// through the tensor-core path (path = 1) or the SIMT path (path = 0).
-// wt3d_bench_gemm also times path 2, the tall-skinny kernel of the solves.
+// through the tensor-core path (path = 1), the SIMT path (path = 0) or the
+// tall-skinny tensor-core kernel of the solves (path = 3; path = 4 with a row
+// gather of B and a row scatter of C).  wt3d_bench_gemm also times path 2,
+// the tall-skinny SIMT kernel, and path 3.
 // ---------------------------------------------------------------------------
 using namespace wt3d;
 extern "C" int wt3d_set_sm_reserve(int n)
@@ -591,6 +451,7 @@ extern "C" int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int
     DevVec<int> err;
     if ((rc = err.alloc(1))) return rc;
     WT_CUDA(cudaMemset(err.p, 0, sizeof(int)));
+    DevVec<int> drow, dcol;
     if (path == 1) {
         if ((rc = tc_init())) return rc;
         DevVec<float> ws;
@@ -599,6 +460,25 @@ extern "C" int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int
         if ((rc = tc_build_launch(L, &g, 1, ws.p))) return rc;
         tc_split(L, 0);
         tc_mma(L, err.p, 0);
+    } else if (path == 3 || path == 4) {
+        // tall-skinny tensor-core kernel; path 4 gathers B rows K-1-k and
+        // scatters C rows M-1-r (atomic epilogue)
+        if (N > 32) { set_error("wt3d_debug_gemm: paths 3 and 4 need N <= 32"); return WT3D_ERR_ARG; }
+        if (path == 4) {
+            std::vector<int> br(K), cr(M);
+            for (int k = 0; k < K; k++) br[k] = K - 1 - k;
+            for (int r = 0; r < M; r++) cr[r] = M - 1 - r;
+            if ((rc = drow.upload(br)) || (rc = dcol.upload(cr))) return rc;
+            g.brow = drow.p;
+            g.crow = dcol.p;
+        }
+        if ((rc = ts_init())) return rc;
+        DevVec<float> ws;
+        if ((rc = ws.alloc(ts_workspace_floats(&g, 1)))) return rc;
+        TsLaunch L;
+        if ((rc = ts_build_launch(L, &g, 1, ws.p))) return rc;
+        ts_expand(L, 0);
+        ts_mma(L, err.p, 0);
     } else {
         DevVec<GemmTask<float>> dt;
         std::vector<GemmTask<float>> v{g};
@@ -642,11 +522,17 @@ extern "C" int wt3d_bench_gemm(int path, int M, int N, int K, int iters, double 
     WT_CUDA(cudaMemset(err.p, 0, sizeof(int)));
     DevVec<float> ws;
     TcLaunch L;
+    TsLaunch LT;
     DevVec<GemmTask<float>> dt;
     if (path == 1) {
         if ((rc = tc_init()) || (rc = ws.alloc(tc_workspace_floats(&g, 1))) || (rc = tc_build_launch(L, &g, 1, ws.p)))
             return rc;
         tc_split(L, 0);
+    } else if (path == 3) {
+        if (N > 32) { set_error("wt3d_bench_gemm: path 3 needs N <= 32"); return WT3D_ERR_ARG; }
+        if ((rc = ts_init()) || (rc = ws.alloc(ts_workspace_floats(&g, 1))) || (rc = ts_build_launch(LT, &g, 1, ws.p)))
+            return rc;
+        ts_expand(LT, 0);
     } else {
         std::vector<GemmTask<float>> v{g};
         if ((rc = dt.upload(v))) return rc;
@@ -659,6 +545,7 @@ extern "C" int wt3d_bench_gemm(int path, int M, int N, int K, int iters, double 
     if (path == 2 && N > TSBN) { set_error("wt3d_bench_gemm: path 2 needs N <= 32"); return WT3D_ERR_ARG; }
     auto launch = [&]() {
         if (path == 1) tc_mma(L, err.p, 0);
+        else if (path == 3) ts_mma(LT, err.p, 0);
         else if (path == 2) k_gemm_ts<float><<<(unsigned)ts_tiles, 256>>>(dt.p, 1);
         else k_gemm<float><<<(unsigned)tiles, 256>>>(dt.p, 1);
     };

@@ -24,7 +24,33 @@ struct TcLaunch {
     long long tiles = 0, a_work = 0, b_tiles = 0;
 };
 
+// One GEMM of a tall-skinny tensor-core launch (substitution passes: N <= 32).
+struct TsTask {
+    const cx<float> *A;
+    const cx<float> *B;
+    cx<float> *C;
+    const int *brow, *crow;         // optional row gather of B, row scatter of C
+    float *bhi, *blo;               // expanded, split B~ (64 x Kr) in the launch workspace
+    int lda, ldb, ldc, M, N, K, Kr;
+    int kchunk, nkc, atom;          // K-chunk per work unit, chunks, atomic epilogue
+    int map0;                       // first of this task's 2 tensor maps
+    long long unit0, b_work0;
+};
+
+struct TsLaunch {
+    DevVec<TsTask> tasks;
+    DevVec<unsigned char> maps;    // CUtensorMap array (2 per task)
+    int ntasks = 0;
+    long long units = 0, b_tiles = 0;
+};
+
 int tc_init();
+int ts_init();
+bool ts_eligible(const GemmTask<float> &g);
+long long ts_workspace_floats(const GemmTask<float> *g, int n);
+int ts_build_launch(TsLaunch &L, const GemmTask<float> *g, int n, float *ws);
+void ts_expand(const TsLaunch &L, cudaStream_t st);
+void ts_mma(const TsLaunch &L, int *err, cudaStream_t st);
 bool tc_eligible(const GemmTask<float> &g);
 long long tc_workspace_floats(const GemmTask<float> *g, int n);
 int tc_build_launch(TcLaunch &L, const GemmTask<float> *g, int n, float *ws);

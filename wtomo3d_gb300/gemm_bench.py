@@ -1,12 +1,13 @@
 """Microbenchmark of the front-update GEMM C -= A B (complex64, row-major)
 through the tcgen05 kernel (path 1), the SIMT kernel (path 0) or the
-tall-skinny SIMT kernel of the solves (path 2, N <= 32), on random operands
+tall-skinny SIMT kernel of the solves (path 2, N <= 32) or the tall-skinny
+tcgen05 kernel of the solves (path 3, N <= 32), on random operands
 resident on the device:
 
     python -m wtomo3d_gb300.gemm_bench M N K [--path 1] [--reps 5]
 
-Prints one JSON line with the mean launch time and the real-flop rate
-8 M N K / t.  The tensor-core timing excludes the operand split, which the
+Prints one JSON line with the mean launch time, the real-flop rate 8 M N K / t
+and the rate at which A (8 M K bytes) is read.  The tensor-core timing excludes the operand split, which the
 factorisation runs as a separate kernel.
 """
 import argparse
@@ -23,7 +24,7 @@ def main():
     ap.add_argument("M", type=int)
     ap.add_argument("N", type=int)
     ap.add_argument("K", type=int)
-    ap.add_argument("--path", type=int, default=1, choices=[0, 1, 2])
+    ap.add_argument("--path", type=int, default=1, choices=[0, 1, 2, 3])
     ap.add_argument("--reps", type=int, default=5)
     a = ap.parse_args()
     import wtomo3d_gb300 as wt
@@ -34,8 +35,8 @@ def main():
     if rc:
         raise SystemExit("wt3d_bench_gemm failed (%d): %s" % (rc, L.wt3d_last_error().decode()))
     fl = 8.0 * a.M * a.N * a.K
-    print(json.dumps({"M": a.M, "N": a.N, "K": a.K, "path": ["simt", "tcgen05", "simt-tall-skinny"][a.path], "ms": ms.value,
-                      "tflops": fl / ms.value / 1e9}))
+    print(json.dumps({"M": a.M, "N": a.N, "K": a.K, "path": ["simt", "tcgen05", "simt-tall-skinny", "tcgen05-tall-skinny"][a.path], "ms": ms.value,
+                      "tflops": fl / ms.value / 1e9, "a_gbs": 8.0 * a.M * a.K / ms.value / 1e6}))
 
 
 if __name__ == "__main__":
