@@ -5,20 +5,22 @@
 // only, so the kernel is meant to run at the speed of reading A from HBM.
 //
 // A is not copied or pre-split: front blocks start and stride at arbitrary
-// 8-byte boundaries, which rules out TMA, so eight loader warps read A with
-// plain 8-byte loads (one 128-byte row segment per half-warp), split every
-// value into TF32 hi + lo (x = hi + lo to ~2^-24) and store both halves into
-// the 128-byte-swizzled K-major tiles the MMA reads.  B is expanded once per
+// 8-byte boundaries, which rules out TMA, so eight loader warps stream A with
+// 8-byte asynchronous copies (cp.async, one 128-byte row segment per
+// half-warp) into a ring of TS_RAW raw stages (~112 KB per SM in flight),
+// then split every value into TF32 hi + lo (x = hi + lo to ~2^-24)
+// and store both halves into the 128-byte-swizzled K-major tiles the MMA
+// reads.  B is expanded once per
 // launch into the 64 x 2K real matrix B~ (rows 2j, 2j+1 of column j, as in the
 // square tensor-core GEMM), split into hi and lo, and fetched by TMA.  The
 // complex product is the real product A_r B~^T into a 128 x 64 FP32 TMEM
 // accumulator with D = Ahi Bhi + Ahi Blo + Alo Bhi.
 //
-// Work unit = (task, 128-row tile, K-chunk); persistent CTAs, two per SM.
-// Warps 0-7 load and split A, warp 8 issues the TMA copies of B~ (and owns the
-// TMEM allocation), warp 9 (one lane) issues the MMAs, warps 10-13 drain the
-// double-buffered accumulator: C -= D in place, or with atomics when the task
-// is split along K or its rows are scattered (border updates).  Every
+// Work unit = (task, 128-row tile, K-chunk); persistent CTAs, one per SM.
+// Warps 0-15 load and split A, warp 16 issues the TMA copies of B~ (and owns
+// the TMEM allocation), warp 17 (one lane) issues the MMAs, warps 18-21 drain
+// the double-buffered accumulator: C -= D in place, or with atomics when the
+// task is split along K or its rows are scattered (border updates).  Every
 // mbarrier wait is bounded; on expiry the kernel records an error code and
 // winds down as the square kernel does.
 #include "tc_gemm.h"
@@ -29,16 +31,25 @@ namespace wt3d {
 constexpr int TS_BM = 128;                        // complex rows per tile (MMA M)
 constexpr int TS_NR = 64;                         // real accumulator columns: 32 complex (MMA N)
 constexpr int TS_KC = 16;                         // complex k per stage: one 128-byte swizzle row
-constexpr int TS_STAGES = 2;
+constexpr int TS_STAGES = 2;                      // split A stages (hi + lo)
+constexpr int TS_BSTAGES = 2;                     // B~ stages (TMA from L2)
 constexpr int TS_A_BYTES = TS_BM * 128;           // 16 KB per split half
 constexpr int TS_B_BYTES = TS_NR * 128;           // 8 KB per split half
-constexpr int TS_STAGE_BYTES = 2 * TS_A_BYTES + 2 * TS_B_BYTES;
-constexpr int TS_SMEM = TS_STAGES * TS_STAGE_BYTES + 1024 + 256;
-constexpr int TS_LOADERS = 8;                     // loader warps
+constexpr int TS_ASTAGE_BYTES = 2 * TS_A_BYTES;
+constexpr int TS_BSTAGE_BYTES = 2 * TS_B_BYTES;
+constexpr int TS_RAW = 8;                         // raw A stages in flight (asynchronous copies)
+constexpr int TS_RAW_BYTES = TS_BM * TS_KC * 8;   // 16 KB
+constexpr int TS_B_OFF = TS_STAGES * TS_ASTAGE_BYTES;
+constexpr int TS_RAW_OFF = TS_B_OFF + TS_BSTAGES * TS_BSTAGE_BYTES;
+constexpr int TS_BAR_OFF = TS_RAW_OFF + TS_RAW * TS_RAW_BYTES;
+constexpr int TS_SMEM = TS_BAR_OFF + 1024 + 256;
+constexpr int TS_LOADERS = 16;                    // loader warps
 constexpr int TS_WB = TS_LOADERS, TS_WM = TS_LOADERS + 1, TS_WE = TS_LOADERS + 2;
 constexpr int TS_THREADS = (TS_LOADERS + 6) * 32; // + B producer, MMA, 4 epilogue warps
-constexpr int TS_PER_THREAD = TS_BM * TS_KC / (TS_LOADERS * 32);   // complex loads per loader thread per stage
-static_assert(TS_PER_THREAD == 8, "loader mapping assumes 8 elements per thread");
+constexpr int TS_LT = TS_LOADERS * 32;            // loader threads
+constexpr int TS_PER_THREAD = TS_BM * TS_KC / TS_LT;   // complex elements per loader thread per stage
+constexpr int TS_QROWS = TS_LT / TS_KC;           // rows between a thread's elements
+static_assert(TS_PER_THREAD * TS_LT == TS_BM * TS_KC && TS_QROWS % 8 == 0, "loader mapping");
 
 // Unit u of a launch: its task, first row, and K range [k0, k1).
 __device__ __forceinline__ const TsTask *ts_unit(const TsTask *__restrict__ tasks, int ntasks, long long u, int &m0,
@@ -99,29 +110,80 @@ __global__ void __launch_bounds__(256) k_ts_expand_b(const TsTask *__restrict__ 
     }
 }
 
-// Loader thread l holds elements e = 256 i + l (i < 8) of a 128 x 16 complex
-// stage: row e / 16, k e % 16, so a half-warp reads one contiguous 128-byte
-// row segment.
-__device__ __forceinline__ void ts_load(const TsTask *t, int m0, int kb, int k1, int l, float2 (&v)[TS_PER_THREAD])
+// Position of a CTA's loaders in its sequence of stages: unit u (every
+// gridDim.x-th unit from blockIdx.x), its K range and stage i within it, with
+// the per-thread quantities of the unit precomputed.  Loader thread l owns
+// elements e = TS_LT q + l (q < TS_PER_THREAD) of a 128 x 16 complex stage:
+// row e / 16 = TS_QROWS q + l / 16, column e % 16 = l % 16, so a half-warp
+// covers one contiguous 128-byte row segment of A and all of a thread's
+// elements share one column.
+struct TsCursor {
+    const TsTask *t;
+    const cx<float> *src;   // element q = 0 of stage 0 of this thread
+    long long u, qstep;     // qstep: complex elements between the thread's rows
+    int k0, k1, nsub, i, nq;
+    bool valid;
+};
+
+__device__ __forceinline__ void ts_cursor_at(TsCursor &c, const TsTask *__restrict__ tasks, int ntasks, long long nunits,
+                                             long long u, int l)
 {
-#pragma unroll
-    for (int i = 0; i < TS_PER_THREAD; i++) {
-        const int e = i * (TS_LOADERS * 32) + l, r = m0 + (e >> 4), k = kb + (e & 15);
-        v[i] = make_float2(0.f, 0.f);
-        if (r < t->M && k < k1)
-            v[i] = __ldg(reinterpret_cast<const float2 *>(t->A + (long long)r * t->lda + k));
-    }
+    c.u = u;
+    c.valid = u < nunits;
+    if (!c.valid) return;
+    int m0;
+    c.t = ts_unit(tasks, ntasks, u, m0, c.k0, c.k1);
+    c.nsub = (c.k1 - c.k0 + TS_KC - 1) / TS_KC;
+    c.i = 0;
+    const int r0 = m0 + (l >> 4), M = c.t->M;
+    c.nq = r0 < M ? min(TS_PER_THREAD, (M - r0 + TS_QROWS - 1) / TS_QROWS) : 0;   // elements q < nq in range
+    c.qstep = (long long)TS_QROWS * c.t->lda;
+    c.src = c.t->A + (long long)r0 * c.t->lda + c.k0 + (l & 15);
 }
 
-__global__ void __launch_bounds__(TS_THREADS, 2)
+__device__ __forceinline__ void ts_cursor_next(TsCursor &c, const TsTask *__restrict__ tasks, int ntasks,
+                                               long long nunits, int l)
+{
+    if (++c.i == c.nsub) ts_cursor_at(c, tasks, ntasks, nunits, c.u + gridDim.x, l);
+}
+
+// this thread's column of the cursor's stage lies inside the unit's K range
+__device__ __forceinline__ bool ts_col_ok(const TsCursor &c, int l) { return c.k0 + c.i * TS_KC + (l & 15) < c.k1; }
+
+// asynchronous 8-byte copies of the thread's elements into its slots raw[q][l]
+__device__ __forceinline__ void ts_issue(const TsCursor &c, int l, uint32_t raw)
+{
+    if (!ts_col_ok(c, l)) return;
+    const cx<float> *src = c.src + c.i * TS_KC;
+#pragma unroll
+    for (int q = 0; q < TS_PER_THREAD; q++)
+        if (q < c.nq)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(raw + (uint32_t)((q * TS_LT + l) * 8)),
+                         "l"(src + q * c.qstep)
+                         : "memory");
+}
+
+// hi = TF32 rounding of x (to nearest), lo = TF32 rounding of x - hi
+__device__ __forceinline__ void split_cvt(float x, float &hi, float &lo)
+{
+    uint32_t h, lw;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+    hi = __uint_as_float(h);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lw) : "f"(x - hi));
+    lo = __uint_as_float(lw);
+}
+
+__global__ void __launch_bounds__(TS_THREADS, 1)
     k_tc_ts(const TsTask *__restrict__ tasks, int ntasks, long long nunits, const CUtensorMap *__restrict__ maps,
             int *err)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + TS_STAGES * TS_STAGE_BYTES);
-    uint64_t *empty = full + TS_STAGES;
-    uint64_t *tfull = empty + TS_STAGES;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + TS_BAR_OFF);   // split A stage written (8 loader warps)
+    uint64_t *empty = full + TS_STAGES;                                  // split A stage consumed (MMA commit)
+    uint64_t *bfull = empty + TS_STAGES;                                 // B~ stage landed (TMA)
+    uint64_t *bempty = bfull + TS_BSTAGES;                               // B~ stage consumed (MMA commit)
+    uint64_t *tfull = bempty + TS_BSTAGES;
     uint64_t *tempty = tfull + 2;
     uint64_t *drain = tempty + 2;
     uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(drain + 1);
@@ -134,8 +196,12 @@ __global__ void __launch_bounds__(TS_THREADS, 2)
     }
     if (threadIdx.x == TS_WM * 32) {
         for (int s = 0; s < TS_STAGES; s++) {
-            mbar_init(&full[s], TS_LOADERS + 1);   // 8 loader warps + the B copy's expect_tx arrival
+            mbar_init(&full[s], TS_LOADERS);
             mbar_init(&empty[s], 1);
+        }
+        for (int s = 0; s < TS_BSTAGES; s++) {
+            mbar_init(&bfull[s], 1);
+            mbar_init(&bempty[s], 1);
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(&tfull[b], 1);
@@ -150,42 +216,61 @@ __global__ void __launch_bounds__(TS_THREADS, 2)
     const uint32_t tmem = *tmem_holder;
 
     if (warp < TS_LOADERS) {
-        // ---------------- A loaders: global -> split -> swizzled tiles ----------------
+        // ---------------- A loaders: global -> raw ring -> split -> swizzled tiles ----------------
+        // The copy cursor runs TS_RAW - 1 stages ahead of the conversion
+        // cursor, across unit boundaries; one commit group per stage (empty
+        // groups past the end keep the count uniform).
         const int l = threadIdx.x;
-        long long g = 0;
-        bool ok = true;
-        for (long long u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
-            int m0, k0, k1;
-            const TsTask *t = ts_unit(tasks, ntasks, u, m0, k0, k1);
-            const int nsub = (k1 - k0 + TS_KC - 1) / TS_KC;
-            float2 nxt[TS_PER_THREAD];
-            ts_load(t, m0, k0, k1, l, nxt);
-            for (int i = 0; i < nsub; i++, g++) {
-                float2 cur[TS_PER_THREAD];
-#pragma unroll
-                for (int q = 0; q < TS_PER_THREAD; q++) cur[q] = nxt[q];
-                if (i + 1 < nsub) ts_load(t, m0, k0 + (i + 1) * TS_KC, k1, l, nxt);   // in flight meanwhile
-                const int s = (int)(g % TS_STAGES);
-                const uint32_t ph = (uint32_t)((g / TS_STAGES) & 1) ^ 1u;
-                if (!mbar_wait(&empty[s], ph)) { atomicCAS(err, 0, 11); ok = false; break; }
-                uint8_t *ahi = smem + s * TS_STAGE_BYTES, *alo = ahi + TS_A_BYTES;
-#pragma unroll
-                for (int q = 0; q < TS_PER_THREAD; q++) {
-                    const int e = q * (TS_LOADERS * 32) + l, r = e >> 4, kc = e & 15;
-                    // 128-byte swizzle: 16-byte chunk c of row r sits at chunk c ^ (r mod 8)
-                    const int off = (r >> 3) * 1024 + (r & 7) * 128 + ((((kc >> 1) ^ (r & 7))) << 4) + ((kc & 1) << 3);
-                    float h0, l0, h1, l1;
-                    split_tf32(cur[q].x, h0, l0);
-                    split_tf32(cur[q].y, h1, l1);
-                    *reinterpret_cast<float2 *>(ahi + off) = make_float2(h0, h1);
-                    *reinterpret_cast<float2 *>(alo + off) = make_float2(l0, l1);
-                }
-                // generic-proxy stores become visible to the tensor core's async proxy
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&full[s]);
+        uint8_t *rawb = smem + TS_RAW_OFF;
+        const uint32_t raw0 = smem_u32(rawb);
+        TsCursor cp, cs;
+        ts_cursor_at(cp, tasks, ntasks, nunits, blockIdx.x, l);
+        ts_cursor_at(cs, tasks, ntasks, nunits, blockIdx.x, l);
+        // byte offset of element q in a swizzled tile: 16-byte chunk c of row r
+        // sits at chunk c ^ (r mod 8); r mod 8 and the column are fixed per thread
+        const int rl = l >> 4, kc = l & 15;
+        const int offl = (rl >> 3) * 1024 + (rl & 7) * 128 + (((kc >> 1) ^ (rl & 7)) << 4) + ((kc & 1) << 3);
+        long long gc = 0, g = 0;
+        for (int p = 0; p < TS_RAW - 1; p++, gc++) {
+            if (cp.valid) {
+                ts_issue(cp, l, raw0 + (uint32_t)((gc % TS_RAW) * TS_RAW_BYTES));
+                ts_cursor_next(cp, tasks, ntasks, nunits, l);
             }
+            asm volatile("cp.async.commit_group;" ::: "memory");
         }
+        while (cs.valid) {
+            if (cp.valid) {
+                ts_issue(cp, l, raw0 + (uint32_t)((gc % TS_RAW) * TS_RAW_BYTES));
+                ts_cursor_next(cp, tasks, ntasks, nunits, l);
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+            gc++;
+            asm volatile("cp.async.wait_group %0;" ::"n"(TS_RAW - 1) : "memory");   // stage g has landed
+            const float2 *rv = reinterpret_cast<const float2 *>(rawb + (g % TS_RAW) * TS_RAW_BYTES);
+            const int s = (int)(g % TS_STAGES);
+            const uint32_t ph = (uint32_t)((g / TS_STAGES) & 1) ^ 1u;
+            if (!mbar_wait(&empty[s], ph)) { atomicCAS(err, 0, 11); break; }
+            uint8_t *ahi = smem + s * TS_ASTAGE_BYTES, *alo = ahi + TS_A_BYTES;
+            const int nq = ts_col_ok(cs, l) ? cs.nq : 0;
+#pragma unroll
+            for (int q = 0; q < TS_PER_THREAD; q++) {
+                float2 v = make_float2(0.f, 0.f);
+                if (q < nq) v = rv[q * TS_LT + l];
+                const int off = q * (TS_QROWS / 8) * 1024 + offl;
+                float h0, l0, h1, l1;
+                split_cvt(v.x, h0, l0);
+                split_cvt(v.y, h1, l1);
+                *reinterpret_cast<float2 *>(ahi + off) = make_float2(h0, h1);
+                *reinterpret_cast<float2 *>(alo + off) = make_float2(l0, l1);
+            }
+            // generic-proxy stores become visible to the tensor core's async proxy
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&full[s]);
+            ts_cursor_next(cs, tasks, ntasks, nunits, l);
+            g++;
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");   // no copy into shared memory outlives the CTA
     } else if (warp == TS_WB && lane == 0) {
         // ---------------- B~ producer (TMA) ----------------
         long long g = 0;
@@ -196,20 +281,20 @@ __global__ void __launch_bounds__(TS_THREADS, 2)
             const CUtensorMap *mp = maps + t->map0;
             const int nsub = (k1 - k0 + TS_KC - 1) / TS_KC;
             for (int i = 0; i < nsub; i++, g++) {
-                const int s = (int)(g % TS_STAGES);
-                const uint32_t ph = (uint32_t)((g / TS_STAGES) & 1) ^ 1u;
-                if (!mbar_wait(&empty[s], ph)) { atomicCAS(err, 0, 12); ok = false; break; }
-                uint8_t *st = smem + s * TS_STAGE_BYTES + 2 * TS_A_BYTES;
-                mbar_expect_tx(&full[s], 2 * TS_B_BYTES);
+                const int s = (int)(g % TS_BSTAGES);
+                const uint32_t ph = (uint32_t)((g / TS_BSTAGES) & 1) ^ 1u;
+                if (!mbar_wait(&bempty[s], ph)) { atomicCAS(err, 0, 12); ok = false; break; }
+                uint8_t *st = smem + TS_B_OFF + s * TS_BSTAGE_BYTES;
+                mbar_expect_tx(&bfull[s], 2 * TS_B_BYTES);
                 const int x = 2 * (k0 + i * TS_KC);   // real column, a multiple of 32
-                tma_load_2d(st, mp + 0, x, 0, &full[s]);
-                tma_load_2d(st + TS_B_BYTES, mp + 1, x, 0, &full[s]);
+                tma_load_2d(st, mp + 0, x, 0, &bfull[s]);
+                tma_load_2d(st + TS_B_BYTES, mp + 1, x, 0, &bfull[s]);
             }
         }
-        for (int s = 0; s < TS_STAGES; s++) {
+        for (int s = 0; s < TS_BSTAGES; s++) {
             if (g <= s) continue;
-            const long long last = g - 1 - ((g - 1 - s) % TS_STAGES);
-            mbar_wait(&full[s], (uint32_t)((last / TS_STAGES) & 1));
+            const long long last = g - 1 - ((g - 1 - s) % TS_BSTAGES);
+            mbar_wait(&bfull[s], (uint32_t)((last / TS_BSTAGES) & 1));
         }
     } else if (warp == TS_WM && lane == 0) {
         // ---------------- MMA issuer ----------------
@@ -227,12 +312,16 @@ __global__ void __launch_bounds__(TS_THREADS, 2)
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t dacc = tmem + (uint32_t)(b * TS_NR);
             for (int i = 0; i < nsub; i++, g++) {
-                const int s = (int)(g % TS_STAGES);
-                if (!mbar_wait(&full[s], (uint32_t)((g / TS_STAGES) & 1))) { atomicCAS(err, 0, 13); ok = false; break; }
+                const int s = (int)(g % TS_STAGES), sb = (int)(g % TS_BSTAGES);
+                if (!mbar_wait(&full[s], (uint32_t)((g / TS_STAGES) & 1)) ||
+                    !mbar_wait(&bfull[sb], (uint32_t)((g / TS_BSTAGES) & 1))) {
+                    atomicCAS(err, 0, 13);
+                    ok = false;
+                    break;
+                }
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t base = smem_u32(smem + s * TS_STAGE_BYTES);
-                const uint32_t a_hi = base, a_lo = base + TS_A_BYTES;
-                const uint32_t b_hi = base + 2 * TS_A_BYTES, b_lo = b_hi + TS_B_BYTES;
+                const uint32_t a_hi = smem_u32(smem + s * TS_ASTAGE_BYTES), a_lo = a_hi + TS_A_BYTES;
+                const uint32_t b_hi = smem_u32(smem + TS_B_OFF + sb * TS_BSTAGE_BYTES), b_lo = b_hi + TS_B_BYTES;
 #pragma unroll
                 for (int kk = 0; kk < 4; kk++) {
                     const uint32_t off = kk * 32;   // 8 TF32 values along K
@@ -243,6 +332,7 @@ __global__ void __launch_bounds__(TS_THREADS, 2)
                     umma_tf32(dacc, dal, dbh, idesc, 1);
                 }
                 umma_commit(&empty[s]);
+                umma_commit(&bempty[sb]);
             }
             if (!ok) break;
             umma_commit(&tfull[b]);
@@ -347,7 +437,7 @@ int ts_build_launch(TsLaunch &L, const GemmTask<float> *g, int n, float *ws)
     // K-chunk so that the launch has about four units per resident CTA
     double work = 0;
     for (int i = 0; i < n; i++) work += (double)((g[i].M + TS_BM - 1) / TS_BM) * g[i].K;
-    const long long slots = 2LL * ts_sms();
+    const long long slots = ts_sms();   // one CTA per SM
     const int kchunk = (int)std::max<long long>(256, align_up((long long)std::ceil(work / (4.0 * slots)), TS_KC));
     long long off = 0, units = 0, bw = 0;
     for (int i = 0; i < n; i++) {
@@ -392,7 +482,7 @@ void ts_expand(const TsLaunch &L, cudaStream_t st)
 void ts_mma(const TsLaunch &L, int *err, cudaStream_t st)
 {
     if (L.ntasks == 0) return;
-    const long long grid = std::min<long long>(L.units, 2LL * ts_sms());
+    const long long grid = std::min<long long>(L.units, ts_sms());
     k_tc_ts<<<(unsigned)grid, TS_THREADS, TS_SMEM, st>>>(L.tasks.p, L.ntasks, L.units,
                                                          reinterpret_cast<const CUtensorMap *>(L.maps.p), err);
 }
