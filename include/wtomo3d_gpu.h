@@ -342,7 +342,8 @@ int wt3d_debug_fetch(wt3d_solver *h, int what, void *out, long long count);
 /* One complex64 GEMM C -= A B on host row-major arrays through the tensor-core
  * kernel (path 1), the SIMT kernel (path 0) or the tall-skinny tensor-core
  * kernel of the substitution passes (path 3, N <= 32; path 4 also gathers B
- * rows K-1-k and scatters C rows M-1-r); for checks of the kernels. */
+ * rows K-1-k and scatters C rows M-1-r; path 5 computes C -= A^H B with A
+ * given as the K x M block, lda >= M); for checks of the kernels. */
 int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int lda, const void *B, int ldb, void *C,
                     int ldc);
 

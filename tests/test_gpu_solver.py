@@ -222,8 +222,9 @@ def test_tensor_core_substitution_matches_simt():
     """40^3 (the configuration-1 grid), complex64 factors: the substitution
     passes with their large blocks on the tall-skinny tensor-core kernel
     (WT3D_TS unset) and on the SIMT kernel (WT3D_TS=0) reach the same refined
-    solution in the same number of passes, and the tensor-core launches are in
-    the schedule."""
+    solution in the same number of passes, forward and conjugate-transpose
+    (whose blocks the kernel reads transposed), and the tensor-core launches
+    are in the schedule."""
     import ctypes
     import os
     g = Grid(40, 40, 40, 25.0, pmld=10 * 25.0, fst=0)
@@ -239,6 +240,9 @@ def test_tensor_core_substitution_matches_simt():
                 s.set_model(*model.homogeneous(40, 40, 40))
                 s.factor(2 * np.pi)
                 X = s.solve(B, tol=1e-10, maxit=20)
+                it_f = s.last_iters
+                XH = s.solve_adjoint(B, tol=1e-10, maxit=20)
+                it_a = s.last_iters
                 L = wt.lib()
                 L.wt3d_profile_launches.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                                     ctypes.c_int, ctypes.c_void_p]
@@ -248,10 +252,11 @@ def test_tensor_core_substitution_matches_simt():
                 assert L.wt3d_profile_launches(s._h, 1, 8, ctypes.c_void_p(rec.ctypes.data), cap,
                                                ctypes.byref(cnt)) == 0
                 kinds = rec[:4 * min(cnt.value, cap)].reshape(-1, 4)[:, 0]
-                out[ts] = (X, s.last_iters, int(np.sum(kinds == 8)))
+                out[ts] = (X, it_f, XH, it_a, int(np.sum(kinds == 8)))
         finally:
             os.environ.pop("WT3D_TS", None)
-    (X1, it1, n1), (X0, it0, n0) = out["1"], out["0"]
+    (X1, it1, XH1, ia1, n1), (X0, it0, XH0, ia0, n0) = out["1"], out["0"]
     assert n1 > 0 and n0 == 0, (n1, n0)
-    assert it1 <= it0 + 1, (it1, it0)
+    assert it1 <= it0 + 1 and ia1 <= ia0 + 1, (it1, it0, ia1, ia0)
     assert np.linalg.norm(X1 - X0) <= 1e-6 * np.linalg.norm(X0)
+    assert np.linalg.norm(XH1 - XH0) <= 1e-6 * np.linalg.norm(XH0)

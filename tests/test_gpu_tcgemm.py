@@ -57,15 +57,17 @@ def test_gemm_strided_views():
 
 
 def gemm_ld(path, A, lda, B, C):
-    """C -= A B with A passed as the first A.shape[1] columns of rows lda apart."""
+    """C -= A B (path 5: C -= A^H B) with A passed as the first A.shape[1]
+    columns of rows lda apart."""
     L = wt.lib()
     L.wt3d_debug_gemm.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                        ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
-    M, K = A.shape
+    rows, cols = A.shape
+    M, K = (cols, rows) if path == 5 else (rows, cols)
     N = B.shape[1]
-    Abuf = np.zeros((M, lda), np.complex64)
-    Abuf[:, :K] = A
-    Abuf[:, K:] = np.nan     # never read
+    Abuf = np.zeros((rows, lda), np.complex64)
+    Abuf[:, :cols] = A
+    Abuf[:, cols:] = np.nan     # never read
     B = np.ascontiguousarray(B, np.complex64)
     C = np.ascontiguousarray(C, np.complex64).copy()
     p = lambda a: ctypes.c_void_p(a.ctypes.data)
@@ -94,5 +96,24 @@ def test_tall_skinny_tensor_core_gemm(shape, path):
         prod, scale = prod[::-1], scale[::-1]
     ref = C.astype(np.complex128) - prod
     out = gemm_ld(path, A, K + 3 if K % 2 == 0 else K, B, C)
+    err = (np.abs(out - ref) / (scale + np.abs(C))).max()
+    assert err < 1e-6 + 3e-7 * np.sqrt(K), err
+
+
+@pytest.mark.parametrize("shape", [(128, 32, 256), (130, 32, 300), (1000, 17, 777), (300, 1, 4099),
+                                   (2048, 32, 5000)])
+def test_tall_skinny_tensor_core_gemm_conjugate(shape):
+    """Path 5: C -= A^H B with A stored as the K x M block (the adjoint
+    substitution passes read factor blocks this way), odd row stride."""
+    M, N, K = shape
+    r = np.random.default_rng(3 * M + N + 7 * K)
+    At = (r.standard_normal((K, M)) + 1j * r.standard_normal((K, M))).astype(np.complex64)
+    B = (r.standard_normal((K, N)) + 1j * r.standard_normal((K, N))).astype(np.complex64)
+    C = (r.standard_normal((M, N)) + 1j * r.standard_normal((M, N))).astype(np.complex64)
+    AH = At.astype(np.complex128).conj().T
+    ref = C.astype(np.complex128) - AH @ B.astype(np.complex128)
+    scale = np.abs(AH) @ np.abs(B).astype(np.float64)
+    lda = M + 3 if M % 2 == 0 else M
+    out = gemm_ld(5, At, lda, B, C)
     err = (np.abs(out - ref) / (scale + np.abs(C))).max()
     assert err < 1e-6 + 3e-7 * np.sqrt(K), err

@@ -423,7 +423,8 @@ int tc_init()
 // C ABI check entry: one GEMM C -= A B on host complex64 arrays (row-major),
 // through the tensor-core path (path = 1), the SIMT path (path = 0) or the
 // tall-skinny tensor-core kernel of the solves (path = 3; path = 4 with a row
-// gather of B and a row scatter of C).  wt3d_bench_gemm also times path 2,
+// gather of B and a row scatter of C; path = 5 with C -= A^H B for A given as
+// the K x M block, lda >= M).  wt3d_bench_gemm also times path 2,
 // the tall-skinny SIMT kernel, and path 3.
 // ---------------------------------------------------------------------------
 using namespace wt3d;
@@ -439,9 +440,10 @@ extern "C" int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int
 {
     DevVec<cx<float>> dA, dB, dC;
     int rc;
-    if ((rc = dA.alloc((size_t)M * lda)) || (rc = dB.alloc((size_t)K * ldb)) || (rc = dC.alloc((size_t)M * ldc)))
+    const size_t arows = path == 5 ? (size_t)K : (size_t)M;   // path 5: A holds the K x M block whose A^H is used
+    if ((rc = dA.alloc(arows * lda)) || (rc = dB.alloc((size_t)K * ldb)) || (rc = dC.alloc((size_t)M * ldc)))
         return rc;
-    WT_CUDA(cudaMemcpy(dA.p, A, sizeof(cx<float>) * M * lda, cudaMemcpyHostToDevice));
+    WT_CUDA(cudaMemcpy(dA.p, A, sizeof(cx<float>) * arows * lda, cudaMemcpyHostToDevice));
     WT_CUDA(cudaMemcpy(dB.p, B, sizeof(cx<float>) * K * ldb, cudaMemcpyHostToDevice));
     WT_CUDA(cudaMemcpy(dC.p, C, sizeof(cx<float>) * M * ldc, cudaMemcpyHostToDevice));
     GemmTask<float> g{};
@@ -460,10 +462,11 @@ extern "C" int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int
         if ((rc = tc_build_launch(L, &g, 1, ws.p))) return rc;
         tc_split(L, 0);
         tc_mma(L, err.p, 0);
-    } else if (path == 3 || path == 4) {
+    } else if (path >= 3 && path <= 5) {
         // tall-skinny tensor-core kernel; path 4 gathers B rows K-1-k and
-        // scatters C rows M-1-r (atomic epilogue)
-        if (N > 32) { set_error("wt3d_debug_gemm: paths 3 and 4 need N <= 32"); return WT3D_ERR_ARG; }
+        // scatters C rows M-1-r (atomic epilogue); path 5 uses A^H
+        if (N > 32) { set_error("wt3d_debug_gemm: paths 3 to 5 need N <= 32"); return WT3D_ERR_ARG; }
+        g.conjA = path == 5 ? 1 : 0;
         if (path == 4) {
             std::vector<int> br(K), cr(M);
             for (int k = 0; k < K; k++) br[k] = K - 1 - k;

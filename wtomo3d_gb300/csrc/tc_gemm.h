@@ -33,6 +33,7 @@ struct TsTask {
     float *bhi, *blo;               // expanded, split B~ (64 x Kr) in the launch workspace
     int lda, ldb, ldc, M, N, K, Kr;
     int kchunk, nkc, atom;          // K-chunk per work unit, chunks, atomic epilogue
+    int conjA;                      // A^H of the stored K x M block (lda its row stride)
     int map0;                       // first of this task's 2 tensor maps
     long long unit0, b_work0;
 };

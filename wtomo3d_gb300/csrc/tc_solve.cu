@@ -1,7 +1,7 @@
 // Tall-skinny complex64 GEMM  C -= A B  on the tcgen05 tensor cores, for the
 // substitution passes of the solve: A is a factor block (M x K, K-major rows
-// in the front storage, any leading dimension), B and C hold at most 32
-// right-hand sides.  Each factor entry is used for 32 complex multiply-adds
+// in the front storage, any leading dimension) or, in the adjoint passes, the
+// conjugate transpose of one, and B and C hold at most 32 right-hand sides.  Each factor entry is used for 32 complex multiply-adds
 // only, so the kernel is meant to run at the speed of reading A from HBM.
 //
 // A is not copied or pre-split: front blocks start and stride at arbitrary
@@ -50,6 +50,7 @@ constexpr int TS_LT = TS_LOADERS * 32;            // loader threads
 constexpr int TS_PER_THREAD = TS_BM * TS_KC / TS_LT;   // complex elements per loader thread per stage
 constexpr int TS_QROWS = TS_LT / TS_KC;           // rows between a thread's elements
 static_assert(TS_PER_THREAD * TS_LT == TS_BM * TS_KC && TS_QROWS % 8 == 0, "loader mapping");
+static_assert((TS_LT / TS_BM) * TS_PER_THREAD == TS_KC, "conjugate-transposed loader mapping");
 
 // Unit u of a launch: its task, first row, and K range [k0, k1).
 __device__ __forceinline__ const TsTask *ts_unit(const TsTask *__restrict__ tasks, int ntasks, long long u, int &m0,
@@ -112,17 +113,23 @@ __global__ void __launch_bounds__(256) k_ts_expand_b(const TsTask *__restrict__ 
 
 // Position of a CTA's loaders in its sequence of stages: unit u (every
 // gridDim.x-th unit from blockIdx.x), its K range and stage i within it, with
-// the per-thread quantities of the unit precomputed.  Loader thread l owns
-// elements e = TS_LT q + l (q < TS_PER_THREAD) of a 128 x 16 complex stage:
-// row e / 16 = TS_QROWS q + l / 16, column e % 16 = l % 16, so a half-warp
-// covers one contiguous 128-byte row segment of A and all of a thread's
-// elements share one column.
+// the per-thread quantities of the unit precomputed.  A stage is 128 rows x
+// 16 k of the operand; loader thread l owns TS_PER_THREAD of its elements:
+//   A as stored (row-major, K-major): row TS_QROWS q + l / 16, column l % 16:
+//     a half-warp reads one contiguous 128-byte row segment, and all of a
+//     thread's elements share one column;
+//   A^H (conjugate transpose of a stored K x M block, MN-major): row l % 128,
+//     column l / 128 + 4 q: a warp reads 32 consecutive stored entries of one
+//     stored row, and all of a thread's elements share one row.
 struct TsCursor {
     const TsTask *t;
     const cx<float> *src;   // element q = 0 of stage 0 of this thread
-    long long u, qstep;     // qstep: complex elements between the thread's rows
-    int k0, k1, nsub, i, nq;
-    bool valid;
+    long long u, qstep;     // complex elements between the thread's elements q and q + 1
+    long long sstep;        // complex elements between consecutive stages
+    int k0, k1, nsub, i;
+    int nq;                 // A: elements in range (rows); A^H: 4 if the row is in range, else 0
+    int kq;                 // first column of this thread within a stage
+    bool valid, conj;
 };
 
 __device__ __forceinline__ void ts_cursor_at(TsCursor &c, const TsTask *__restrict__ tasks, int ntasks, long long nunits,
@@ -135,10 +142,24 @@ __device__ __forceinline__ void ts_cursor_at(TsCursor &c, const TsTask *__restri
     c.t = ts_unit(tasks, ntasks, u, m0, c.k0, c.k1);
     c.nsub = (c.k1 - c.k0 + TS_KC - 1) / TS_KC;
     c.i = 0;
-    const int r0 = m0 + (l >> 4), M = c.t->M;
-    c.nq = r0 < M ? min(TS_PER_THREAD, (M - r0 + TS_QROWS - 1) / TS_QROWS) : 0;   // elements q < nq in range
-    c.qstep = (long long)TS_QROWS * c.t->lda;
-    c.src = c.t->A + (long long)r0 * c.t->lda + c.k0 + (l & 15);
+    const int M = c.t->M;
+    const long long lda = c.t->lda;
+    c.conj = c.t->conjA != 0;
+    if (!c.conj) {
+        const int r0 = m0 + (l >> 4);
+        c.kq = l & 15;
+        c.nq = r0 < M ? min(TS_PER_THREAD, (M - r0 + TS_QROWS - 1) / TS_QROWS) : 0;
+        c.qstep = (long long)TS_QROWS * lda;
+        c.sstep = TS_KC;
+        c.src = c.t->A + (long long)r0 * lda + c.k0 + c.kq;
+    } else {
+        const int r = m0 + (l & (TS_BM - 1));
+        c.kq = l / TS_BM;
+        c.nq = r < M ? TS_PER_THREAD : 0;
+        c.qstep = (long long)(TS_LT / TS_BM) * lda;
+        c.sstep = (long long)TS_KC * lda;
+        c.src = c.t->A + (long long)(c.k0 + c.kq) * lda + r;
+    }
 }
 
 __device__ __forceinline__ void ts_cursor_next(TsCursor &c, const TsTask *__restrict__ tasks, int ntasks,
@@ -147,20 +168,33 @@ __device__ __forceinline__ void ts_cursor_next(TsCursor &c, const TsTask *__rest
     if (++c.i == c.nsub) ts_cursor_at(c, tasks, ntasks, nunits, c.u + gridDim.x, l);
 }
 
-// this thread's column of the cursor's stage lies inside the unit's K range
-__device__ __forceinline__ bool ts_col_ok(const TsCursor &c, int l) { return c.k0 + c.i * TS_KC + (l & 15) < c.k1; }
+// elements q < ts_count of the cursor's stage lie in the operand
+__device__ __forceinline__ int ts_count(const TsCursor &c)
+{
+    const int kb = c.k0 + c.i * TS_KC + c.kq;   // column of element q = 0
+    if (!c.conj) return kb < c.k1 ? c.nq : 0;
+    constexpr int kstep = TS_LT / TS_BM;         // columns between a thread's elements
+    return c.nq ? max(0, min(TS_PER_THREAD, (c.k1 - kb + kstep - 1) / kstep)) : 0;
+}
 
 // asynchronous 8-byte copies of the thread's elements into its slots raw[q][l]
 __device__ __forceinline__ void ts_issue(const TsCursor &c, int l, uint32_t raw)
 {
-    if (!ts_col_ok(c, l)) return;
-    const cx<float> *src = c.src + c.i * TS_KC;
+    const int n = ts_count(c);
+    const cx<float> *src = c.src + c.i * c.sstep;
 #pragma unroll
     for (int q = 0; q < TS_PER_THREAD; q++)
-        if (q < c.nq)
+        if (q < n)
             asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(raw + (uint32_t)((q * TS_LT + l) * 8)),
                          "l"(src + q * c.qstep)
                          : "memory");
+}
+
+// byte offset of element (row r, column k) of a stage in a 128-byte-swizzled
+// K-major tile: 16-byte chunk c of row r sits at chunk c ^ (r mod 8)
+__device__ __forceinline__ int ts_swz(int r, int k)
+{
+    return (r >> 3) * 1024 + (r & 7) * 128 + ((((k >> 1) ^ (r & 7))) << 4) + ((k & 1) << 3);
 }
 
 // hi = TF32 rounding of x (to nearest), lo = TF32 rounding of x - hi
@@ -226,10 +260,6 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
         TsCursor cp, cs;
         ts_cursor_at(cp, tasks, ntasks, nunits, blockIdx.x, l);
         ts_cursor_at(cs, tasks, ntasks, nunits, blockIdx.x, l);
-        // byte offset of element q in a swizzled tile: 16-byte chunk c of row r
-        // sits at chunk c ^ (r mod 8); r mod 8 and the column are fixed per thread
-        const int rl = l >> 4, kc = l & 15;
-        const int offl = (rl >> 3) * 1024 + (rl & 7) * 128 + (((kc >> 1) ^ (rl & 7)) << 4) + ((kc & 1) << 3);
         long long gc = 0, g = 0;
         for (int p = 0; p < TS_RAW - 1; p++, gc++) {
             if (cp.valid) {
@@ -251,12 +281,15 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
             const uint32_t ph = (uint32_t)((g / TS_STAGES) & 1) ^ 1u;
             if (!mbar_wait(&empty[s], ph)) { atomicCAS(err, 0, 11); break; }
             uint8_t *ahi = smem + s * TS_ASTAGE_BYTES, *alo = ahi + TS_A_BYTES;
-            const int nq = ts_col_ok(cs, l) ? cs.nq : 0;
+            const int nq = ts_count(cs);
+            const float ysign = cs.conj ? -1.f : 1.f;
 #pragma unroll
             for (int q = 0; q < TS_PER_THREAD; q++) {
                 float2 v = make_float2(0.f, 0.f);
                 if (q < nq) v = rv[q * TS_LT + l];
-                const int off = q * (TS_QROWS / 8) * 1024 + offl;
+                v.y *= ysign;
+                const int off = cs.conj ? ts_swz(l & (TS_BM - 1), cs.kq + q * (TS_LT / TS_BM))
+                                        : ts_swz(TS_QROWS * q + (l >> 4), l & 15);
                 float h0, l0, h1, l1;
                 split_cvt(v.x, h0, l0);
                 split_cvt(v.y, h1, l1);
@@ -416,9 +449,9 @@ static int ts_sms()
 
 bool ts_eligible(const GemmTask<float> &g)
 {
-    // large factor blocks of the substitution passes; conjugate-transposed
-    // blocks (adjoint solves) are MN-major and stay on the SIMT kernel
-    return !g.conjA && g.N <= 32 && g.M >= TS_BM && g.K >= 256;
+    // large factor blocks of the substitution passes, as stored or conjugate-
+    // transposed (adjoint passes)
+    return g.N <= 32 && g.M >= TS_BM && g.K >= 256;
 }
 
 static long long ts_kr(int K) { return align_up(2LL * K, 64); }   // whole 32-complex tiles of B~
@@ -445,6 +478,7 @@ int ts_build_launch(TsLaunch &L, const GemmTask<float> *g, int n, float *ws)
         t.A = g[i].A; t.lda = g[i].lda;
         t.B = g[i].B; t.ldb = g[i].ldb; t.brow = g[i].brow;
         t.C = g[i].C; t.ldc = g[i].ldc; t.crow = g[i].crow;
+        t.conjA = g[i].conjA;
         t.M = g[i].M; t.N = g[i].N; t.K = g[i].K;
         t.Kr = (int)ts_kr(t.K);
         t.kchunk = kchunk;
