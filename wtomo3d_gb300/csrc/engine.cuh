@@ -80,6 +80,9 @@ public:
     std::unique_ptr<Schedule<T>> fsched;
     std::map<int, std::unique_ptr<Schedule<T>>> ssched[2];   // [adjoint][m]
     static constexpr int WB = 512;   // outer block width of the two-level LU
+    // pivots below pivot_rel times the largest entry are perturbed: only
+    // (near-)zero ones, since Dirichlet rows carry unit pivots next to O(1e8)
+    // stiffness entries
     double pivot_rel = 1e-20;
     // tcgen05 path for complex64 front updates (WT3D_TC=0 selects the SIMT kernel)
     bool use_tc = std::is_same<T, float>::value && !(getenv("WT3D_TC") && getenv("WT3D_TC")[0] == '0');
@@ -88,7 +91,7 @@ public:
     bool building_solve = false;   // set while a solve schedule is built: only those route to the TS kernel
     DevVec<float> own_tcws;   // private split workspace, only if the shared one is too small
     DevVec<int> tc_err;                                 // barrier-timeout flag of the tensor-core kernel
-    std::vector<Schedule<T> *> built_tc;   // only (near-)zero pivots are replaced: Dirichlet rows carry unit pivots next to O(1e8) stiffness entries
+    std::vector<Schedule<T> *> built_tc;   // schedules whose tensor maps point into the split workspace
     // launch schedules as captured CUDA graphs (WT3D_GRAPHS=0: direct launches, for profilers)
     bool use_graphs = !(getenv("WT3D_GRAPHS") && getenv("WT3D_GRAPHS")[0] == '0');
 
