@@ -351,7 +351,9 @@ int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int lda, const
  * launches of C -= A B (M x K by K x N complex64, device-filled operands);
  * path 1 = tensor-core kernel (operand split excluded), 0 = SIMT kernel,
  * 2 = tall-skinny SIMT kernel, 3 = tall-skinny tensor-core kernel (B
- * expansion excluded); paths 2 and 3 need N <= 32. */
+ * expansion excluded; A by TMA when 16-byte aligned with an even stride),
+ * 6 = path 3 with A always copied by the loader warps; paths 2, 3 and 6 need
+ * N <= 32. */
 int wt3d_bench_gemm(int path, int M, int N, int K, int iters, double *ms_out);
 
 /* ---- allocation-free entry point ----------------------------------------

@@ -79,11 +79,13 @@ def gemm_ld(path, A, lda, B, C):
 @pytest.mark.parametrize("shape", [(128, 32, 256), (130, 32, 300), (1000, 17, 777), (300, 1, 4099),
                                    (2048, 32, 5000)])
 @pytest.mark.parametrize("path", [3, 4])
-def test_tall_skinny_tensor_core_gemm(shape, path):
-    """The substitution passes' tensor-core kernel (A read and split on the fly,
-    odd leading dimension so rows start off 16-byte boundaries, ragged M and K,
-    fewer than 32 columns, K split across CTAs); path 4 gathers B rows K-1-k and
-    scatters C rows M-1-r."""
+@pytest.mark.parametrize("stride", ["odd", "even"])
+def test_tall_skinny_tensor_core_gemm(shape, path, stride):
+    """The substitution passes' tensor-core kernel (A split on the fly, ragged
+    M and K, fewer than 32 columns, K split across CTAs); path 4 gathers B rows
+    K-1-k and scatters C rows M-1-r.  An odd leading dimension puts rows off
+    16-byte boundaries (A copied by the loader warps); an even one lets TMA
+    stream A."""
     M, N, K = shape
     r = np.random.default_rng(M + 5 * N + 11 * K + path)
     A = (r.standard_normal((M, K)) + 1j * r.standard_normal((M, K))).astype(np.complex64)
@@ -95,7 +97,11 @@ def test_tall_skinny_tensor_core_gemm(shape, path):
     if path == 4:
         prod, scale = prod[::-1], scale[::-1]
     ref = C.astype(np.complex128) - prod
-    out = gemm_ld(path, A, K + 3 if K % 2 == 0 else K, B, C)
+    if stride == "odd":
+        lda = K + 3 if K % 2 == 0 else K
+    else:
+        lda = K if K % 2 == 0 else K + 1
+    out = gemm_ld(path, A, lda, B, C)
     err = (np.abs(out - ref) / (scale + np.abs(C))).max()
     assert err < 1e-6 + 3e-7 * np.sqrt(K), err
 

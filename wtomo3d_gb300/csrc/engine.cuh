@@ -45,6 +45,7 @@ struct Schedule {
     std::vector<std::vector<GemmTask<float>>> tc_pending;   // tensor-core task lists, built after allocation
     std::vector<std::unique_ptr<TcLaunch>> tc;
     std::vector<std::vector<GemmTask<float>>> ts_pending;   // tall-skinny tensor-core task lists (solves)
+    std::vector<char> ts_tma;                                 // ... whose A is streamed by TMA
     std::vector<std::unique_ptr<TsLaunch>> ts;
     DevVec<float> tsws;                                       // their expanded right-hand sides
     cudaGraphExec_t graph = nullptr;
@@ -229,13 +230,20 @@ public:
                                        LK_TCGEMM, fl, by});
             }
             if (use_ts && building_solve) {
-                std::vector<GemmTask<float>> tsv, rest;
-                for (auto &g : simt) (ts_eligible(g) ? tsv : rest).push_back(g);
-                if (!tsv.empty()) {
+                // blocks TMA can address (16-byte aligned, even stride) and the rest:
+                // one tall-skinny launch each
+                std::vector<GemmTask<float>> tsv[2], rest;
+                for (auto &g : simt) {
+                    if (!ts_eligible(g)) rest.push_back(g);
+                    else tsv[ts_tma_ok(g) ? 1 : 0].push_back(g);
+                }
+                for (int tma = 0; tma < 2; tma++) {
+                    if (tsv[tma].empty()) continue;
                     double fl = 0, by = 0;
-                    for (auto &g : tsv) { fl += 8.0 * g.M * (double)g.N * g.K; by += gemm_bytes(g); }
+                    for (auto &g : tsv[tma]) { fl += 8.0 * g.M * (double)g.N * g.K; by += gemm_bytes(g); }
                     const int idx = (int)sc.ts_pending.size();
-                    sc.ts_pending.push_back(std::move(tsv));
+                    sc.ts_pending.push_back(std::move(tsv[tma]));
+                    sc.ts_tma.push_back((char)tma);
                     Schedule<T> *psc = &sc;
                     sc.launches.push_back({[psc, idx](cudaStream_t st) { ts_expand(*psc->ts[idx], st); }, LK_SPLIT, 0});
                     sc.launches.push_back({[psc, idx, this](cudaStream_t st) { ts_mma(*psc->ts[idx], tc_err.p, st); },
@@ -318,9 +326,11 @@ public:
             int rc;
             if ((rc = sc.tsws.alloc(need))) return rc;
             sc.ts.clear();
-            for (auto &v : sc.ts_pending) {
+            for (size_t i = 0; i < sc.ts_pending.size(); i++) {
+                auto &v = sc.ts_pending[i];
                 sc.ts.emplace_back(new TsLaunch());
-                if ((rc = ts_build_launch(*sc.ts.back(), v.data(), (int)v.size(), sc.tsws.p))) return rc;
+                if ((rc = ts_build_launch(*sc.ts.back(), v.data(), (int)v.size(), sc.tsws.p, sc.ts_tma[i] != 0)))
+                    return rc;
             }
         }
         return WT3D_OK;

@@ -166,6 +166,7 @@ int symbolic_grid(int nx, int ny, int nz, int leaf_nodes, Symbolic &S)
     long long fac = 0;
     for (int f = 0; f < nf; f++) {
         Front &F = S.fronts[f];
+        fac += fac & 1;   // even offsets: 16-byte-aligned complex64 fronts (TMA-addressable blocks)
         F.fac_off = fac;
         fac += (long long)F.p * F.nf() + (long long)F.b * F.p;
         double p = F.p, b = F.b;

@@ -424,8 +424,10 @@ int tc_init()
 // through the tensor-core path (path = 1), the SIMT path (path = 0) or the
 // tall-skinny tensor-core kernel of the solves (path = 3; path = 4 with a row
 // gather of B and a row scatter of C; path = 5 with C -= A^H B for A given as
-// the K x M block, lda >= M).  wt3d_bench_gemm also times path 2,
-// the tall-skinny SIMT kernel, and path 3.
+// the K x M block, lda >= M); paths 3 and 4 stream A by TMA when it is
+// 16-byte aligned with an even stride.  wt3d_bench_gemm also times path 2,
+// the tall-skinny SIMT kernel, path 3, and path 6 (path 3 with A always
+// copied by the loader warps).
 // ---------------------------------------------------------------------------
 using namespace wt3d;
 extern "C" int wt3d_set_sm_reserve(int n)
@@ -479,7 +481,7 @@ extern "C" int wt3d_debug_gemm(int path, int M, int N, int K, const void *A, int
         DevVec<float> ws;
         if ((rc = ws.alloc(ts_workspace_floats(&g, 1)))) return rc;
         TsLaunch L;
-        if ((rc = ts_build_launch(L, &g, 1, ws.p))) return rc;
+        if ((rc = ts_build_launch(L, &g, 1, ws.p, ts_tma_ok(g)))) return rc;
         ts_expand(L, 0);
         ts_mma(L, err.p, 0);
     } else {
@@ -531,9 +533,11 @@ extern "C" int wt3d_bench_gemm(int path, int M, int N, int K, int iters, double 
         if ((rc = tc_init()) || (rc = ws.alloc(tc_workspace_floats(&g, 1))) || (rc = tc_build_launch(L, &g, 1, ws.p)))
             return rc;
         tc_split(L, 0);
-    } else if (path == 3) {
-        if (N > 32) { set_error("wt3d_bench_gemm: path 3 needs N <= 32"); return WT3D_ERR_ARG; }
-        if ((rc = ts_init()) || (rc = ws.alloc(ts_workspace_floats(&g, 1))) || (rc = ts_build_launch(LT, &g, 1, ws.p)))
+    } else if (path == 3 || path == 6) {
+        if (N > 32) { set_error("wt3d_bench_gemm: paths 3 and 6 need N <= 32"); return WT3D_ERR_ARG; }
+        const bool tma = path == 3 && ts_tma_ok(g);
+        if ((rc = ts_init()) || (rc = ws.alloc(ts_workspace_floats(&g, 1))) ||
+            (rc = ts_build_launch(LT, &g, 1, ws.p, tma)))
             return rc;
         ts_expand(LT, 0);
     } else {
@@ -548,7 +552,7 @@ extern "C" int wt3d_bench_gemm(int path, int M, int N, int K, int iters, double 
     if (path == 2 && N > TSBN) { set_error("wt3d_bench_gemm: path 2 needs N <= 32"); return WT3D_ERR_ARG; }
     auto launch = [&]() {
         if (path == 1) tc_mma(L, err.p, 0);
-        else if (path == 3) ts_mma(LT, err.p, 0);
+        else if (path == 3 || path == 6) ts_mma(LT, err.p, 0);
         else if (path == 2) k_gemm_ts<float><<<(unsigned)ts_tiles, 256>>>(dt.p, 1);
         else k_gemm<float><<<(unsigned)tiles, 256>>>(dt.p, 1);
     };

@@ -34,22 +34,24 @@ struct TsTask {
     int lda, ldb, ldc, M, N, K, Kr;
     int kchunk, nkc, atom;          // K-chunk per work unit, chunks, atomic epilogue
     int conjA;                      // A^H of the stored K x M block (lda its row stride)
-    int map0;                       // first of this task's 2 tensor maps
+    int map0;                       // first of this task's 3 tensor maps (B~ hi, B~ lo, raw A)
     long long unit0, b_work0;
 };
 
 struct TsLaunch {
     DevVec<TsTask> tasks;
-    DevVec<unsigned char> maps;    // CUtensorMap array (2 per task)
+    DevVec<unsigned char> maps;    // CUtensorMap array (3 per task)
     int ntasks = 0;
     long long units = 0, b_tiles = 0;
+    bool tma = false;              // A streamed by TMA (every task 16-byte aligned with an even stride)
 };
 
 int tc_init();
 int ts_init();
 bool ts_eligible(const GemmTask<float> &g);
+bool ts_tma_ok(const GemmTask<float> &g);
 long long ts_workspace_floats(const GemmTask<float> *g, int n);
-int ts_build_launch(TsLaunch &L, const GemmTask<float> *g, int n, float *ws);
+int ts_build_launch(TsLaunch &L, const GemmTask<float> *g, int n, float *ws, bool tma);
 void ts_expand(const TsLaunch &L, cudaStream_t st);
 void ts_mma(const TsLaunch &L, int *err, cudaStream_t st);
 bool tc_eligible(const GemmTask<float> &g);

@@ -153,6 +153,28 @@ inline int make_map(CUtensorMap *m, float *base, long long rows, int Kr, int box
     return WT3D_OK;
 }
 
+// 2-D FP32 tensor map of rows x width floats with a row stride in bytes (a
+// multiple of 16), boxes of 32 floats x box_rows, no swizzle; reads outside the
+// tensor return zeros.
+inline int make_map_plain(CUtensorMap *m, const float *base, long long rows, long long width, long long stride_bytes,
+                          int box_rows)
+{
+    auto fn = encode_fn();
+    if (!fn) { set_error("cuTensorMapEncodeTiled unavailable"); return WT3D_ERR_CUDA; }
+    cuuint64_t gdim[2] = {(cuuint64_t)width, (cuuint64_t)rows};
+    cuuint64_t gstr[1] = {(cuuint64_t)stride_bytes};
+    cuuint32_t box[2] = {32u, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), gdim, gstr, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+        return WT3D_ERR_CUDA;
+    }
+    return WT3D_OK;
+}
+
 inline long long align_up(long long x, long long a) { return (x + a - 1) / a * a; }
 
 }  // namespace wt3d

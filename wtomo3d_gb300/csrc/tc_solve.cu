@@ -18,13 +18,16 @@
 //
 // Work unit = (task, 128-row tile, K-chunk); persistent CTAs, one per SM.
 // Warps 0-15 load and split A, warp 16 issues the TMA copies of B~ (and owns
-// the TMEM allocation), warp 17 (one lane) issues the MMAs, warps 18-21 drain
-// the double-buffered accumulator: C -= D in place, or with atomics when the
-// task is split along K or its rows are scattered (border updates).  Every
-// mbarrier wait is bounded; on expiry the kernel records an error code and
-// winds down as the square kernel does.
+// the TMEM allocation), warp 17 (one lane) issues the MMAs, warp 18 streams A
+// by TMA in the variant for 16-byte-aligned blocks with even strides (the
+// loaders then only convert), warps 19-22 drain the double-buffered
+// accumulator: C -= D in place, or with atomics when the task is split along K
+// or its rows are scattered (border updates).  Every mbarrier wait is bounded;
+// on expiry the kernel records an error code and winds down as the square
+// kernel does.
 #include "tc_gemm.h"
 #include "tc_ptx.cuh"
+#include <cstring>
 
 namespace wt3d {
 
@@ -42,10 +45,10 @@ constexpr int TS_RAW_BYTES = TS_BM * TS_KC * 8;   // 16 KB
 constexpr int TS_B_OFF = TS_STAGES * TS_ASTAGE_BYTES;
 constexpr int TS_RAW_OFF = TS_B_OFF + TS_BSTAGES * TS_BSTAGE_BYTES;
 constexpr int TS_BAR_OFF = TS_RAW_OFF + TS_RAW * TS_RAW_BYTES;
-constexpr int TS_SMEM = TS_BAR_OFF + 1024 + 256;
+constexpr int TS_SMEM = TS_BAR_OFF + 1024 + 512;
 constexpr int TS_LOADERS = 16;                    // loader warps
-constexpr int TS_WB = TS_LOADERS, TS_WM = TS_LOADERS + 1, TS_WE = TS_LOADERS + 2;
-constexpr int TS_THREADS = (TS_LOADERS + 6) * 32; // + B producer, MMA, 4 epilogue warps
+constexpr int TS_WB = TS_LOADERS, TS_WM = TS_LOADERS + 1, TS_WA = TS_LOADERS + 2, TS_WE = TS_LOADERS + 3;
+constexpr int TS_THREADS = (TS_LOADERS + 7) * 32; // + B producer, MMA, A producer (TMA variant), 4 epilogue warps
 constexpr int TS_LT = TS_LOADERS * 32;            // loader threads
 constexpr int TS_PER_THREAD = TS_BM * TS_KC / TS_LT;   // complex elements per loader thread per stage
 constexpr int TS_QROWS = TS_LT / TS_KC;           // rows between a thread's elements
@@ -207,6 +210,11 @@ __device__ __forceinline__ void split_cvt(float x, float &hi, float &lo)
     lo = __uint_as_float(lw);
 }
 
+// TMA = false: loaders copy A with cp.async (any alignment, as stored or
+// conjugate-transposed).  TMA = true: every task's A is 16-byte aligned with an
+// even row stride, as stored; warp TS_WA streams raw 128 x 16 complex tiles of
+// A into the ring by TMA and the loaders only convert.
+template <bool TMA>
 __global__ void __launch_bounds__(TS_THREADS, 1)
     k_tc_ts(const TsTask *__restrict__ tasks, int ntasks, long long nunits, const CUtensorMap *__restrict__ maps,
             int *err)
@@ -220,7 +228,9 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
     uint64_t *tfull = bempty + TS_BSTAGES;
     uint64_t *tempty = tfull + 2;
     uint64_t *drain = tempty + 2;
-    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(drain + 1);
+    uint64_t *rfull = drain + 1;                                         // raw A slot landed (TMA variant)
+    uint64_t *rempty = rfull + TS_RAW;                                   // raw A slot converted (loader warps)
+    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(rempty + TS_RAW);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == TS_WB) {
@@ -242,6 +252,10 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
             mbar_init(&tempty[b], 4);
         }
         mbar_init(drain, 1);
+        for (int s = 0; s < TS_RAW; s++) {
+            mbar_init(&rfull[s], 1);
+            mbar_init(&rempty[s], TS_LOADERS);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -258,25 +272,32 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
         uint8_t *rawb = smem + TS_RAW_OFF;
         const uint32_t raw0 = smem_u32(rawb);
         TsCursor cp, cs;
-        ts_cursor_at(cp, tasks, ntasks, nunits, blockIdx.x, l);
         ts_cursor_at(cs, tasks, ntasks, nunits, blockIdx.x, l);
         long long gc = 0, g = 0;
-        for (int p = 0; p < TS_RAW - 1; p++, gc++) {
-            if (cp.valid) {
-                ts_issue(cp, l, raw0 + (uint32_t)((gc % TS_RAW) * TS_RAW_BYTES));
-                ts_cursor_next(cp, tasks, ntasks, nunits, l);
+        if constexpr (!TMA) {
+            ts_cursor_at(cp, tasks, ntasks, nunits, blockIdx.x, l);
+            for (int p = 0; p < TS_RAW - 1; p++, gc++) {
+                if (cp.valid) {
+                    ts_issue(cp, l, raw0 + (uint32_t)((gc % TS_RAW) * TS_RAW_BYTES));
+                    ts_cursor_next(cp, tasks, ntasks, nunits, l);
+                }
+                asm volatile("cp.async.commit_group;" ::: "memory");
             }
-            asm volatile("cp.async.commit_group;" ::: "memory");
         }
         while (cs.valid) {
-            if (cp.valid) {
-                ts_issue(cp, l, raw0 + (uint32_t)((gc % TS_RAW) * TS_RAW_BYTES));
-                ts_cursor_next(cp, tasks, ntasks, nunits, l);
+            const int slot = (int)(g % TS_RAW);
+            if constexpr (!TMA) {
+                if (cp.valid) {
+                    ts_issue(cp, l, raw0 + (uint32_t)((gc % TS_RAW) * TS_RAW_BYTES));
+                    ts_cursor_next(cp, tasks, ntasks, nunits, l);
+                }
+                asm volatile("cp.async.commit_group;" ::: "memory");
+                gc++;
+                asm volatile("cp.async.wait_group %0;" ::"n"(TS_RAW - 1) : "memory");   // stage g has landed
+            } else {
+                if (!mbar_wait(&rfull[slot], (uint32_t)((g / TS_RAW) & 1))) { atomicCAS(err, 0, 16); break; }
             }
-            asm volatile("cp.async.commit_group;" ::: "memory");
-            gc++;
-            asm volatile("cp.async.wait_group %0;" ::"n"(TS_RAW - 1) : "memory");   // stage g has landed
-            const float2 *rv = reinterpret_cast<const float2 *>(rawb + (g % TS_RAW) * TS_RAW_BYTES);
+            const uint8_t *rs = rawb + slot * TS_RAW_BYTES;
             const int s = (int)(g % TS_STAGES);
             const uint32_t ph = (uint32_t)((g / TS_STAGES) & 1) ^ 1u;
             if (!mbar_wait(&empty[s], ph)) { atomicCAS(err, 0, 11); break; }
@@ -286,7 +307,12 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
 #pragma unroll
             for (int q = 0; q < TS_PER_THREAD; q++) {
                 float2 v = make_float2(0.f, 0.f);
-                if (q < nq) v = rv[q * TS_LT + l];
+                if (q < nq) {
+                    if constexpr (TMA)   // the TMA box: row r of the stage at r * 128 bytes
+                        v = *reinterpret_cast<const float2 *>(rs + (TS_QROWS * q + (l >> 4)) * 128 + (l & 15) * 8);
+                    else                 // the thread's own slots raw[q][l]
+                        v = reinterpret_cast<const float2 *>(rs)[q * TS_LT + l];
+                }
                 v.y *= ysign;
                 const int off = cs.conj ? ts_swz(l & (TS_BM - 1), cs.kq + q * (TS_LT / TS_BM))
                                         : ts_swz(TS_QROWS * q + (l >> 4), l & 15);
@@ -299,11 +325,14 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
             // generic-proxy stores become visible to the tensor core's async proxy
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
-            if (lane == 0) mbar_arrive(&full[s]);
+            if (lane == 0) {
+                mbar_arrive(&full[s]);
+                if constexpr (TMA) mbar_arrive(&rempty[slot]);
+            }
             ts_cursor_next(cs, tasks, ntasks, nunits, l);
             g++;
         }
-        asm volatile("cp.async.wait_all;" ::: "memory");   // no copy into shared memory outlives the CTA
+        if constexpr (!TMA) asm volatile("cp.async.wait_all;" ::: "memory");   // no copy into shared memory outlives the CTA
     } else if (warp == TS_WB && lane == 0) {
         // ---------------- B~ producer (TMA) ----------------
         long long g = 0;
@@ -328,6 +357,30 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
             if (g <= s) continue;
             const long long last = g - 1 - ((g - 1 - s) % TS_BSTAGES);
             mbar_wait(&bfull[s], (uint32_t)((last / TS_BSTAGES) & 1));
+        }
+    } else if (TMA && warp == TS_WA && lane == 0) {
+        // ---------------- raw A producer (TMA variant) ----------------
+        uint8_t *rawb = smem + TS_RAW_OFF;
+        long long g = 0;
+        bool ok = true;
+        for (long long u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
+            int m0, k0, k1;
+            const TsTask *t = ts_unit(tasks, ntasks, u, m0, k0, k1);
+            const CUtensorMap *mp = maps + t->map0 + 2;
+            const int nsub = (k1 - k0 + TS_KC - 1) / TS_KC;
+            for (int i = 0; i < nsub; i++, g++) {
+                const int slot = (int)(g % TS_RAW);
+                if (!mbar_wait(&rempty[slot], (uint32_t)((g / TS_RAW) & 1) ^ 1u)) { atomicCAS(err, 0, 17); ok = false; break; }
+                mbar_expect_tx(&rfull[slot], TS_RAW_BYTES);
+                // x: real column, a multiple of 32 floats (128 bytes); rows past M and columns
+                // past K read as zeros
+                tma_load_2d(rawb + slot * TS_RAW_BYTES, mp, 2 * (k0 + i * TS_KC), m0, &rfull[slot]);
+            }
+        }
+        for (int s = 0; s < TS_RAW; s++) {
+            if (g <= s) continue;
+            const long long last = g - 1 - ((g - 1 - s) % TS_RAW);
+            mbar_wait(&rfull[s], (uint32_t)((last / TS_RAW) & 1));
         }
     } else if (warp == TS_WM && lane == 0) {
         // ---------------- MMA issuer ----------------
@@ -454,6 +507,12 @@ bool ts_eligible(const GemmTask<float> &g)
     return g.N <= 32 && g.M >= TS_BM && g.K >= 256;
 }
 
+bool ts_tma_ok(const GemmTask<float> &g)
+{
+    // TMA needs a 16-byte-aligned start and a row stride that is a multiple of 16 bytes
+    return !g.conjA && ((uintptr_t)g.A % 16) == 0 && (g.lda % 2) == 0;
+}
+
 static long long ts_kr(int K) { return align_up(2LL * K, 64); }   // whole 32-complex tiles of B~
 
 long long ts_workspace_floats(const GemmTask<float> *g, int n)
@@ -463,10 +522,11 @@ long long ts_workspace_floats(const GemmTask<float> *g, int n)
     return w;
 }
 
-int ts_build_launch(TsLaunch &L, const GemmTask<float> *g, int n, float *ws)
+int ts_build_launch(TsLaunch &L, const GemmTask<float> *g, int n, float *ws, bool tma)
 {
     std::vector<TsTask> tasks(n);
-    std::vector<CUtensorMap> maps(2 * n);
+    std::vector<CUtensorMap> maps(3 * n);
+    memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
     // K-chunk so that the launch has about four units per resident CTA
     double work = 0;
     for (int i = 0; i < n; i++) work += (double)((g[i].M + TS_BM - 1) / TS_BM) * g[i].K;
@@ -490,12 +550,19 @@ int ts_build_launch(TsLaunch &L, const GemmTask<float> *g, int n, float *ws)
         units += (long long)((t.M + TS_BM - 1) / TS_BM) * t.nkc;
         t.b_work0 = bw;
         bw += t.Kr / 64;
-        t.map0 = 2 * i;
+        t.map0 = 3 * i;
         int rc;
-        if ((rc = make_map(&maps[2 * i], t.bhi, TS_NR, t.Kr, TS_NR)) ||
-            (rc = make_map(&maps[2 * i + 1], t.blo, TS_NR, t.Kr, TS_NR)))
+        if ((rc = make_map(&maps[3 * i], t.bhi, TS_NR, t.Kr, TS_NR)) ||
+            (rc = make_map(&maps[3 * i + 1], t.blo, TS_NR, t.Kr, TS_NR)))
             return rc;
+        if (tma) {
+            if (!ts_tma_ok(g[i])) { set_error("ts_build_launch: task not addressable by TMA"); return WT3D_ERR_ARG; }
+            if ((rc = make_map_plain(&maps[3 * i + 2], reinterpret_cast<const float *>(t.A), t.M, 2LL * t.K,
+                                     8LL * t.lda, TS_BM)))
+                return rc;
+        }
     }
+    L.tma = tma;
     L.ntasks = n;
     L.units = units;
     L.b_tiles = bw;
@@ -517,13 +584,15 @@ void ts_mma(const TsLaunch &L, int *err, cudaStream_t st)
 {
     if (L.ntasks == 0) return;
     const long long grid = std::min<long long>(L.units, ts_sms());
-    k_tc_ts<<<(unsigned)grid, TS_THREADS, TS_SMEM, st>>>(L.tasks.p, L.ntasks, L.units,
-                                                         reinterpret_cast<const CUtensorMap *>(L.maps.p), err);
+    const CUtensorMap *maps = reinterpret_cast<const CUtensorMap *>(L.maps.p);
+    if (L.tma) k_tc_ts<true><<<(unsigned)grid, TS_THREADS, TS_SMEM, st>>>(L.tasks.p, L.ntasks, L.units, maps, err);
+    else k_tc_ts<false><<<(unsigned)grid, TS_THREADS, TS_SMEM, st>>>(L.tasks.p, L.ntasks, L.units, maps, err);
 }
 
 int ts_init()
 {
-    WT_CUDA(cudaFuncSetAttribute(k_tc_ts, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM));
+    WT_CUDA(cudaFuncSetAttribute(k_tc_ts<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM));
+    WT_CUDA(cudaFuncSetAttribute(k_tc_ts<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM));
     if (!encode_fn()) { set_error("cuTensorMapEncodeTiled unavailable"); return WT3D_ERR_CUDA; }
     return WT3D_OK;
 }

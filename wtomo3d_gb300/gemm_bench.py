@@ -1,7 +1,8 @@
 """Microbenchmark of the front-update GEMM C -= A B (complex64, row-major)
 through the tcgen05 kernel (path 1), the SIMT kernel (path 0) or the
 tall-skinny SIMT kernel of the solves (path 2, N <= 32) or the tall-skinny
-tcgen05 kernel of the solves (path 3, N <= 32), on random operands
+tcgen05 kernel of the solves (path 3, N <= 32; A by TMA when aligned, path 6
+with A always copied by the loader warps), on random operands
 resident on the device:
 
     python -m wtomo3d_gb300.gemm_bench M N K [--path 1] [--reps 5]
@@ -24,7 +25,7 @@ def main():
     ap.add_argument("M", type=int)
     ap.add_argument("N", type=int)
     ap.add_argument("K", type=int)
-    ap.add_argument("--path", type=int, default=1, choices=[0, 1, 2, 3])
+    ap.add_argument("--path", type=int, default=1, choices=[0, 1, 2, 3, 6])
     ap.add_argument("--reps", type=int, default=5)
     a = ap.parse_args()
     import wtomo3d_gb300 as wt
@@ -35,7 +36,7 @@ def main():
     if rc:
         raise SystemExit("wt3d_bench_gemm failed (%d): %s" % (rc, L.wt3d_last_error().decode()))
     fl = 8.0 * a.M * a.N * a.K
-    print(json.dumps({"M": a.M, "N": a.N, "K": a.K, "path": ["simt", "tcgen05", "simt-tall-skinny", "tcgen05-tall-skinny"][a.path], "ms": ms.value,
+    print(json.dumps({"M": a.M, "N": a.N, "K": a.K, "path": {0: "simt", 1: "tcgen05", 2: "simt-tall-skinny", 3: "tcgen05-tall-skinny", 6: "tcgen05-tall-skinny-copies"}[a.path], "ms": ms.value,
                       "tflops": fl / ms.value / 1e9, "a_gbs": 8.0 * a.M * a.K / ms.value / 1e6}))
 
 
