@@ -37,6 +37,12 @@ def test_rhs_sources_and_receivers():
                     node, w = wt.source_weights(g, *xyz[r], ireg, sprd)
                     for c in range(3):
                         assert abs(smp[j, r, c] - np.dot(w, U[j, 3 * node + c])) < 1e-12
+            # receiver responses and inactive pairs (makeuh.f:92-103)
+            resp = np.array([1.0, 0.5j, -2.0])
+            act = np.array([[1, 0, 1], [1, 1, 0]])
+            smr = s.sample_receivers(dU.data_ptr(), 2, xyz, ireg, sprd, response=resp, active=act)
+            np.testing.assert_allclose(smr, np.where(act[:, :, None] != 0, smp * resp[None, :, None], 0),
+                                       rtol=1e-12, atol=1e-14 * np.abs(smp).max())
             del F, dU
 
 
@@ -55,6 +61,9 @@ def test_pressure_matches_makeuh_restatement():
         dU = torch.from_numpy(U).cuda()
         for ireg in (0, 3):
             got = s.sample_pressure(dU.data_ptr(), 2, xyz, ireg, 0.5)
+            act = np.array([[1, 0], [0, 1]])
+            np.testing.assert_allclose(s.sample_pressure(dU.data_ptr(), 2, xyz, ireg, 0.5, active=act),
+                                       np.where(act != 0, got, 0), rtol=1e-12, atol=1e-14 * np.abs(got).max())
             for j in range(2):
                 for r in range(2):
                     x, y, z = xyz[r]

@@ -318,21 +318,29 @@ class Solver:
         _check(lib().wt3d_rhs_sources(self._h, len(comp), _ptr(xyz), _ptr(comp), None if st is None else _ptr(st),
                                       int(ireg), float(sprd), ctypes.c_void_p(d_F)))
 
-    def sample_receivers(self, d_U, nrhs, xyz, ireg=0, sprd=0.5):
-        """Three-component receiver samples, shape (nrhs, nrec, 3)."""
+    def sample_receivers(self, d_U, nrhs, xyz, ireg=0, sprd=0.5, response=None, active=None):
+        """Three-component receiver samples, shape (nrhs, nrec, 3); optionally
+        times the receiver responses at this frequency (nrec,) and zero for
+        inactive source-receiver pairs active[nrhs, nrec] == 0 (makeuh.f:76-104;
+        see wtomo3d_gb300.receivers)."""
+        from . import receivers
         xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
         out = np.zeros((nrhs, len(xyz), 3), np.complex128)
         _check(lib().wt3d_sample_receivers(self._h, int(nrhs), ctypes.c_void_p(d_U), len(xyz), _ptr(xyz), int(ireg),
                                            float(sprd), _ptr(out)))
-        return out
+        if response is None and active is None:
+            return out
+        return receivers.apply_geophone_response(out, response, active)
 
-    def sample_pressure(self, d_U, nrhs, xyz, ireg=0, sprd=0.5):
-        """Hydrophone pressure (makeuh.f), shape (nrhs, nrec)."""
+    def sample_pressure(self, d_U, nrhs, xyz, ireg=0, sprd=0.5, active=None):
+        """Hydrophone pressure (makeuh.f), shape (nrhs, nrec); zero for
+        inactive source-hydrophone pairs active[nrhs, nrec] == 0."""
+        from . import receivers
         xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
         out = np.zeros((nrhs, len(xyz)), np.complex128)
         _check(lib().wt3d_sample_pressure(self._h, int(nrhs), ctypes.c_void_p(d_U), len(xyz), _ptr(xyz), int(ireg),
                                           float(sprd), _ptr(out)))
-        return out
+        return out if active is None else receivers.apply_hydrophone_mask(out, active)
 
     def apply_device(self, d_X, d_Y, nrhs):
         """Y = A X on device arrays (column-major n x nrhs complex128)."""
