@@ -459,16 +459,16 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
                             }
                     } else {
 #pragma unroll
-                        for (int c0 = 0; c0 < 16; c0 += 8) {   // 8 loads in flight per group
+                        for (int g8 = 0; g8 < 16; g8 += 8) {   // 8 loads in flight per group
                             cx<float> cv[8];
 #pragma unroll
                             for (int c = 0; c < 8; c++)
-                                if (c0 + c < nc) cv[c] = p[c0 + c];
+                                if (g8 + c < nc) cv[c] = p[g8 + c];
 #pragma unroll
                             for (int c = 0; c < 8; c++)
-                                if (c0 + c < nc)
-                                    p[c0 + c] = cx<float>(cv[c].re - __uint_as_float(v[2 * (c0 + c)]),
-                                                          cv[c].im - __uint_as_float(v[2 * (c0 + c) + 1]));
+                                if (g8 + c < nc)
+                                    p[g8 + c] = cx<float>(cv[c].re - __uint_as_float(v[2 * (g8 + c)]),
+                                                          cv[c].im - __uint_as_float(v[2 * (g8 + c) + 1]));
                         }
                     }
                 }
