@@ -62,6 +62,34 @@ def test_structure(dims, leaf):
     np.testing.assert_allclose(e["flops"], (8 * (p ** 3 / 3 + p * p * b + p * b * b)).sum(), rtol=1e-12)
 
 
+def test_tma_addressable_substitution_blocks():
+    """96x96x64: fronts start at even offsets, so a substitution block is
+    16-byte aligned exactly when its stride is even (L21: p, U12: p + b).
+    Among the blocks the tall-skinny tensor-core kernel takes (M >= 128,
+    K >= 256), about half of the bytes qualify for TMA (49 %)."""
+    e = export(96, 96, 64)
+    p, b = e["p"].astype(np.int64), e["b"].astype(np.int64)
+    fac, off = 0, []
+    for pf, bf in zip(p.tolist(), b.tolist()):
+        fac += fac & 1
+        off.append(fac)
+        fac += pf * (pf + bf) + bf * pf
+    off = np.array(off)
+    assert e["info"][1] == fac
+    tot = ok = 0
+    for f in range(len(p)):
+        pf, bf = int(p[f]), int(b[f])
+        if bf >= 128 and pf >= 256:   # forward border update: L21 (b x p, stride p)
+            base = off[f] + pf * (pf + bf)
+            tot += bf * pf
+            ok += bf * pf if (base % 2 == 0 and pf % 2 == 0) else 0
+        if pf >= 128 and bf >= 256:   # backward: U12 (p x b, stride p + b)
+            base = off[f] + pf
+            tot += bf * pf
+            ok += bf * pf if (base % 2 == 0 and (pf + bf) % 2 == 0) else 0
+    assert tot > 0 and 0.45 < ok / tot < 0.55, ok / tot
+
+
 def test_top_separator_size():
     # 96x96x64: the first cut is the x = 48 plane, 96*64 nodes = 18432 dofs
     e = export(96, 96, 64)
