@@ -203,3 +203,40 @@ def test_dispersion_oracle_limits(oracle):
     aq, _ = oracle.assemble_q(g, vp, vs, rho, q, q, 3.0, om, ir)
     assert np.abs(aq.imag).max() > 1e-4 * np.abs(a0).max()          # attenuation present
     assert np.abs(aq.real - a0.real).max() <= 1e-3 * np.abs(a0).max()  # (1 - i q/2)^2: real part 1 - q^2/4
+
+
+def test_pml_without_damping_is_the_interior_stencil(oracle):
+    """The reference's PML fidelity hooks (fdfd3d.f:56-57, pml3d.f:297-304):
+    with zero damping (pmlr = 1, so pmlf = 3 ln(1/pmlr) / (2 pmld^3) = 0,
+    hence r1 = 1 and r2 = 0) every row inside a 6-node PML equals the same row
+    assembled as an interior row (a grid whose PML is only the boundary
+    layer), bit for bit.  omega is real, so the REAL(omega^2) quirk of the
+    interior mass terms (pfdfd3d.f:140-142) cannot differ."""
+    import scipy.sparse as sp
+    nx, ny, nz, dx = 14, 13, 12, 20.0
+    vp, vs, rho = model.layered_random(nx, ny, nz, dx, seed=3)
+    om = 2 * np.pi * 1.3
+    ir, jc = oracle.pattern(nx, ny, nz)
+    g_pml = Grid(nx, ny, nz, dx, pmld=5 * dx, pmlr=1.0, fst=0)
+    g_int = Grid(nx, ny, nz, dx, pmld=0.5 * dx, pmlr=1.0, fst=0)
+    assert g_pml.pml()[1] == 0.0 and g_pml.pml()[2] == 6 and g_int.pml()[2] == 1
+    a_pml, e1 = oracle.assemble(g_pml, vp, vs, rho, om, ir)
+    a_int, e2 = oracle.assemble(g_int, vp, vs, rho, om, ir)
+    assert e1 == 0 and e2 == 0
+    n = g_pml.n
+    A = sp.csr_matrix((a_pml, jc - 1, ir - 1), shape=(n, n))
+    B = sp.csr_matrix((a_int, jc - 1, ir - 1), shape=(n, n))
+    rows = []
+    for iy in range(2, ny):
+        for ix in range(2, nx):
+            for iz in range(2, nz):
+                if min(ix, iy, iz) <= 6 or ix > nx - 6 or iy > ny - 6 or iz > nz - 6:
+                    g = (iz - 1) + nz * (ix - 1) + nz * nx * (iy - 1)
+                    rows += [3 * g, 3 * g + 1, 3 * g + 2]
+    rows = np.array(rows)
+    assert rows.size > 3000
+    assert (A[rows] != B[rows]).nnz == 0
+    # with damping the same rows do differ: the comparison has teeth
+    a_damped, _ = oracle.assemble(Grid(nx, ny, nz, dx, pmld=5 * dx, fst=0), vp, vs, rho, om, ir)
+    D = sp.csr_matrix((a_damped, jc - 1, ir - 1), shape=(n, n))
+    assert (D[rows] != B[rows]).nnz > 0
