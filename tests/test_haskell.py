@@ -48,3 +48,21 @@ def test_library_haskgrn_matches_oracle(oracle, s_wave, f):
     assert np.abs(U - Uo).max() <= 1e-12 * scale
     assert np.abs(W - Wo).max() <= 1e-12 * scale
     assert np.all(np.isfinite(U)) and np.all(np.isfinite(W))
+
+
+def test_node_above_model_top_is_rejected(oracle):
+    """The reference's dloc < 0 guard (haskgrn.f:435-440): a node depth above
+    the top of the 1-D model is an error in the oracle and in the library;
+    the same model starting at the surface is accepted."""
+    import ctypes
+    vp, vs, rho, zt = halfspace()
+    zt_low = zt + 50.0                 # model top 50 m below the surface
+    arr = [np.ascontiguousarray(a, np.float64) for a in (vp, vs, rho, zt_low)]
+    U = np.zeros(4, np.complex128)
+    W = np.zeros(4, np.complex128)
+    p = lambda a: ctypes.c_void_p(a.ctypes.data)
+    rc = oracle.L.ora_haskgrn(2, *[p(a) for a in arr], 2 * np.pi, np.radians(10.0), 0, 4, 20.0, 0.0, p(U), p(W))
+    assert rc != 0
+    with pytest.raises(wt.WT3DError):
+        wt.haskgrn(wt.Layered1D(vp, vs, rho, zt_low), 2 * np.pi, np.radians(10.0), 4, 20.0)
+    wt.haskgrn(wt.Layered1D(vp, vs, rho, zt), 2 * np.pi, np.radians(10.0), 4, 20.0)
