@@ -65,6 +65,18 @@ void strumpack_serial_finter(int *job, int *nrows, int *nnz,
                              float _Complex *rhs, float _Complex *sol,
                              int *ierr);
 
+/* Refinement target of job 3 (default relative residual 1e-10 within 20
+ * substitution passes).  The reference sets its refinement tolerances once,
+ * at job 1 (STRUMPACK_set_rctol / set_actol, strumpack_finter.c:38-39),
+ * and a caller cannot change them; this setter serves the same purpose.
+ * Job 3 sets *ierr = 1 and prints the residual reached when the target is
+ * missed, and still returns that last iterate in sol.  Returns WT3D_ERR_ARG
+ * for tol <= 0 or maxit < 0. */
+int wt3d_finter_set_refinement(double tol, int maxit);
+/* Relative residual ||b - A x|| / ||b|| (FP64, assembled operator) that the
+ * last job-3 call reached. */
+double wt3d_finter_last_relres(void);
+
 /* ---- pattern and assembly ----------------------------------------------
  * wt3d_pattern replaces srel3d_getsize + srel3d + SPARSE_ADJ2CRS
  * (srgraphs.f:626-734, sparse.f:13-49).  n = 3*nx*ny*nz, nnz =

@@ -87,3 +87,12 @@ def test_too_large_grid_is_rejected_before_any_device_work():
     with pytest.raises(wt.WT3DError) as e:
         wt.Solver(wt.Grid(1, 5, 5, 10.0))
     assert e.value.code == wt.WT3D_ERR_ARG
+
+
+def test_finter_refinement_setter_rejects_bad_arguments():
+    """The drop-in's refinement setter checks its arguments on the host."""
+    L = wt.lib()
+    L.wt3d_finter_set_refinement.argtypes = [ctypes.c_double, ctypes.c_int]
+    assert L.wt3d_finter_set_refinement(0.0, 5) == wt.WT3D_ERR_ARG
+    assert L.wt3d_finter_set_refinement(1e-8, -1) == wt.WT3D_ERR_ARG
+    assert L.wt3d_finter_set_refinement(1e-10, 20) == 0

@@ -2,6 +2,8 @@
 oracle assembles, the mixed-precision refinement reaching its tolerance, the
 FP64 path, the adjoint solve, many right-hand sides, and the
 strumpack_serial_finter job protocol."""
+import ctypes
+
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -163,6 +165,18 @@ def test_strumpack_job_protocol(oracle):
         xr = spla.spsolve(A.tocsc(), rhs.astype(np.complex128))
         err = np.linalg.norm(sol - xr) / np.linalg.norm(xr)
         assert err <= 1e-6, err     # complex64 output, FP64-refined
+        assert wt.lib().wt3d_finter_last_relres() <= 1e-10
+    # a refinement target that one pass cannot reach is a failed solve
+    # (ierr = 1) that still returns its iterate
+    L = wt.lib()
+    assert L.wt3d_finter_set_refinement(ctypes.c_double(1e-16), 1) == 0
+    try:
+        sol = np.zeros(n, np.complex64)
+        assert wt.strumpack_serial_finter(3, n, nnz, ir, jc, a64, rhs, sol) == 1
+        assert L.wt3d_finter_last_relres() > 1e-16
+        assert np.linalg.norm(sol - xr) <= 1e-3 * np.linalg.norm(xr)
+    finally:
+        assert L.wt3d_finter_set_refinement(ctypes.c_double(1e-10), 20) == 0
     assert wt.strumpack_serial_finter(-1, n, nnz, ir, jc, a0, dummy, dummy.copy()) == 0
     np.testing.assert_array_equal(ir, ir0)
     np.testing.assert_array_equal(jc, jc0)

@@ -61,6 +61,34 @@ def test_noalloc_matches_allocating_entry_point_twice():
         assert (np.abs(out - exact) / scale).max() < 1e-6 + 3e-7 * np.sqrt(K)
 
 
+def test_noalloc_strided_operands_on_a_caller_stream():
+    """Leading dimensions wider than the operands (views into wider arrays)
+    and a caller stream: the product matches, and the padding columns of C
+    are left as they were."""
+    import torch
+    L = _lib()
+    M, N, K = 200, 140, 96
+    lda, ldb, ldc = K + 24, N + 12, N + 20
+    r = np.random.default_rng(7)
+    cplx = lambda *sh: (r.standard_normal(sh) + 1j * r.standard_normal(sh)).astype(np.complex64)
+    Aw, Bw, Cw = cplx(M, lda), cplx(K, ldb), cplx(M, ldc)
+    A, B, C = Aw[:, :K], Bw[:, :N], Cw[:, :N]
+    ref = _allocating_reference(L, np.ascontiguousarray(A), np.ascontiguousarray(B), C)
+    dA, dB, dC = (torch.from_numpy(x).cuda() for x in (Aw, Bw, Cw))
+    st = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    for _ in range(2):
+        dC.copy_(torch.from_numpy(Cw))
+        torch.cuda.synchronize()
+        rc = L.wt3d_gemm_noalloc(M, N, K, ctypes.c_void_p(dA.data_ptr()), lda, ctypes.c_void_p(dB.data_ptr()), ldb,
+                                 ctypes.c_void_p(dC.data_ptr()), ldc, ctypes.c_void_p(st.cuda_stream))
+        assert rc == 0, L.wt3d_last_error()
+        out = dC.cpu().numpy()
+        scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64) + np.abs(C)
+        assert (np.abs(out[:, :N] - ref) / scale).max() < 1e-6 + 3e-7 * np.sqrt(K)
+        assert np.array_equal(out[:, N:], Cw[:, N:]), "padding columns of C were written"
+
+
 def test_noalloc_rejects_oversized_problem():
     L = _lib()
     lim = L.wt3d_gemm_noalloc_max_floats()

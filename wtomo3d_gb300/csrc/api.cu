@@ -1400,6 +1400,28 @@ int wt3d_solver_bytes(const wt3d_grid *g, int precision, double *out)
 static wt3d_solver *g_sp = nullptr;
 static bool g_sp_factored = false;
 static std::mutex g_sp_mu;
+// job 3's refinement target, iteration limit and the residual it last reached
+static double g_sp_tol = 1e-10;
+static int g_sp_maxit = 20;
+static double g_sp_relres = 0.0;
+
+int wt3d_finter_set_refinement(double tol, int maxit)
+{
+    if (!(tol > 0) || maxit < 0) {
+        set_error("wt3d_finter_set_refinement: need tol > 0 and maxit >= 0");
+        return WT3D_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lock(g_sp_mu);
+    g_sp_tol = tol;
+    g_sp_maxit = maxit;
+    return WT3D_OK;
+}
+
+double wt3d_finter_last_relres(void)
+{
+    std::lock_guard<std::mutex> lock(g_sp_mu);
+    return g_sp_relres;
+}
 
 void strumpack_serial_finter(int *job, int *nrows, int *nnz, int *irptr, int *jcptr, float _Complex *a,
                              float _Complex *rhs, float _Complex *sol, int *ierr)
@@ -1440,14 +1462,22 @@ void strumpack_serial_finter(int *job, int *nrows, int *nnz, int *irptr, int *jc
         for (long long i = 0; i < n; i++) b[i] = std::complex<double>(r[i]);
         double rr = 0;
         int rc = wt3d_solve(g_sp, 1, reinterpret_cast<double _Complex *>(b.data()),
-                            reinterpret_cast<double _Complex *>(x.data()), 1e-10, 20, &rr, nullptr);
+                            reinterpret_cast<double _Complex *>(x.data()), g_sp_tol, g_sp_maxit, &rr, nullptr);
+        g_sp_relres = rr;
         if (rc != WT3D_OK && rc != WT3D_ERR_NOCONV) {
             printf("%s: Error in solution phase1\n", fcnm);
             *ierr = 1;
             return;
         }
+        // the last iterate is returned either way; a solve that missed the
+        // refinement target is a failed solve for the caller
         std::complex<float> *s = reinterpret_cast<std::complex<float> *>(sol);
         for (long long i = 0; i < n; i++) s[i] = std::complex<float>(x[i]);
+        if (rc == WT3D_ERR_NOCONV) {
+            printf("%s: Error in solution phase1: relative residual %.3e after %d refinement steps, target %.1e\n",
+                   fcnm, rr, g_sp_maxit, g_sp_tol);
+            *ierr = 1;
+        }
     } else if (*job == -1) {
         if (g_sp) wt3d_solver_destroy(g_sp);
         g_sp = nullptr;

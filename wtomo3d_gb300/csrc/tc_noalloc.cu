@@ -13,7 +13,9 @@
 // The scratch array holds NOALLOC_MAX_FLOATS floats (64 MiB); every GPU on
 // which this library is loaded keeps it for the life of the process.  All calls
 // share it, so calls that overlap on the GPU (from different streams or
-// threads) race: serialise them.  The first call on a device looks up the
+// threads) race: serialise them.  The error word that reports an expired
+// pipeline wait is shared the same way: a call that overlaps another can
+// report the other's timeout or clear it.  The first call on a device looks up the
 // array's device address with that device current and caches it; make that
 // first call before relying on the entry point elsewhere.  The kernels here are
 // variants of the ones in tc_gemm.cu that take their single task and tensor
@@ -127,7 +129,9 @@ __global__ void __launch_bounds__(NB_THREADS, 1)
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + NB_STAGES * NB_STAGE_BYTES);
     uint64_t *empty = full + NB_STAGES;
     uint64_t *accum = empty + NB_STAGES;
-    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(accum + 1);
+    uint64_t *drain = accum + 1;
+    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(drain + 1);
+    int *epi_fail = reinterpret_cast<int *>(tmem_holder + 1);   // an epilogue warp's accumulator wait expired
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long lt = blockIdx.x;
     const int m0 = (int)(lt / t.tiles_n) * NB_BM, n0r = (int)(lt % t.tiles_n) * NB_BNR;
@@ -143,6 +147,8 @@ __global__ void __launch_bounds__(NB_THREADS, 1)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&empty[s])));
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(accum)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(drain)));
+        *epi_fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -151,9 +157,12 @@ __global__ void __launch_bounds__(NB_THREADS, 1)
     const uint32_t tmem = *tmem_holder;
     if (warp == 0 && lane == 0) {
         const CUtensorMap *maps[4] = {&mah, &mal, &mbh, &mbl};
+        int issued = 0;
         for (int ks = 0; ks < nk; ks++) {
             const int s = ks % NB_STAGES;
-            if (!bar_wait(&empty[s], ((ks / NB_STAGES) & 1) ^ 1)) atomicCAS(&g_err, 0, 1);
+            // an expired wait stops the producer; the MMA lane then times out in turn
+            if (!bar_wait(&empty[s], ((ks / NB_STAGES) & 1) ^ 1)) { atomicCAS(&g_err, 0, 1); break; }
+            issued = ks + 1;
             uint8_t *st = smem + s * NB_STAGE_BYTES;
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(&full[s])),
                          "r"(NB_STAGE_BYTES)
@@ -168,12 +177,20 @@ __global__ void __launch_bounds__(NB_THREADS, 1)
                     "l"((uint64_t)maps[q]), "r"(x), "r"(y[q]), "r"(su32(&full[s]))
                     : "memory");
         }
+        // the last copy issued into each stage has landed before the stage
+        // memory is reused by the epilogue or the CTA exits
+        for (int s = 0; s < NB_STAGES; s++) {
+            if (issued <= s) continue;
+            const int last = issued - 1 - ((issued - 1 - s) % NB_STAGES);
+            bar_wait(&full[s], (last / NB_STAGES) & 1);
+        }
     } else if (warp == 1 && lane == 0) {
         const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NB_BNR >> 3) << 17) |
                                ((uint32_t)(NB_BM >> 4) << 24);
+        bool ok = true;
         for (int ks = 0; ks < nk; ks++) {
             const int s = ks % NB_STAGES;
-            if (!bar_wait(&full[s], (ks / NB_STAGES) & 1)) atomicCAS(&g_err, 0, 2);
+            if (!bar_wait(&full[s], (ks / NB_STAGES) & 1)) { atomicCAS(&g_err, 0, 2); ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t base = su32(smem + s * NB_STAGE_BYTES);
             const uint32_t ah = base, al = base + NB_A_BYTES, bh = base + 2 * NB_A_BYTES, bl = bh + NB_B_BYTES;
@@ -193,17 +210,34 @@ __global__ void __launch_bounds__(NB_THREADS, 1)
                              su32(&empty[s]))
                          : "memory");
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(accum))
+        // the accumulator is complete only if every k-step was issued; on a
+        // timeout it is never signalled and the epilogue gives up in turn
+        if (ok)
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             su32(accum))
+                         : "memory");
+        // no MMA of this CTA is in flight once the drain barrier completes
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(drain))
                      : "memory");
+        bar_wait(drain, 0);
     } else if (warp >= 2) {
-        if (!bar_wait(accum, 0)) atomicCAS(&g_err, 0, 3);
+        if (!bar_wait(accum, 0)) {
+            atomicCAS(&g_err, 0, 3);
+            if (lane == 0) atomicOr(epi_fail, 1);
+        }
+        __syncwarp();
+        // every epilogue warp learns whether any of them gave up before the
+        // staged rows (written by other warps) are read or C is touched
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        const bool epi_ok = *(volatile int *)epi_fail == 0;
+        asm volatile("bar.sync 1, 128;" ::: "memory");
         asm volatile("tcgen05.fence::after_thread_sync;");
         const int q = warp & 3;
         const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16);
         float *stage = reinterpret_cast<float *>(smem);
         constexpr int EP = NB_BNR + 4;
         float *myrow = stage + (32 * q + lane) * EP;
-        for (int ch = 0; ch < NB_BNR / 32; ch++) {
+        for (int ch = 0; ch < NB_BNR / 32 && epi_ok; ch++) {
             uint32_t v[32];
             asm volatile(
                 "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"
@@ -222,7 +256,7 @@ __global__ void __launch_bounds__(NB_THREADS, 1)
         }
         asm volatile("bar.sync 1, 128;" ::: "memory");
         const int c0 = n0r / 2, ew = warp - 2;
-        for (int r = ew; r < NB_BM; r += 4) {
+        for (int r = ew; r < NB_BM && epi_ok; r += 4) {
             const int row = m0 + r;
             if (row >= t.M) break;
             cx<float> *crow = t.C + (long long)row * t.ldc + c0;
@@ -257,20 +291,26 @@ struct DeviceScratch {
 DeviceScratch g_dev[64];
 std::mutex g_mu;
 
+// Resolved once, under g_mu, by the first call on any device.
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+int resolve_encode()
+{
+    if (g_encode) return WT3D_OK;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+        set_error("cuTensorMapEncodeTiled unavailable");
+        return WT3D_ERR_CUDA;
+    }
+    g_encode = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    return WT3D_OK;
+}
+
 int encode(CUtensorMap *m, float *base, long long rows, int Kr, int box_rows)
 {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
-                cudaSuccess ||
-            q != cudaDriverEntryPointSuccess) {
-            set_error("cuTensorMapEncodeTiled unavailable");
-            return WT3D_ERR_CUDA;
-        }
-        fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
+    const PFN_cuTensorMapEncodeTiled_v12000 fn = g_encode;
     cuuint64_t gdim[2] = {(cuuint64_t)Kr, (cuuint64_t)rows};
     cuuint64_t gstr[1] = {(cuuint64_t)Kr * 4};
     cuuint32_t box[2] = {(cuuint32_t)NB_BK, (cuuint32_t)box_rows};
@@ -314,6 +354,7 @@ extern "C" int wt3d_gemm_noalloc(int M, int N, int K, const void *dA, int lda, c
         // device address (its host-side name is only a stand-in)
         std::lock_guard<std::mutex> lk(g_mu);
         if (!D.ready) {
+            if (int rc = resolve_encode()) return rc;
             WT_CUDA(cudaGetSymbolAddress((void **)&D.scratch, g_scratch));
             WT_CUDA(cudaGetSymbolAddress((void **)&D.err, g_err));
             WT_CUDA(cudaFuncSetAttribute(k_na_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, NB_SMEM));
