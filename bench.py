@@ -103,6 +103,24 @@ def plane_wave_sources(nrhs, seed=11):
     return ain, baz
 
 
+def workload_config(args, world=1):
+    """The workload description shared by every arm (identical dicts)."""
+    nrhs = args.nrhs
+    nl = args.lanes
+    return {"workload": "config2 %dx%dx%d: per frequency assemble A(omega), factor, solve 32 plane-wave sources "
+                        "to relres <= tol" % tuple(args.dims), "h_m": 20.0,
+            "pml_nodes": 10, "free_surface": True, "usemin": True,
+            "model": "4 flat layers Vp 3000-6000, Vs=Vp/1.73, 5% Gaussian-correlated 200 m (seed 1), Gardner rho",
+            "freqs_hz": FREQS, "sources_per_step": nrhs,
+            "rhs": ("%d Haskell plane-wave P sources per frequency (incidence U[0,30] deg, back-azimuth U[0,360), "
+                    "seed 11), scattered-field f = (A_bg - A) u0 against the unperturbed layered background" % nrhs),
+            "tol": args.tol,
+            "l2": "inputs larger than L2: the factors (74.7 GB complex64 at 96x96x64) are re-read every pass",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "pipelining": "%d solver handles of the same grid, alternate frequencies from %d host threads: "
+                          "one frequency's substitution passes overlap the next one's factorisation" % (nl, nl)}
+
+
 def run_pipelined(n_steps, first, work, nlanes):
     """Runs steps first .. first+n_steps-1; step i on lane i % nlanes, one host
     thread per lane (the library releases the interpreter lock).  Lanes are
@@ -131,7 +149,7 @@ def run_pipelined(n_steps, first, work, nlanes):
     return out
 
 
-def run_ours(args, rank, world):
+def run_ours(args, rank, world, mixed_solutions):
     import ctypes
     import torch
     import wtomo3d_gb300 as wt
@@ -148,8 +166,6 @@ def run_ours(args, rank, world):
     layers = wt.Layered1D(*model.layered1d(nz, dx))
     nrhs = args.nrhs
     ain, baz = plane_wave_sources(nrhs)
-    rhs_desc = ("%d Haskell plane-wave P sources per frequency (incidence U[0,30] deg, back-azimuth U[0,360), "
-                "seed 11), scattered-field f = (A_bg - A) u0 against the unperturbed layered background" % nrhs)
     # two lanes (handles) of the same grid, pipelined frequencies; the
     # factorisations' tensor-core GEMM leaves sm_reserve SMs to the other
     # lane's substitution passes
@@ -238,6 +254,16 @@ def run_ours(args, rank, world):
         dt = time.perf_counter() - t0
         resident.append({"freq": last_f[l], "solves_per_s": nrhs / dt, "ms": 1e3 * dt, "passes": S[l].last_iters,
                          "relres": float(rr.max())})
+        # the mixed-precision wavefields of this frequency, kept on the host for
+        # the comparison with the FP64 GPU factorisation
+        mixed_solutions[last_f[l]] = (dX[l].cpu().numpy(), rr.copy())
+    # the FP64 leg's other frequencies, solved here by the mixed path too
+    for f in getattr(args, "fp64_freqs", []) or []:
+        if f not in mixed_solutions:
+            S[0].factor(2 * np.pi * f)
+            S[0].rhs_planewave(layers, ain, baz, d_F=dB[0].data_ptr())
+            rr = S[0].solve_device(dB[0].data_ptr(), dX[0].data_ptr(), nrhs, tol=args.tol, maxit=30)
+            mixed_solutions[f] = (dX[0].cpu().numpy(), rr.copy())
     s = S[0]
 
     # ---- roofline of the dominant kernel (one profiled factorisation) ----
@@ -253,15 +279,7 @@ def run_ours(args, rank, world):
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64 fronts (fp32) + f64 refinement", "data": "synthetic",
-        "config": {"workload": "config2 mixed-precision %dx%dx%d" % tuple(args.dims), "h_m": dx,
-                   "pml_nodes": 10, "free_surface": True, "usemin": True,
-                   "model": "4 flat layers Vp 3000-6000, Vs=Vp/1.73, 5% Gaussian-correlated 200 m (seed 1), Gardner rho",
-                   "freqs_hz": FREQS, "sources_per_step": nrhs, "rhs": rhs_desc, "tol": args.tol,
-                   "l2": "inputs larger than L2 (factors %.1f GB)" % (st["factor_bytes"] / 1e9),
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "pipelining": "%d solver handles of the same grid, alternate frequencies from %d host threads: "
-                                 "one frequency's substitution passes overlap the next one's factorisation; "
-                                 "tensor-core GEMM on %d SMs less" % (nl, nl, args.sm_reserve if nl > 1 else 0)},
+        "config": workload_config(args, world),
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "resident": resident,
         "gpu_launches": launches,
@@ -277,7 +295,7 @@ def run_ours(args, rank, world):
                      "traffic_algorithmic": TC_CAPTURE["algorithmic_bytes"]},
         "steps_detail": recs,
         "factor": {"flops": st["factor_flops"], "entries": st["factor_entries"], "fronts": st["nfronts"],
-                   "analyse_s": t_analyse, "profile_ms": prof},
+                   "bytes": st["factor_bytes"], "analyse_s": t_analyse, "profile_ms": prof},
         "solve_pass_profile_ms": sprof,
         "clocks": ck,
     }
@@ -372,17 +390,20 @@ def run_serve(args):
     return summ
 
 
-def run_fp64(args):
+def run_fp64_leg(args, mixed_solutions):
     """The FP64 GPU factorisation oracle on the same workload: complex128
-    fronts (FP64 SIMT kernels), FP64 refinement to the same tolerance.  Only
-    the device-resident rate is measured (one factorisation at 96x96x64 takes
-    minutes at GB300's FP64 rate)."""
+    fronts (FP64 SIMT kernels) and the same FP64 refinement, one frequency per
+    step, device-resident inputs.  Every frequency of args.fp64_freqs is
+    factored once; its 32 wavefields are compared with the mixed-precision
+    wavefields of the same frequency (err = max over sources of
+    ||x_mixed - x_fp64|| / ||x_fp64||)."""
     import torch
     import wtomo3d_gb300 as wt
     from wtomo3d_gb300 import Grid, model
     nx, ny, nz = args.dims
     dx = 20.0
     g = Grid(nx, ny, nz, dx, pmld=10 * dx, fst=1, usemin=1)
+    torch.cuda.empty_cache()
     s = wt.Solver(g, wt.PREC_FP64)
     s.set_model(*model.layered_random(nx, ny, nz, dx, seed=1))
     s.set_background(*model.layered(nx, ny, nz))
@@ -390,49 +411,73 @@ def run_fp64(args):
     ain, baz = plane_wave_sources(args.nrhs)
     dB = torch.zeros((args.nrhs, g.n), dtype=torch.complex128, device="cuda")
     dX = torch.zeros_like(dB)
-    recs = []
+    recs, errs = [], {}
     t_total = 0.0
-    for i in range(args.warmup + args.steps):
-        f = FREQS[i % len(FREQS)]
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        s.factor(2 * np.pi * f)
-        s.rhs_planewave(layers, ain, baz, d_F=dB.data_ptr())
-        rr = s.solve_device(dB.data_ptr(), dX.data_ptr(), args.nrhs, tol=args.tol, maxit=30)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        st = s.stats()
-        if i >= args.warmup:
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    try:
+        for f in args.fp64_freqs:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.factor(2 * np.pi * f)
+            s.rhs_planewave(layers, ain, baz, d_F=dB.data_ptr())
+            rr = s.solve_device(dB.data_ptr(), dX.data_ptr(), args.nrhs, tol=args.tol, maxit=30)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            st = s.stats()
             t_total += dt
-            recs.append(dict(freq=f, relres=float(rr.max()), iters=s.last_iters, factor_ms=st["t_factor_ms"],
-                             solve_ms=st["t_solve_ms"], step_s=dt))
-    value = args.nrhs * args.steps / t_total
-    del dB, dX
-    s.close()
-    return {"impl": "fp64-gpu-oracle", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
-            "higher_is_better": True, "dtype": "c128 fronts (fp64) + f64 refinement", "data": "synthetic",
-            "config": {"workload": "config2 FP64 oracle %dx%dx%d" % tuple(args.dims), "sources_per_step": args.nrhs,
-                       "tol": args.tol, "factor_flops": st["factor_flops"]},
-            "steps_detail": recs}
+            rec = dict(freq=f, relres=float(rr.max()), iters=s.last_iters, factor_ms=st["t_factor_ms"],
+                       solve_ms=st["t_solve_ms"], step_s=dt)
+            if f in mixed_solutions:
+                Xm, rrm = mixed_solutions[f]
+                X64 = dX.cpu().numpy()
+                e = np.linalg.norm(Xm - X64, axis=1) / np.linalg.norm(X64, axis=1)
+                errs[f] = float(e.max())
+                rec.update(err_vs_fp64=float(e.max()), err_vs_fp64_median=float(np.median(e)),
+                           mixed_relres=float(rrm.max()))
+            recs.append(rec)
+    finally:
+        ck = clocks.stop()
+        del dB, dX
+        torch.cuda.synchronize()
+        st = s.stats()
+        s.close()
+    value = args.nrhs * len(args.fp64_freqs) / t_total
+    return {"impl": "fp64-gpu-oracle", "value": value, "unit": "solves/s",
+            "ms_per_step": 1e3 * t_total / len(args.fp64_freqs), "steps": len(args.fp64_freqs),
+            "dtype": "c128 fronts (fp64) + f64 refinement", "factor_flops": st["factor_flops"],
+            "note": "one frequency per step: factorisation + plane-wave sources + solves, inputs resident",
+            "steps_detail": recs, "clocks": ck}, errs
 
 
-def run_cpu(args, steps, warmup):
+def run_cpu(args, steps, warmup, workload=None):
+    """The CPU port (oracle/cpu_baseline.py) over `steps` frequencies after
+    `warmup` untimed ones: full single-thread assembly plus a sampled
+    multifrontal factor and substitution per frequency."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import cpu_baseline
-    vals, det = [], None
-    for i in range(warmup + steps):
-        v, det = cpu_baseline.measure(dims=tuple(args.dims), nrhs=args.nrhs, budget_s=args.cpu_budget,
-                                      freq=FREQS[i % len(FREQS)])
-        if i >= warmup:
-            vals.append(v)
-    v = float(np.mean(vals))
-    sample = ("oracle C assembly of the full %dx%dx%d operator (1 thread) + FP64 LAPACK multifrontal on a "
-              "%.0f s sample of fronts from every level of the same elimination tree (%d fronts), extrapolated "
-              "by flops; solves at the best sampled BLAS rate" % (tuple(args.dims) + (args.cpu_budget,
-                                                                                    det["fronts_sampled"])))
-    return v, {"value": v, "unit": "solves/s", "cores": det["threads"], "kind": "port", "sample": sample,
-               "detail": det}
+    w = workload or cpu_baseline.Workload(tuple(args.dims))
+    t_est, dets = 0.0, []
+    try:
+        for i in range(warmup + steps):
+            v, det = w.step(FREQS[i % len(FREQS)], args.nrhs, args.cpu_budget, i)
+            if i >= warmup:
+                t_est += args.nrhs / v
+                dets.append(det)
+    finally:
+        if workload is None:
+            w.close()
+    v = args.nrhs * steps / t_est
+    sample = ("per frequency: the oracle's C assembly of the full %dx%dx%d operator (1 thread, timed in full) + "
+              "the FP64 multifrontal (numpy/LAPACK) on a %.1f s sample of fronts from every level of its own "
+              "nested-dissection tree, levels with at least one front per core at the single-core rate divided by "
+              "the core count, the others with threaded BLAS; factor extrapolated by flops, one forward + backward "
+              "substitution of the 32 sources by factor entries (an FP64 factor needs one pass for 1e-8)"
+              % (tuple(args.dims) + (args.cpu_budget,)))
+    agg = {k: float(np.mean([d[k] for d in dets])) for k in ("t_assemble_s", "t_factor_est_s", "t_solve_est_s")}
+    agg.update(threads=w.threads, factor_flops=w.tree["flops"], factor_entries=w.tree["entries"], steps=steps)
+    return v, {"value": v, "unit": "solves/s", "cores": w.threads, "kind": "port", "sample": sample,
+               "detail": agg}
 
 
 def main():
@@ -440,11 +485,14 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference", "fp64"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--dims", type=int, nargs=3, default=[96, 96, 64])
     ap.add_argument("--nrhs", type=int, default=32)
     ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--cpu-budget", type=float, default=2.0, help="seconds of sampled fronts per CPU step")
+    ap.add_argument("--no-c1", action="store_true", help="reference arm: skip the full 40^3 CPU factor and solve")
+    ap.add_argument("--fp64-freqs", type=lambda t: [float(x) for x in t.split(",") if x],
+                    default=[0.5, 2.0], help="frequencies of the FP64 GPU factorisation leg ('' skips it)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--clocks-log", default=None, help="file for the nvidia-smi samples of the timed region")
@@ -457,22 +505,31 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
 
     if args.impl == "reference":
+        # the CPU port on the host cores; rank 0 only, the other ranks exit
         if rank != 0:
             return
-        v, cb = run_cpu(args, args.steps, min(args.warmup, 1))
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import cpu_baseline
+        t0 = time.perf_counter()
+        w = cpu_baseline.Workload(tuple(args.dims))
+        try:
+            v, cb = run_cpu(args, args.steps, args.warmup, workload=w)
+        finally:
+            w.close()
+        wall = time.perf_counter() - t0
         out = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps,
-               "warmup": min(args.warmup, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "impl": "reference", "dtype": "c128 (fp64)", "data": "synthetic",
-               "config": {"workload": "config2 %dx%dx%d, CPU port (reference CPU path unbuildable here)"
-                          % tuple(args.dims), "freqs_hz": FREQS, "sources_per_step": args.nrhs},
-               "cpu_baseline": cb,
-               "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+               "warmup": args.warmup, "ms_per_step": 1e3 * args.nrhs / v, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "impl": "reference", "dtype": "c128 (fp64)", "data": "synthetic",
+               "config": workload_config(args, world), "cpu_baseline": cb,
+               "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+               "note": ("the reference's STRUMPACK/MPI path cannot be built here (no Fortran compiler, STRUMPACK, "
+                        "HDF5 or MPI; sources missing from its tree): its CPU port is timed instead, with each "
+                        "frequency's factor and substitution extrapolated from a sample (ms_per_step is that "
+                        "estimate; wall_s is the arm's own run time)"),
+               "wall_s": wall}
+        if not args.no_c1:
+            out["c1_full"] = cpu_baseline.config1_full()
         print(json.dumps(out))
-        return
-
-    if args.impl == "fp64":
-        if rank == 0:
-            print(json.dumps(run_fp64(args)))
         return
 
     if world > 1:
@@ -480,13 +537,21 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    out = run_ours(args, rank, world)
+    mixed_solutions = {}
+    out = run_ours(args, rank, world, mixed_solutions)
     if rank == 0:
         # assembly throughput at the benchmark grid and at the largest grid
         # (128x128x96, 12-node PML), whose factors do not fit one GPU
         out["assembly"] = [assembly_rate(tuple(args.dims)), assembly_rate((128, 128, 96))]
     if rank == 0 and not args.no_serve:
         out["serve"] = run_serve(args)
+    if rank == 0 and args.fp64_freqs:
+        fp, errs = run_fp64_leg(args, mixed_solutions)
+        out["fp64"] = fp
+        out["mixed_over_fp64"] = out["value"] / fp["value"]
+        if errs:
+            out["err_vs_fp64"] = max(errs.values())
+            out["err_vs_fp64_by_freq"] = {str(k): v for k, v in errs.items()}
     if rank == 0:
         if not args.no_cpu:
             v, cb = run_cpu(args, 1, 0)

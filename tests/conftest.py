@@ -7,7 +7,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 TESTS = os.path.dirname(os.path.abspath(__file__))
-for p in (TESTS, os.path.join(TESTS, "golden")):
+for p in (TESTS, os.path.join(TESTS, "golden"), os.path.join(ROOT, "oracle")):
     if p not in sys.path:
         sys.path.insert(0, p)
 

@@ -81,6 +81,7 @@ public:
     std::unique_ptr<Schedule<T>> fsched;
     std::map<int, std::unique_ptr<Schedule<T>>> ssched[2];   // [adjoint][m]
     static constexpr int WB = 512;   // outer block width of the two-level LU
+    static constexpr int WS = 512;   // outer block width of the blocked substitutions
     // pivots below pivot_rel times the largest entry are perturbed: only
     // (near-)zero ones, since Dirichlet rows carry unit pivots next to O(1e8)
     // stiffness entries
@@ -175,10 +176,17 @@ public:
         std::call_once(attr_once[dev & 63], [] {
             size_t sp = sizeof(cx<T>) * (KB * (KB + 1) + 2 * KB * (KB + 1));
             cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp);
+            cudaFuncSetAttribute(k_tile_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp);
             cudaFuncSetAttribute(k_trsm_row<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (TRW + 1))));
             cudaFuncSetAttribute(k_trsm_col<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1))));
+            if constexpr (std::is_same<T, float>::value) {
+                cudaFuncSetAttribute(k_trsm_row_reg<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (TRW + 1))));
+                cudaFuncSetAttribute(k_trsm_col_reg<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1))));
+            }
             cudaFuncSetAttribute(k_diag_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1))));
         });
@@ -473,16 +481,22 @@ public:
                     size_t smr = sizeof(cx<T>) * (KB * (KB + 1) + KB * (TRW + 1));
                     size_t smc = sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1));
                     sc->launches.push_back({[psc, this, p0, np, smp](cudaStream_t st) {
-                        k_panel<T><<<np, 256, smp, st>>>(psc->panel.p + p0, fr.p, fac.p, ipiv.p, maxabs.p, pivot_rel, npert.p,
-                                                         dinv.p);
+                        k_panel<T><<<np, 256, smp, st>>>(psc->panel.p + p0, fr.p, fac.p, ipiv.p, maxabs.p, pivot_rel,
+                                                         npert.p);
                     }, LK_PANEL, 0});
                     if (nr)
                         sc->launches.push_back({[psc, this, r0, nr, smr](cudaStream_t st) {
-                            k_trsm_row<T><<<nr, TRW, smr, st>>>(psc->row.p + r0, fr.p, fac.p, ipiv.p);
+                            if constexpr (std::is_same<T, float>::value)
+                                k_trsm_row_reg<0><<<nr, TRW, smr, st>>>(psc->row.p + r0, fr.p, fac.p, ipiv.p);
+                            else
+                                k_trsm_row<T><<<nr, TRW, smr, st>>>(psc->row.p + r0, fr.p, fac.p, ipiv.p);
                         }, LK_TRSM, 0});
                     if (ncl)
                         sc->launches.push_back({[psc, this, cc0, ncl, smc](cudaStream_t st) {
-                            k_trsm_col<T><<<ncl, TCR, smc, st>>>(psc->col.p + cc0, fr.p, fac.p);
+                            if constexpr (std::is_same<T, float>::value)
+                                k_trsm_col_reg<0><<<ncl, TCR, smc, st>>>(psc->col.p + cc0, fr.p, fac.p);
+                            else
+                                k_trsm_col<T><<<ncl, TCR, smc, st>>>(psc->col.p + cc0, fr.p, fac.p);
                         }, LK_TRSM, 0});
                     push_gemm_launch(*sc, hg, g0, tiles);
                 }
@@ -516,6 +530,15 @@ public:
                 }
                 push_gemm_launch(*sc, hg, g0, tiles);
             }
+        }
+        // the tile inverses the solves use, for every panel at once
+        {
+            const int npall = (int)hp.size();
+            const size_t smi = sizeof(cx<T>) * (KB * (KB + 1) + 2 * KB * (KB + 1));
+            if (npall)
+                sc->launches.push_back({[psc, this, npall, smi](cudaStream_t st) {
+                    k_tile_inverse<T><<<npall, 2 * KB, smi, st>>>(psc->panel.p, fr.p, fac.p, dinv.p);
+                }, LK_PANEL, 0});
         }
         int rc;
         if ((rc = sc->panel.upload(hp))) return rc;
@@ -555,29 +578,54 @@ public:
                 k_diag_solve<T><<<np, 256, smd, st>>>(psc->panel.p + p0, fr.p, dinv.p, ipiv.p, Xp, ldx, m, mode);
             }, LK_DIAG, 0, (double)np * (KB * KB + 2.0 * KB * m) * sizeof(cx<T>)});
         };
+        // Two-level blocking of the in-front substitutions, like the
+        // factorisation's: inside each WS-wide outer block the KB panels are
+        // solved one by one (diagonal tile product, then a K = KB update of
+        // the block's own rows), and the rows outside the block receive one
+        // K = WS update, which the tall-skinny tensor-core kernel takes.
         // ---- forward sweep: leaves to root ----
         for (int L = nlev - 1; L >= 0; L--) {
             const std::vector<int> &fl = sym.levels[L];
             int maxp = 0;
             for (int f : fl) maxp = std::max(maxp, sym.fronts[f].p);
-            for (int k = 0; k < maxp; k += KB) {
-                size_t p0 = hp.size(), g0 = hg.size();
+            for (int c0 = 0; c0 < maxp; c0 += WS) {
+                for (int k = c0; k < std::min(c0 + WS, maxp); k += KB) {
+                    size_t p0 = hp.size(), g0 = hg.size();
+                    long long tiles = 0;
+                    for (int f : fl) {
+                        const Front &Fr = sym.fronts[f];
+                        if (Fr.p <= k) continue;
+                        const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k), k2 = k + kb;
+                        const int cend = std::min(c0 + WS, Fr.p);
+                        hp.push_back(PanelTask{f, k});
+                        cx<T> *Pb = F + Fr.fac_off;
+                        cx<T> *Y = Xp + (long long)Fr.first * ldx;
+                        if (!adjoint)   // Y[k2:cend] -= L[k2:cend, k:k2] Y[k:k2]
+                            add_gemm(hg, tiles, Pb + (long long)k2 * nf + k, nf, Y + (long long)k * ldx, ldx,
+                                     Y + (long long)k2 * ldx, ldx, cend - k2, m, kb);
+                        else            // Y[k2:cend] -= U[k:k2, k2:cend]^H Y[k:k2]
+                            add_gemm(hg, tiles, Pb + (long long)k * nf + k2, nf, Y + (long long)k * ldx, ldx,
+                                     Y + (long long)k2 * ldx, ldx, cend - k2, m, kb, nullptr, nullptr, 1);
+                    }
+                    diag_launch(p0, adjoint ? 2 : 0);
+                    push_gemm_launch(*sc, hg, g0, tiles);
+                }
+                // rows below the outer block
+                size_t g0 = hg.size();
                 long long tiles = 0;
                 for (int f : fl) {
                     const Front &Fr = sym.fronts[f];
-                    if (Fr.p <= k) continue;
-                    const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k), k2 = k + kb;
-                    hp.push_back(PanelTask{f, k});
+                    if (Fr.p <= c0) continue;
+                    const int nf = Fr.nf(), cend = std::min(c0 + WS, Fr.p);
                     cx<T> *Pb = F + Fr.fac_off;
                     cx<T> *Y = Xp + (long long)Fr.first * ldx;
-                    if (!adjoint)   // Y[k2:p] -= L[k2:p, k:k2] Y[k:k2]
-                        add_gemm(hg, tiles, Pb + (long long)k2 * nf + k, nf, Y + (long long)k * ldx, ldx,
-                                 Y + (long long)k2 * ldx, ldx, Fr.p - k2, m, kb);
-                    else            // Y[k2:p] -= U[k:k2, k2:p]^H Y[k:k2]
-                        add_gemm(hg, tiles, Pb + (long long)k * nf + k2, nf, Y + (long long)k * ldx, ldx,
-                                 Y + (long long)k2 * ldx, ldx, Fr.p - k2, m, kb, nullptr, nullptr, 1);
+                    if (!adjoint)   // Y[cend:p] -= L[cend:p, c0:cend] Y[c0:cend]
+                        add_gemm(hg, tiles, Pb + (long long)cend * nf + c0, nf, Y + (long long)c0 * ldx, ldx,
+                                 Y + (long long)cend * ldx, ldx, Fr.p - cend, m, cend - c0);
+                    else            // Y[cend:p] -= U[c0:cend, cend:p]^H Y[c0:cend]
+                        add_gemm(hg, tiles, Pb + (long long)c0 * nf + cend, nf, Y + (long long)c0 * ldx, ldx,
+                                 Y + (long long)cend * ldx, ldx, Fr.p - cend, m, cend - c0, nullptr, nullptr, 1);
                 }
-                diag_launch(p0, adjoint ? 2 : 0);
                 push_gemm_launch(*sc, hg, g0, tiles);
             }
             // border update  X[border] -= L21 Y   (adjoint: U12^H Y)
@@ -601,10 +649,10 @@ public:
             const std::vector<int> &fl = sym.levels[L];
             size_t g0 = hg.size();
             long long tiles = 0;
-            int maxsteps = 0;
+            int maxp = 0;
             for (int f : fl) {
                 const Front &Fr = sym.fronts[f];
-                maxsteps = std::max(maxsteps, (Fr.p + KB - 1) / KB);
+                maxp = std::max(maxp, Fr.p);
                 if (Fr.b == 0) continue;
                 const int nf = Fr.nf();
                 cx<T> *Pb = F + Fr.fac_off;
@@ -617,36 +665,71 @@ public:
                     add_gemm(hg, tiles, Lo, Fr.p, Xp, ldx, Y, ldx, Fr.p, m, Fr.b, brow, nullptr, 1);
             }
             push_gemm_launch(*sc, hg, g0, tiles);
-            for (int s = maxsteps - 1; s >= 0; s--) {
-                const int k = s * KB;
-                size_t p0 = hp.size(), g1 = hg.size();
-                long long t1 = 0;
-                for (int f : fl) {
-                    const Front &Fr = sym.fronts[f];
-                    if (Fr.p <= k) continue;
-                    const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k), k2 = k + kb;
-                    cx<T> *Pb = F + Fr.fac_off;
-                    cx<T> *Y = Xp + (long long)Fr.first * ldx;
-                    hp.push_back(PanelTask{f, k});
-                    if (adjoint)   // Y[k:k2] -= L[k2:p, k:k2]^H Y[k2:p]   (before the diagonal solve)
-                        add_gemm(hg, t1, Pb + (long long)k2 * nf + k, nf, Y + (long long)k2 * ldx, ldx,
-                                 Y + (long long)k * ldx, ldx, kb, m, Fr.p - k2, nullptr, nullptr, 1);
-                }
-                if (!adjoint) {
-                    diag_launch(p0, 1);
-                    // Y[0:k] -= U[0:k, k:k2] Y[k:k2]
+            for (int c0 = (maxp - 1) / WS * WS; c0 >= 0; c0 -= WS) {
+                if (adjoint) {
+                    // Y[c0:cend] -= L[cend:p, c0:cend]^H Y[cend:p]  (rows below the block, solved already)
+                    size_t g1 = hg.size();
+                    long long t1 = 0;
                     for (int f : fl) {
                         const Front &Fr = sym.fronts[f];
-                        if (Fr.p <= k || k == 0) continue;
-                        const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k);
+                        if (Fr.p <= c0) continue;
+                        const int nf = Fr.nf(), cend = std::min(c0 + WS, Fr.p);
+                        if (Fr.p <= cend) continue;
                         cx<T> *Pb = F + Fr.fac_off;
                         cx<T> *Y = Xp + (long long)Fr.first * ldx;
-                        add_gemm(hg, t1, Pb + k, nf, Y + (long long)k * ldx, ldx, Y, ldx, k, m, kb);
+                        add_gemm(hg, t1, Pb + (long long)cend * nf + c0, nf, Y + (long long)cend * ldx, ldx,
+                                 Y + (long long)c0 * ldx, ldx, cend - c0, m, Fr.p - cend, nullptr, nullptr, 1);
                     }
                     push_gemm_launch(*sc, hg, g1, t1);
-                } else {
+                }
+                const int nsteps = (std::min(c0 + WS, maxp) - c0 + KB - 1) / KB;
+                for (int s = nsteps - 1; s >= 0; s--) {
+                    const int k = c0 + s * KB;
+                    size_t p0 = hp.size(), g1 = hg.size();
+                    long long t1 = 0;
+                    for (int f : fl) {
+                        const Front &Fr = sym.fronts[f];
+                        if (Fr.p <= k) continue;
+                        const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k), k2 = k + kb;
+                        const int cend = std::min(c0 + WS, Fr.p);
+                        cx<T> *Pb = F + Fr.fac_off;
+                        cx<T> *Y = Xp + (long long)Fr.first * ldx;
+                        hp.push_back(PanelTask{f, k});
+                        if (adjoint)   // Y[k:k2] -= L[k2:cend, k:k2]^H Y[k2:cend]   (before the diagonal solve)
+                            add_gemm(hg, t1, Pb + (long long)k2 * nf + k, nf, Y + (long long)k2 * ldx, ldx,
+                                     Y + (long long)k * ldx, ldx, kb, m, cend - k2, nullptr, nullptr, 1);
+                    }
+                    if (!adjoint) {
+                        diag_launch(p0, 1);
+                        // Y[c0:k] -= U[c0:k, k:k2] Y[k:k2]
+                        for (int f : fl) {
+                            const Front &Fr = sym.fronts[f];
+                            if (Fr.p <= k || k == c0) continue;
+                            const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k);
+                            cx<T> *Pb = F + Fr.fac_off;
+                            cx<T> *Y = Xp + (long long)Fr.first * ldx;
+                            add_gemm(hg, t1, Pb + (long long)c0 * nf + k, nf, Y + (long long)k * ldx, ldx,
+                                     Y + (long long)c0 * ldx, ldx, k - c0, m, kb);
+                        }
+                        push_gemm_launch(*sc, hg, g1, t1);
+                    } else {
+                        push_gemm_launch(*sc, hg, g1, t1);
+                        diag_launch(p0, 3);
+                    }
+                }
+                if (!adjoint && c0 > 0) {
+                    // rows above the block: Y[0:c0] -= U[0:c0, c0:cend] Y[c0:cend]
+                    size_t g1 = hg.size();
+                    long long t1 = 0;
+                    for (int f : fl) {
+                        const Front &Fr = sym.fronts[f];
+                        if (Fr.p <= c0) continue;
+                        const int nf = Fr.nf(), cend = std::min(c0 + WS, Fr.p);
+                        cx<T> *Pb = F + Fr.fac_off;
+                        cx<T> *Y = Xp + (long long)Fr.first * ldx;
+                        add_gemm(hg, t1, Pb + c0, nf, Y + (long long)c0 * ldx, ldx, Y, ldx, c0, m, cend - c0);
+                    }
                     push_gemm_launch(*sc, hg, g1, t1);
-                    diag_launch(p0, 3);
                 }
             }
         }

@@ -151,7 +151,7 @@ template <class T>
 __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
                                                cx<T> *__restrict__ fac, int *__restrict__ ipiv,
                                                const unsigned long long *__restrict__ amax2, double pivot_rel,
-                                               int *__restrict__ npert, cx<T> *__restrict__ inv)
+                                               int *__restrict__ npert)
 {
     // static-pivot threshold: pivot_rel * max |a_ij| of the assembled operator
     const T thresh = (T)(pivot_rel * sqrt(__longlong_as_double((long long)*amax2)));
@@ -218,38 +218,62 @@ __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tas
         int i = idx / kb, j = idx % kb;
         D[(long long)i * nf + j] = S[i * LD + j];
     }
-    // Inverses of the unit-lower L_D and upper U_D factors of the tile, for the
-    // substitution passes of the solves (dense products instead of serial
-    // recurrences).  Thread c < kb: column c of L_D^{-1}; kb <= c < 2kb:
-    // column c-kb of U_D^{-1}.  Padded to KB x KB with the identity.
+}
+
+// ---------------------------------------------------------------------------
+// Inverses of the unit-lower L_D and upper U_D factors of every factored tile,
+// for the substitution passes of the solves (dense products instead of serial
+// recurrences).  Run once after the factorisation over all panels: a tile is
+// final once its panel step is done (later steps change only rows and columns
+// to its right and below, and row interchanges are LINPACK style), so this
+// work is off the factorisation's chain of dependent panel steps.
+// Thread c < KB: column c of L_D^{-1}; KB <= c < 2 KB: column c - KB of
+// U_D^{-1}.  Padded to KB x KB with the identity.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(2 * KB) k_tile_inverse(const PanelTask *__restrict__ tasks,
+                                                         const FrontDev *__restrict__ fr,
+                                                         const cx<T> *__restrict__ fac, cx<T> *__restrict__ inv)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    cx<T> *S = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1), then 2 KB scratch columns
+    const int LD = KB + 1;
+    const PanelTask t = tasks[blockIdx.x];
+    const FrontDev F = fr[t.f];
+    const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
+    const cx<T> *D = fac + F.fac + (long long)k * nf + k;
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < kb * kb; idx += blockDim.x) {
+        const int i = idx / kb, j = idx % kb;
+        S[i * LD + j] = D[(long long)i * nf + j];
+    }
+    __syncthreads();
     cx<T> *Li = inv + (long long)(F.pan + k / KB) * (2 * KB * KB);
     cx<T> *Ui = Li + KB * KB;
     cx<T> *col = S + KB * LD;            // per-thread scratch column, 2 KB x (KB + 1)
     const int c = tid;
-    if (c < 2 * KB) {
-        const bool up = c >= KB;
-        const int cc = up ? c - KB : c;
-        cx<T> *x = col + c * (KB + 1);
-        if (!up) {
-            for (int i = 0; i < KB; i++) {
-                cx<T> s = (i == cc) ? cx<T>(1) : cx<T>(0);
-                if (i < kb && cc < kb)
-                    for (int l = cc; l < i; l++) s = s - S[i * LD + l] * x[l];
-                x[i] = s;
-            }
-        } else {
-            for (int i = KB - 1; i >= 0; i--) {
-                cx<T> s = (i == cc) ? cx<T>(1) : cx<T>(0);
-                if (i < kb && cc < kb) {
-                    for (int l = i + 1; l <= cc; l++) s = s - S[i * LD + l] * x[l];
-                    s = cdiv(s, S[i * LD + i]);
-                }
-                x[i] = s;
-            }
+    const bool up = c >= KB;
+    const int cc = up ? c - KB : c;
+    cx<T> *x = col + c * (KB + 1);
+    if (!up) {
+        for (int i = 0; i < KB; i++) {
+            cx<T> s = (i == cc) ? cx<T>(1) : cx<T>(0);
+            if (i < kb && cc < kb)
+                for (int l = cc; l < i; l++) s = s - S[i * LD + l] * x[l];
+            x[i] = s;
         }
-        cx<T> *dst = up ? Ui : Li;
-        for (int i = 0; i < KB; i++) dst[i * KB + cc] = x[i];
+    } else {
+        for (int i = KB - 1; i >= 0; i--) {
+            cx<T> s = (i == cc) ? cx<T>(1) : cx<T>(0);
+            if (i < kb && cc < kb) {
+                for (int l = i + 1; l <= cc; l++) s = s - S[i * LD + l] * x[l];
+                s = cdiv(s, S[i * LD + i]);
+            }
+            x[i] = s;
+        }
     }
+    cx<T> *dst = up ? Ui : Li;
+    for (int i = 0; i < KB; i++) dst[i * KB + cc] = x[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -352,6 +376,133 @@ __global__ void __launch_bounds__(TCR) k_trsm_col(const ColTask *__restrict__ ta
     __syncthreads();
     for (int q = tid; q < nr * kb; q += blockDim.x) {
         int r = q / kb, j = q % kb;
+        xb[(long long)r * ld + j] = Xs[r * (KB + 1) + j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// complex64 variants of the two band solves with the band's vector in
+// registers.  Both are right-looking: once an unknown is final, its multiples
+// are subtracted from all later ones, which are independent of each other, so
+// the 64 x 64 / 2 multiply-adds per column (row) run as independent chains
+// instead of one dependent recurrence.  The KB x KB triangle is padded with the
+// identity beyond kb (a last, narrower panel), so the loops are fixed-length
+// and unroll completely.
+// ---------------------------------------------------------------------------
+template <int UNUSED = 0>
+__global__ void __launch_bounds__(TRW) k_trsm_row_reg(const RowTask *__restrict__ tasks,
+                                                             const FrontDev *__restrict__ fr, cx<float> *__restrict__ fac,
+                                                      const int *__restrict__ ipiv)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    cx<float> *L = reinterpret_cast<cx<float> *>(smraw);          // KB x (KB+1)
+    cx<float> *Bt = L + KB * (KB + 1);                           // KB x (TRW+1)
+    __shared__ int idx[KB];
+    const RowTask t = tasks[blockIdx.x];
+    const FrontDev F = fr[t.f];
+    const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
+    const int c0 = t.c0, nc = min(TRW, nf - c0);
+    const int tid = threadIdx.x;
+    cx<float> *base = fac + F.fac + (long long)k * nf;
+    for (int q = tid; q < KB * KB; q += blockDim.x) {
+        const int i = q / KB, j = q % KB;
+        L[i * (KB + 1) + j] = (i < kb && j < kb) ? base[(long long)i * nf + k + j] : cx<float>(0.f, 0.f);
+    }
+    if (tid == 0) {
+        for (int i = 0; i < kb; i++) idx[i] = i;
+        for (int j = 0; j < kb; j++) {
+            int pv = ipiv[F.first + k + j] - k;
+            int a = idx[j]; idx[j] = idx[pv]; idx[pv] = a;
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < kb * nc; q += blockDim.x) {
+        const int i = q / nc, c = q % nc;
+        Bt[i * (TRW + 1) + c] = base[(long long)idx[i] * nf + c0 + c];
+    }
+    __syncthreads();
+    cx<float> b[KB];
+#pragma unroll
+    for (int i = 0; i < KB; i++) b[i] = (i < kb) ? Bt[i * (TRW + 1) + tid] : cx<float>(0.f, 0.f);
+#pragma unroll
+    for (int l = 0; l < KB - 1; l++) {
+        const cx<float> bl = b[l];
+#pragma unroll
+        for (int i = l + 1; i < KB; i++) {
+            const cx<float> a = L[i * (KB + 1) + l];
+            b[i].re = fmaf(-a.re, bl.re, fmaf(a.im, bl.im, b[i].re));
+            b[i].im = fmaf(-a.re, bl.im, fmaf(-a.im, bl.re, b[i].im));
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < KB; i++)
+        if (i < kb) Bt[i * (TRW + 1) + tid] = b[i];
+    __syncthreads();
+    for (int q = tid; q < kb * nc; q += blockDim.x) {
+        const int i = q / nc, c = q % nc;
+        base[(long long)i * nf + c0 + c] = Bt[i * (TRW + 1) + c];
+    }
+}
+
+template <int UNUSED = 0>
+__global__ void __launch_bounds__(TCR) k_trsm_col_reg(const ColTask *__restrict__ tasks,
+                                                      const FrontDev *__restrict__ fr, cx<float> *__restrict__ fac)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    cx<float> *U = reinterpret_cast<cx<float> *>(smraw);          // KB x (KB+1)
+    cx<float> *Xs = U + KB * (KB + 1);                           // TCR x (KB+1)
+    __shared__ cx<float> invd[KB];
+    const ColTask t = tasks[blockIdx.x];
+    const FrontDev F = fr[t.f];
+    const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
+    const int tid = threadIdx.x;
+    const cx<float> *D = fac + F.fac + (long long)k * nf + k;
+    for (int q = tid; q < KB * KB; q += blockDim.x) {
+        const int i = q / KB, j = q % KB;
+        U[i * (KB + 1) + j] = (i < kb && j < kb) ? D[(long long)i * nf + j]
+                                                 : cx<float>(i == j ? 1.f : 0.f, 0.f);
+    }
+    cx<float> *xb;
+    long long ld;
+    int nr;
+    if (t.which == 0) {
+        xb = fac + F.fac + (long long)t.r0 * nf + k;
+        ld = nf;
+        nr = min(TCR, F.p - t.r0);
+    } else {
+        xb = fac + F.fac + (long long)F.p * nf + (long long)t.r0 * F.p + k;
+        ld = F.p;
+        nr = min(TCR, F.b - t.r0);
+    }
+    for (int q = tid; q < nr * kb; q += blockDim.x) {
+        const int r = q / kb, j = q % kb;
+        Xs[r * (KB + 1) + j] = xb[(long long)r * ld + j];
+    }
+    __syncthreads();
+    for (int j = tid; j < KB; j += blockDim.x) invd[j] = cdiv(cx<float>(1.f, 0.f), U[j * (KB + 1) + j]);
+    __syncthreads();
+    cx<float> x[KB];
+#pragma unroll
+    for (int j = 0; j < KB; j++) x[j] = (j < kb && tid < nr) ? Xs[tid * (KB + 1) + j] : cx<float>(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < KB; j++) {
+        x[j] = x[j] * invd[j];
+        const cx<float> xj = x[j];
+#pragma unroll
+        for (int j2 = j + 1; j2 < KB; j2++) {
+            const cx<float> u = U[j * (KB + 1) + j2];
+            x[j2].re = fmaf(-xj.re, u.re, fmaf(xj.im, u.im, x[j2].re));
+            x[j2].im = fmaf(-xj.re, u.im, fmaf(-xj.im, u.re, x[j2].im));
+        }
+    }
+    if (tid < nr) {
+#pragma unroll
+        for (int j = 0; j < KB; j++)
+            if (j < kb) Xs[tid * (KB + 1) + j] = x[j];
+    }
+    __syncthreads();
+    for (int q = tid; q < nr * kb; q += blockDim.x) {
+        const int r = q / kb, j = q % kb;
         xb[(long long)r * ld + j] = Xs[r * (KB + 1) + j];
     }
 }

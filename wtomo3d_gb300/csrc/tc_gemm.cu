@@ -14,6 +14,16 @@
 // D = Ahi Bhi + Ahi Blo + Alo Bhi in an FP32 TMEM accumulator gives an
 // FP32-class product (the dropped Alo Blo term is ~2^-24 relative).
 //
+// f16 mode (the default; WT3D_TC_F16=0 selects the TF32 split): every row of A
+// and every complex column of B is multiplied by a power of two s that puts its
+// largest |re|, |im| in [2^13, 2^14), and the scaled values are split as
+// hi = rn_f16(x s), lo = rn_f16(x s - hi).  Entries within 2^16 of their row's
+// (column's) largest keep 22 bits, like the TF32 split; smaller ones lose
+// relative precision but stay far below the product's normwise rounding.  The
+// same three products run as kind::f16 MMAs, at twice the TF32 rate and with
+// half the operand bytes per K step; the epilogue multiplies each accumulator
+// entry by 1/(s_row s_col) (exact: powers of two).
+//
 // Kernel structure (one 128 x 128-complex output tile per CTA, 6 warps):
 //   warp 0      TMA producer (cp.async.bulk.tensor, SWIZZLE_128B tiles) and
 //               TMEM allocator;
@@ -25,6 +35,7 @@
 // Every mbarrier wait has an iteration limit; on expiry the kernel records an
 // error code, skips ahead, frees its TMEM and returns.
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 #include "tc_gemm.h"
 #include "tc_ptx.cuh"
@@ -116,6 +127,156 @@ __global__ void __launch_bounds__(256) k_split_b(const TcTask *__restrict__ task
     }
 }
 
+// ---- f16 mode ---------------------------------------------------------------
+// Power of two that maps a largest magnitude m into [2^13, 2^14) (1 for m = 0,
+// and for a non-finite m, whose NaN then propagates as with TF32).
+__device__ __forceinline__ float f16_scale(unsigned mbits)
+{
+    const float m = __uint_as_float(mbits);
+    if (!(m > 0.f) || !(m < INFINITY)) return 1.f;
+    int e;
+    frexpf(m, &e);                 // m in [2^(e-1), 2^e)
+    return ldexpf(1.f, 14 - e);
+}
+
+__device__ __forceinline__ void split_f16(float x, __half &hi, __half &lo)
+{
+    hi = __float2half_rn(x);
+    lo = __float2half_rn(x - __half2float(hi));
+}
+
+// One warp per row of A: the row's largest |re|, |im| over k < K.
+__global__ void k_amax(const TcTask *__restrict__ tasks, int ntasks, long long total_rows)
+{
+    const long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (q >= total_rows) return;
+    int lo_t = 0, hi_t = ntasks - 1;
+    while (lo_t < hi_t) {
+        int mid = (lo_t + hi_t + 1) >> 1;
+        if (tasks[mid].a_row0 <= q) lo_t = mid;
+        else hi_t = mid - 1;
+    }
+    const TcTask &t = tasks[lo_t];
+    const int i = (int)(q - t.a_row0);
+    const cx<float> *row = t.A + (long long)i * t.lda;
+    float m = 0.f;
+    for (int k = lane; k < t.K; k += 32) {
+        const cx<float> v = row[k];
+        m = fmaxf(m, fmaxf(fabsf(v.re), fabsf(v.im)));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) t.amax[i] = __float_as_uint(m);
+}
+
+// 32 complex columns x 256 rows of B per block: column maxima by atomicMax on
+// the float bits (non-negative floats order like their bit patterns).
+__global__ void __launch_bounds__(256) k_bmax(const TcTask *__restrict__ tasks, int ntasks, long long total_tiles)
+{
+    __shared__ float red[8][33];
+    const long long q = blockIdx.x;
+    if (q >= total_tiles) return;
+    int lo_t = 0, hi_t = ntasks - 1;
+    while (lo_t < hi_t) {
+        int mid = (lo_t + hi_t + 1) >> 1;
+        if (tasks[mid].b_work0 <= q) lo_t = mid;
+        else hi_t = mid - 1;
+    }
+    const TcTask &t = tasks[lo_t];
+    const long long r = q - t.b_work0;
+    const int kt = t.Kr / 64;                 // 32-complex k tiles
+    const int j0 = (int)(r / kt) * 32, k0 = (int)(r % kt) * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    float m = 0.f;
+    const int j = j0 + tx;
+    if (j < t.N)
+        for (int kk = ty; kk < 32; kk += 8) {
+            const int k = k0 + kk;
+            if (k < t.K) {
+                const cx<float> v = t.B[(long long)k * t.ldb + j];
+                m = fmaxf(m, fmaxf(fabsf(v.re), fabsf(v.im)));
+            }
+        }
+    red[ty][tx] = m;
+    __syncthreads();
+    if (ty == 0 && j < t.N) {
+        for (int y = 1; y < 8; y++) m = fmaxf(m, red[y][tx]);
+        atomicMax(t.bmax + j, __float_as_uint(m));
+    }
+}
+
+// As k_split_a / k_split_b with scaled FP16 halves; the first k of each row
+// (column) also stores the inverse scale for the epilogue.
+__global__ void k_split_a_f16(const TcTask *__restrict__ tasks, int ntasks, long long total)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= total) return;
+    int lo_t = 0, hi_t = ntasks - 1;
+    while (lo_t < hi_t) {
+        int mid = (lo_t + hi_t + 1) >> 1;
+        if (tasks[mid].a_work0 <= q) lo_t = mid;
+        else hi_t = mid - 1;
+    }
+    const TcTask &t = tasks[lo_t];
+    const long long r = q - t.a_work0;
+    const int kc = t.Kr / 2;
+    const int i = (int)(r / kc), k = (int)(r % kc);
+    const float sc = f16_scale(t.amax[i]);
+    if (k == 0) t.sa[i] = 1.f / sc;
+    cx<float> v(0.f, 0.f);
+    if (k < t.K) v = t.A[(long long)i * t.lda + k];
+    __half h0, l0, h1, l1;
+    split_f16(v.re * sc, h0, l0);
+    split_f16(v.im * sc, h1, l1);
+    const long long o = (long long)i * t.Kr + 2 * k;      // in halves
+    reinterpret_cast<__half2 *>(t.ahi)[o >> 1] = __halves2half2(h0, h1);
+    reinterpret_cast<__half2 *>(t.alo)[o >> 1] = __halves2half2(l0, l1);
+}
+
+__global__ void __launch_bounds__(256) k_split_b_f16(const TcTask *__restrict__ tasks, int ntasks,
+                                                     long long total_tiles)
+{
+    __shared__ float2 tile[32][33];
+    long long q = blockIdx.x;
+    if (q >= total_tiles) return;
+    int lo_t = 0, hi_t = ntasks - 1;
+    while (lo_t < hi_t) {
+        int mid = (lo_t + hi_t + 1) >> 1;
+        if (tasks[mid].b_work0 <= q) lo_t = mid;
+        else hi_t = mid - 1;
+    }
+    const TcTask &t = tasks[lo_t];
+    const long long r = q - t.b_work0;
+    const int kt = t.Kr / 64;
+    const int j0 = (int)(r / kt) * 32, k0 = (int)(r % kt) * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int kk = ty; kk < 32; kk += 8) {
+        int k = k0 + kk, j = j0 + tx;
+        cx<float> v(0.f, 0.f);
+        if (k < t.K && j < t.N) v = t.B[(long long)k * t.ldb + j];
+        tile[kk][tx] = make_float2(v.re, v.im);
+    }
+    __syncthreads();
+    for (int jj = ty; jj < 32; jj += 8) {
+        const int j = j0 + jj;
+        if (j >= t.N) continue;
+        const float sc = f16_scale(t.bmax[j]);
+        const int k = k0 + tx;
+        if (k == 0) t.sb[j] = 1.f / sc;
+        const float br = tile[tx][jj].x * sc, bi = tile[tx][jj].y * sc;
+        __half rh, rl, ih, il, nih, nil;
+        split_f16(br, rh, rl);
+        split_f16(bi, ih, il);
+        split_f16(-bi, nih, nil);
+        const long long o0 = (long long)(2 * j) * t.Kr + 2 * k, o1 = o0 + t.Kr;   // in halves
+        __half2 *bh = reinterpret_cast<__half2 *>(t.bhi), *bl = reinterpret_cast<__half2 *>(t.blo);
+        bh[o0 >> 1] = __halves2half2(rh, nih);
+        bl[o0 >> 1] = __halves2half2(rl, nil);
+        bh[o1 >> 1] = __halves2half2(ih, rh);
+        bl[o1 >> 1] = __halves2half2(il, rl);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // the tensor-core kernel
 // ---------------------------------------------------------------------------
@@ -155,10 +316,13 @@ __device__ __forceinline__ const TcTask *tc_tile(const TcTask *__restrict__ task
 // wait is bounded: a role that times out sets *err and stops, the others then
 // time out in turn, and before TMEM is released the MMA lane waits for its
 // issued MMAs and the producer for its issued copies.
+template <bool F16>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_tc_gemm(const TcTask *__restrict__ tasks, int ntasks, long long ntiles, const CUtensorMap *__restrict__ maps,
               int *err)
 {
+    // elements of one 128-byte stage row: 32 TF32 or 64 FP16 values
+    constexpr int EK = F16 ? 2 * TC_BK : TC_BK;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE_BYTES);
@@ -200,17 +364,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             int m0, n0r;
             const TcTask *t = tc_tile(tasks, ntasks, gt, m0, n0r);
             const CUtensorMap *mp = maps + t->map0;
-            const int nk = t->Kr / TC_BK;
+            const int nk = t->Kr / EK;
             for (int ks = 0; ks < nk; ks++, gks++) {
                 const int s = (int)(gks % TC_STAGES);
                 const uint32_t ph = (uint32_t)((gks / TC_STAGES) & 1) ^ 1u;
                 if (!mbar_wait(&empty[s], ph)) { atomicCAS(err, 0, 1); ok = false; break; }
                 uint8_t *st = smem + s * TC_STAGE_BYTES;
                 mbar_expect_tx(&full[s], TC_STAGE_BYTES);
-                tma_load_2d(st, mp + 0, ks * TC_BK, m0, &full[s]);
-                tma_load_2d(st + TC_A_BYTES, mp + 1, ks * TC_BK, m0, &full[s]);
-                tma_load_2d(st + 2 * TC_A_BYTES, mp + 2, ks * TC_BK, n0r, &full[s]);
-                tma_load_2d(st + 2 * TC_A_BYTES + TC_B_BYTES, mp + 3, ks * TC_BK, n0r, &full[s]);
+                tma_load_2d(st, mp + 0, ks * EK, m0, &full[s]);
+                tma_load_2d(st + TC_A_BYTES, mp + 1, ks * EK, m0, &full[s]);
+                tma_load_2d(st + 2 * TC_A_BYTES, mp + 2, ks * EK, n0r, &full[s]);
+                tma_load_2d(st + 2 * TC_A_BYTES + TC_B_BYTES, mp + 3, ks * EK, n0r, &full[s]);
             }
         }
         // the last copy issued into each stage has landed before the CTA exits
@@ -221,14 +385,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer ----------------
-        constexpr uint32_t idesc = tf32_idesc(TC_BM, TC_BNR);
+        constexpr uint32_t idesc = F16 ? f16_idesc(TC_BM, TC_BNR) : tf32_idesc(TC_BM, TC_BNR);
         long long gks = 0;
         int it = 0;
         bool ok = true;
         for (long long gt = blockIdx.x; gt < ntiles && ok; gt += gridDim.x, it++) {
             int m0, n0r;
             const TcTask *t = tc_tile(tasks, ntasks, gt, m0, n0r);
-            const int nk = t->Kr / TC_BK;
+            const int nk = t->Kr / EK;
             const int b = it & 1;
             const uint32_t use = (uint32_t)(it >> 1);
             if (!mbar_wait(&tempty[b], (use & 1u) ^ 1u)) { atomicCAS(err, 0, 4); ok = false; break; }
@@ -244,12 +408,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const uint32_t b_hi = base + 2 * TC_A_BYTES, b_lo = b_hi + TC_B_BYTES;
 #pragma unroll
                 for (int kk = 0; kk < TC_BK / 8; kk++) {
-                    const uint32_t off = kk * 32;   // 8 TF32 elements = 32 bytes along K
+                    const uint32_t off = kk * 32;   // 32 bytes along K: 8 TF32 or 16 FP16 elements
                     const uint64_t dah = sw128_desc(a_hi + off), dal = sw128_desc(a_lo + off);
                     const uint64_t dbh = sw128_desc(b_hi + off), dbl = sw128_desc(b_lo + off);
-                    umma_tf32(dacc, dah, dbh, idesc, (ks | kk) != 0);
-                    umma_tf32(dacc, dah, dbl, idesc, 1);
-                    umma_tf32(dacc, dal, dbh, idesc, 1);
+                    if constexpr (F16) {
+                        umma_f16(dacc, dah, dbh, idesc, (ks | kk) != 0);
+                        umma_f16(dacc, dah, dbl, idesc, 1);
+                        umma_f16(dacc, dal, dbh, idesc, 1);
+                    } else {
+                        umma_tf32(dacc, dah, dbh, idesc, (ks | kk) != 0);
+                        umma_tf32(dacc, dah, dbl, idesc, 1);
+                        umma_tf32(dacc, dal, dbh, idesc, 1);
+                    }
                 }
                 umma_commit(&empty[s]);
             }
@@ -294,9 +464,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     float cv[32];
 #pragma unroll
                     for (int r = 0; r < 32; r++) cv[r] = r < nr ? cp[r * ldf] : 0.f;
+                    if constexpr (F16) {
+                        // undo the row and column scales (powers of two: exact)
+                        const float sbj = t->sb[cf >> 1];
+                        const float *sar = t->sa + row0;
 #pragma unroll
-                    for (int r = 0; r < 32; r++)
-                        if (r < nr) cp[r * ldf] = cv[r] - tb[r * 33 + lane];
+                        for (int r = 0; r < 32; r++)
+                            if (r < nr) cp[r * ldf] = cv[r] - tb[r * 33 + lane] * (sar[r] * sbj);
+                    } else {
+#pragma unroll
+                        for (int r = 0; r < 32; r++)
+                            if (r < nr) cp[r * ldf] = cv[r] - tb[r * 33 + lane];
+                    }
                 }
                 __syncwarp();
             }
@@ -334,11 +513,19 @@ bool tc_eligible(const GemmTask<float> &g)
     return !g.brow && !g.crow && !g.conjA && g.M >= 64 && g.N >= 96 && g.K >= 32;
 }
 
+// f16 mode unless WT3D_TC_F16=0 (then the TF32 split)
+static bool tc_f16_mode()
+{
+    static const bool on = !(getenv("WT3D_TC_F16") && getenv("WT3D_TC_F16")[0] == '0');
+    return on;
+}
+
 int tc_build_launch(TcLaunch &L, const GemmTask<float> *g, int n, float *ws)
 {
     std::vector<TcTask> tasks(n);
     std::vector<CUtensorMap> maps(4 * n);
-    long long off = 0, tiles = 0, aw = 0, bw = 0;
+    const bool f16 = tc_f16_mode();
+    long long off = 0, tiles = 0, aw = 0, bw = 0, arows = 0;
     for (int i = 0; i < n; i++) {
         TcTask &t = tasks[i];
         t.A = g[i].A; t.lda = g[i].lda;
@@ -346,7 +533,9 @@ int tc_build_launch(TcLaunch &L, const GemmTask<float> *g, int n, float *ws)
         t.C = g[i].C; t.ldc = g[i].ldc;
         t.M = g[i].M; t.N = g[i].N; t.K = g[i].K;
         t.Kr = (int)align_up(2LL * t.K, 2 * TC_BK);   // whole 32-complex tiles for the B transpose
-        const long long asz = align_up((long long)t.M * t.Kr, 256), bsz = align_up(2LL * t.N * t.Kr, 256);
+        // operand sizes in floats (an FP16 pair takes one float's room)
+        const long long asz = align_up((long long)t.M * t.Kr / (f16 ? 2 : 1), 256);
+        const long long bsz = align_up(2LL * t.N * t.Kr / (f16 ? 2 : 1), 256);
         t.ahi = ws + off; off += asz;
         t.alo = ws + off; off += asz;
         t.bhi = ws + off; off += bsz;
@@ -358,18 +547,44 @@ int tc_build_launch(TcLaunch &L, const GemmTask<float> *g, int n, float *ws)
         aw += (long long)t.M * (t.Kr / 2);
         t.b_work0 = bw;
         bw += (long long)((t.N + 31) / 32) * (t.Kr / 64);
+        t.a_row0 = arows;
+        arows += t.M;
         t.map0 = 4 * i;
         int rc;
-        if ((rc = make_map(&maps[4 * i + 0], t.ahi, t.M, t.Kr, TC_BM)) ||
-            (rc = make_map(&maps[4 * i + 1], t.alo, t.M, t.Kr, TC_BM)) ||
-            (rc = make_map(&maps[4 * i + 2], t.bhi, 2LL * t.N, t.Kr, TC_BNR)) ||
-            (rc = make_map(&maps[4 * i + 3], t.blo, 2LL * t.N, t.Kr, TC_BNR)))
+        if (f16) {
+            if ((rc = make_map_f16(&maps[4 * i + 0], t.ahi, t.M, t.Kr, TC_BM)) ||
+                (rc = make_map_f16(&maps[4 * i + 1], t.alo, t.M, t.Kr, TC_BM)) ||
+                (rc = make_map_f16(&maps[4 * i + 2], t.bhi, 2LL * t.N, t.Kr, TC_BNR)) ||
+                (rc = make_map_f16(&maps[4 * i + 3], t.blo, 2LL * t.N, t.Kr, TC_BNR)))
+                return rc;
+        } else if ((rc = make_map(&maps[4 * i + 0], t.ahi, t.M, t.Kr, TC_BM)) ||
+                   (rc = make_map(&maps[4 * i + 1], t.alo, t.M, t.Kr, TC_BM)) ||
+                   (rc = make_map(&maps[4 * i + 2], t.bhi, 2LL * t.N, t.Kr, TC_BNR)) ||
+                   (rc = make_map(&maps[4 * i + 3], t.blo, 2LL * t.N, t.Kr, TC_BNR))) {
             return rc;
+        }
     }
+    // f16 mode: the scale words of all tasks after the operands, column
+    // maxima contiguous (one memset clears them)
+    L.bmax0 = nullptr;
+    L.nbmax = 0;
+    if (f16) {
+        unsigned *bm = reinterpret_cast<unsigned *>(ws + off);
+        for (auto &t : tasks) { t.bmax = bm + L.nbmax; L.nbmax += t.N; }
+        L.bmax0 = bm;
+        off += align_up(L.nbmax, 64);
+        for (auto &t : tasks) {
+            t.amax = reinterpret_cast<unsigned *>(ws + off); off += align_up(t.M, 64);
+            t.sa = ws + off; off += align_up(t.M, 64);
+            t.sb = ws + off; off += align_up(t.N, 64);
+        }
+    }
+    L.f16 = f16;
     L.ntasks = n;
     L.tiles = tiles;
     L.a_work = aw;
     L.b_tiles = bw;
+    L.a_rows = arows;
     int rc;
     if ((rc = L.tasks.upload(tasks))) return rc;
     std::vector<unsigned char> raw(maps.size() * sizeof(CUtensorMap));
@@ -381,6 +596,14 @@ int tc_build_launch(TcLaunch &L, const GemmTask<float> *g, int n, float *ws)
 void tc_split(const TcLaunch &L, cudaStream_t st)
 {
     if (L.ntasks == 0) return;
+    if (L.f16) {
+        cudaMemsetAsync(L.bmax0, 0, sizeof(unsigned) * L.nbmax, st);
+        k_amax<<<ceil_div(L.a_rows * 32, 256), 256, 0, st>>>(L.tasks.p, L.ntasks, L.a_rows);
+        k_bmax<<<(unsigned)L.b_tiles, 256, 0, st>>>(L.tasks.p, L.ntasks, L.b_tiles);
+        k_split_a_f16<<<ceil_div(L.a_work, 256), 256, 0, st>>>(L.tasks.p, L.ntasks, L.a_work);
+        k_split_b_f16<<<(unsigned)L.b_tiles, 256, 0, st>>>(L.tasks.p, L.ntasks, L.b_tiles);
+        return;
+    }
     k_split_a<<<ceil_div(L.a_work, 256), 256, 0, st>>>(L.tasks.p, L.ntasks, L.a_work);
     k_split_b<<<(unsigned)L.b_tiles, 256, 0, st>>>(L.tasks.p, L.ntasks, L.b_tiles);
 }
@@ -405,14 +628,18 @@ void tc_mma(const TcLaunch &L, int *err, cudaStream_t st)
     if (L.ntasks == 0) return;
     const int sms = std::max(1, num_sms() - g_sm_reserve.load());
     const long long grid = std::min<long long>(L.tiles, sms);
-    k_tc_gemm<<<(unsigned)grid, TC_THREADS, TC_SMEM, st>>>(L.tasks.p, L.ntasks, L.tiles,
-                                                           reinterpret_cast<const CUtensorMap *>(L.maps.p), err);
+    const CUtensorMap *maps = reinterpret_cast<const CUtensorMap *>(L.maps.p);
+    if (L.f16)
+        k_tc_gemm<true><<<(unsigned)grid, TC_THREADS, TC_SMEM, st>>>(L.tasks.p, L.ntasks, L.tiles, maps, err);
+    else
+        k_tc_gemm<false><<<(unsigned)grid, TC_THREADS, TC_SMEM, st>>>(L.tasks.p, L.ntasks, L.tiles, maps, err);
 }
 
 int tc_init()
 {
     // idempotent; safe to call from several threads
-    WT_CUDA(cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    WT_CUDA(cudaFuncSetAttribute(k_tc_gemm<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    WT_CUDA(cudaFuncSetAttribute(k_tc_gemm<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     if (!encode_fn()) { set_error("cuTensorMapEncodeTiled unavailable"); return WT3D_ERR_CUDA; }
     return WT3D_OK;
 }

@@ -77,6 +77,21 @@ __device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t da, uint64_t
         "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
 
+// kind::f16 instruction descriptor: FP32 accumulate, FP16 A and B (type
+// code 0), both K-major.
+__host__ __device__ constexpr uint32_t f16_idesc(int M, int N)
+{
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
 __device__ __forceinline__ void umma_commit(uint64_t *bar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -148,6 +163,25 @@ inline int make_map(CUtensorMap *m, float *base, long long rows, int Kr, int box
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+        return WT3D_ERR_CUDA;
+    }
+    return WT3D_OK;
+}
+
+// The same map over FP16 operand rows of Kr halves: 64-half (128-byte) boxes.
+inline int make_map_f16(CUtensorMap *m, void *base, long long rows, int Kr, int box_rows)
+{
+    auto fn = encode_fn();
+    if (!fn) { set_error("cuTensorMapEncodeTiled unavailable"); return WT3D_ERR_CUDA; }
+    cuuint64_t gdim[2] = {(cuuint64_t)Kr, (cuuint64_t)rows};
+    cuuint64_t gstr[1] = {(cuuint64_t)Kr * 2};
+    cuuint32_t box[2] = {64u, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, gdim, gstr, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled (f16) failed: " + std::to_string((int)r));
         return WT3D_ERR_CUDA;
     }
     return WT3D_OK;
