@@ -42,6 +42,8 @@ struct Schedule {
     DevVec<ColTask> col;
     DevVec<GemmTask<T>> gemm;
     DevVec<EATask> ea;
+    DevVec<StepTask> step;                                    // fused substitution steps
+    DevVec<cx<T>> zs;                                         // their per-front scratch slots
     std::vector<std::vector<GemmTask<float>>> tc_pending;   // tensor-core task lists, built after allocation
     std::vector<std::unique_ptr<TcLaunch>> tc;
     std::vector<std::vector<GemmTask<float>>> ts_pending;   // tall-skinny tensor-core task lists (solves)
@@ -188,6 +190,8 @@ public:
                                      (int)(sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1))));
             }
             cudaFuncSetAttribute(k_diag_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1))));
+            cudaFuncSetAttribute(k_sub_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1))));
         });
         return build_factor_schedule();
@@ -570,45 +574,46 @@ public:
         } building(building_solve);
         const int ldx = MAXRHS;
         const int nlev = (int)sym.levels.size();
-        size_t smd = sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1));
-        auto diag_launch = [&](size_t p0, int mode) {
-            int np = (int)(hp.size() - p0);
-            if (!np) return;
-            sc->launches.push_back({[psc, this, p0, np, smd, m, mode, Xp, ldx](cudaStream_t st) {
-                k_diag_solve<T><<<np, 256, smd, st>>>(psc->panel.p + p0, fr.p, dinv.p, ipiv.p, Xp, ldx, m, mode);
-            }, LK_DIAG, 0, (double)np * (KB * KB + 2.0 * KB * m) * sizeof(cx<T>)});
-        };
         // Two-level blocking of the in-front substitutions, like the
         // factorisation's: inside each WS-wide outer block the KB panels are
-        // solved one by one (diagonal tile product, then a K = KB update of
-        // the block's own rows), and the rows outside the block receive one
-        // K = WS update, which the tall-skinny tensor-core kernel takes.
+        // solved one by one, each step one fused launch (k_sub_step: the
+        // diagonal-tile product and the update of the block's other rows);
+        // the rows outside the block then receive one K = WS update, which
+        // the tall-skinny tensor-core kernel takes.
+        std::vector<StepTask> hs;
+        size_t smd_step = sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1));
+        int maxslots = 0;
+        // one fused launch over the step tasks [s0, end)
+        auto step_launch = [&](size_t s0, int mode) {
+            const int ns = (int)(hs.size() - s0);
+            if (!ns) return;
+            sc->launches.push_back({[psc, this, s0, ns, smd_step, m, mode, Xp, ldx](cudaStream_t st) {
+                k_sub_step<T><<<ns, 256, smd_step, st>>>(psc->step.p + s0, fr.p, fac.p, dinv.p, ipiv.p, Xp, ldx, m,
+                                                         mode, psc->zs.p);
+            }, LK_DIAG, 0, (double)ns * (KB * KB + 2.0 * KB * m) * sizeof(cx<T>)});
+        };
+        // the tasks of one panel step of front f (slot = its position in the level)
+        auto add_step = [&](int f, int slot, int k, int kprev, int u0, int u1) {
+            const int nup = u1 > u0 ? (u1 - u0 + SUB_RB - 1) / SUB_RB : 0;
+            hs.push_back(StepTask{f, k, 0, 0, nup ? 0 : 3, kprev, slot});
+            for (int r = u0; r < u1; r += SUB_RB) hs.push_back(StepTask{f, k, r, std::min(r + SUB_RB, u1), 1, -1, slot});
+        };
         // ---- forward sweep: leaves to root ----
         for (int L = nlev - 1; L >= 0; L--) {
             const std::vector<int> &fl = sym.levels[L];
+            maxslots = std::max(maxslots, (int)fl.size());
             int maxp = 0;
             for (int f : fl) maxp = std::max(maxp, sym.fronts[f].p);
             for (int c0 = 0; c0 < maxp; c0 += WS) {
                 for (int k = c0; k < std::min(c0 + WS, maxp); k += KB) {
-                    size_t p0 = hp.size(), g0 = hg.size();
-                    long long tiles = 0;
-                    for (int f : fl) {
-                        const Front &Fr = sym.fronts[f];
+                    const size_t s0 = hs.size();
+                    for (int si = 0; si < (int)fl.size(); si++) {
+                        const Front &Fr = sym.fronts[fl[si]];
                         if (Fr.p <= k) continue;
-                        const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k), k2 = k + kb;
-                        const int cend = std::min(c0 + WS, Fr.p);
-                        hp.push_back(PanelTask{f, k});
-                        cx<T> *Pb = F + Fr.fac_off;
-                        cx<T> *Y = Xp + (long long)Fr.first * ldx;
-                        if (!adjoint)   // Y[k2:cend] -= L[k2:cend, k:k2] Y[k:k2]
-                            add_gemm(hg, tiles, Pb + (long long)k2 * nf + k, nf, Y + (long long)k * ldx, ldx,
-                                     Y + (long long)k2 * ldx, ldx, cend - k2, m, kb);
-                        else            // Y[k2:cend] -= U[k:k2, k2:cend]^H Y[k:k2]
-                            add_gemm(hg, tiles, Pb + (long long)k * nf + k2, nf, Y + (long long)k * ldx, ldx,
-                                     Y + (long long)k2 * ldx, ldx, cend - k2, m, kb, nullptr, nullptr, 1);
+                        const int k2 = k + std::min(KB, Fr.p - k), cend = std::min(c0 + WS, Fr.p);
+                        add_step(fl[si], si, k, k > c0 ? k - KB : -1, k2, cend);
                     }
-                    diag_launch(p0, adjoint ? 2 : 0);
-                    push_gemm_launch(*sc, hg, g0, tiles);
+                    step_launch(s0, adjoint ? 2 : 0);
                 }
                 // rows below the outer block
                 size_t g0 = hg.size();
@@ -666,59 +671,22 @@ public:
             }
             push_gemm_launch(*sc, hg, g0, tiles);
             for (int c0 = (maxp - 1) / WS * WS; c0 >= 0; c0 -= WS) {
-                if (adjoint) {
-                    // Y[c0:cend] -= L[cend:p, c0:cend]^H Y[cend:p]  (rows below the block, solved already)
-                    size_t g1 = hg.size();
-                    long long t1 = 0;
-                    for (int f : fl) {
-                        const Front &Fr = sym.fronts[f];
-                        if (Fr.p <= c0) continue;
-                        const int nf = Fr.nf(), cend = std::min(c0 + WS, Fr.p);
-                        if (Fr.p <= cend) continue;
-                        cx<T> *Pb = F + Fr.fac_off;
-                        cx<T> *Y = Xp + (long long)Fr.first * ldx;
-                        add_gemm(hg, t1, Pb + (long long)cend * nf + c0, nf, Y + (long long)cend * ldx, ldx,
-                                 Y + (long long)c0 * ldx, ldx, cend - c0, m, Fr.p - cend, nullptr, nullptr, 1);
-                    }
-                    push_gemm_launch(*sc, hg, g1, t1);
-                }
                 const int nsteps = (std::min(c0 + WS, maxp) - c0 + KB - 1) / KB;
                 for (int s = nsteps - 1; s >= 0; s--) {
                     const int k = c0 + s * KB;
-                    size_t p0 = hp.size(), g1 = hg.size();
-                    long long t1 = 0;
-                    for (int f : fl) {
-                        const Front &Fr = sym.fronts[f];
+                    const size_t s0 = hs.size();
+                    for (int si = 0; si < (int)fl.size(); si++) {
+                        const Front &Fr = sym.fronts[fl[si]];
                         if (Fr.p <= k) continue;
-                        const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k), k2 = k + kb;
                         const int cend = std::min(c0 + WS, Fr.p);
-                        cx<T> *Pb = F + Fr.fac_off;
-                        cx<T> *Y = Xp + (long long)Fr.first * ldx;
-                        hp.push_back(PanelTask{f, k});
-                        if (adjoint)   // Y[k:k2] -= L[k2:cend, k:k2]^H Y[k2:cend]   (before the diagonal solve)
-                            add_gemm(hg, t1, Pb + (long long)k2 * nf + k, nf, Y + (long long)k2 * ldx, ldx,
-                                     Y + (long long)k * ldx, ldx, kb, m, cend - k2, nullptr, nullptr, 1);
+                        // the rows above the panel inside the block (right-looking for both modes)
+                        add_step(fl[si], si, k, k + KB < cend ? k + KB : -1, c0, k);
                     }
-                    if (!adjoint) {
-                        diag_launch(p0, 1);
-                        // Y[c0:k] -= U[c0:k, k:k2] Y[k:k2]
-                        for (int f : fl) {
-                            const Front &Fr = sym.fronts[f];
-                            if (Fr.p <= k || k == c0) continue;
-                            const int nf = Fr.nf(), kb = std::min(KB, Fr.p - k);
-                            cx<T> *Pb = F + Fr.fac_off;
-                            cx<T> *Y = Xp + (long long)Fr.first * ldx;
-                            add_gemm(hg, t1, Pb + (long long)c0 * nf + k, nf, Y + (long long)k * ldx, ldx,
-                                     Y + (long long)c0 * ldx, ldx, k - c0, m, kb);
-                        }
-                        push_gemm_launch(*sc, hg, g1, t1);
-                    } else {
-                        push_gemm_launch(*sc, hg, g1, t1);
-                        diag_launch(p0, 3);
-                    }
+                    step_launch(s0, adjoint ? 3 : 1);
                 }
-                if (!adjoint && c0 > 0) {
-                    // rows above the block: Y[0:c0] -= U[0:c0, c0:cend] Y[c0:cend]
+                if (c0 > 0) {
+                    // rows above the block:  Y[0:c0] -= U[0:c0, c0:cend] Y[c0:cend]
+                    //                 (adjoint: Y[0:c0] -= L[c0:cend, 0:c0]^H Y[c0:cend])
                     size_t g1 = hg.size();
                     long long t1 = 0;
                     for (int f : fl) {
@@ -727,12 +695,17 @@ public:
                         const int nf = Fr.nf(), cend = std::min(c0 + WS, Fr.p);
                         cx<T> *Pb = F + Fr.fac_off;
                         cx<T> *Y = Xp + (long long)Fr.first * ldx;
-                        add_gemm(hg, t1, Pb + c0, nf, Y + (long long)c0 * ldx, ldx, Y, ldx, c0, m, cend - c0);
+                        if (!adjoint)
+                            add_gemm(hg, t1, Pb + c0, nf, Y + (long long)c0 * ldx, ldx, Y, ldx, c0, m, cend - c0);
+                        else
+                            add_gemm(hg, t1, Pb + (long long)c0 * nf, nf, Y + (long long)c0 * ldx, ldx, Y, ldx, c0, m,
+                                     cend - c0, nullptr, nullptr, 1);
                     }
                     push_gemm_launch(*sc, hg, g1, t1);
                 }
             }
         }
+        if (sc->step.upload(hs) || sc->zs.alloc((size_t)std::max(maxslots, 1) * KB * MAXRHS)) return nullptr;
         if (sc->panel.upload(hp) || sc->gemm.upload(hg) || finish_tc(*sc) || finish_ts(*sc)) return nullptr;
         Schedule<T> *ret = sc.get();
         ssched[adjoint][m] = std::move(sc);

@@ -29,6 +29,13 @@ struct PanelTask { int f, k; };
 struct RowTask { int f, k, c0; };
 struct ColTask { int f, k, r0, which; };
 struct EATask { int child, parent; long long row0; };
+// One CTA of a fused substitution step (k_sub_step): panel k of front f.
+// role 0: flush the previous panel's solved rows (kprev >= 0) from the front's
+// scratch slot into X, then store this panel's solved rows in the slot;
+// role 1: update rows [r0, r1) with this panel's solved rows;
+// role 3: as role 0 for a front with no update CTA in this step (its last
+// panel of the block): the solved rows go straight into X.
+struct StepTask { int f, k, r0, r1, role, kprev, slot; };
 
 template <class T>
 struct GemmTask {
@@ -144,6 +151,26 @@ __global__ void k_extend_add(const EATask *__restrict__ tasks, int ntasks, long 
     }
 }
 
+// Row order of panel k after its LINPACK-style interchanges: idx[i] is the
+// stored row that lands at position i.  The kb pivots are read in parallel
+// into piv_s first (one load each, not a chain of dependent loads by one
+// thread); all threads of the block must call this.
+__device__ __forceinline__ void panel_order(const int *__restrict__ ipiv, int first, int k, int kb, bool pivoted,
+                                            int *idx, int *piv_s)
+{
+    const int tid = threadIdx.x;
+    if (pivoted && tid < kb) piv_s[tid] = ipiv[first + k + tid] - k;
+    __syncthreads();
+    if (tid == 0) {
+        for (int i = 0; i < kb; i++) idx[i] = i;
+        if (pivoted)
+            for (int j = 0; j < kb; j++) {
+                const int pv = piv_s[j];
+                const int a = idx[j]; idx[j] = idx[pv]; idx[pv] = a;
+            }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // panel: LU of the KB x KB diagonal tile with partial pivoting inside the tile
 // ---------------------------------------------------------------------------
@@ -164,6 +191,7 @@ __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tas
     const int LD = KB + 1;
     cx<T> *D = fac + F.fac + (long long)k * nf + k;
     const int tid = threadIdx.x;
+    #pragma unroll 8   // several loads in flight per thread
     for (int idx = tid; idx < kb * kb; idx += blockDim.x) {
         int i = idx / kb, j = idx % kb;
         S[i * LD + j] = D[(long long)i * nf + j];
@@ -243,6 +271,7 @@ __global__ void __launch_bounds__(2 * KB) k_tile_inverse(const PanelTask *__rest
     const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
     const cx<T> *D = fac + F.fac + (long long)k * nf + k;
     const int tid = threadIdx.x;
+    #pragma unroll 8   // several loads in flight per thread
     for (int idx = tid; idx < kb * kb; idx += blockDim.x) {
         const int i = idx / kb, j = idx % kb;
         S[i * LD + j] = D[(long long)i * nf + j];
@@ -287,25 +316,21 @@ __global__ void __launch_bounds__(TRW) k_trsm_row(const RowTask *__restrict__ ta
     extern __shared__ __align__(16) unsigned char smraw[];
     cx<T> *L = reinterpret_cast<cx<T> *>(smraw);          // KB x (KB+1)
     cx<T> *Bt = L + KB * (KB + 1);                       // KB x (TRW+1)
-    __shared__ int idx[KB];
+    __shared__ int idx[KB], piv_s[KB];
     const RowTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
     const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
     const int c0 = t.c0, nc = min(TRW, nf - c0);
     const int tid = threadIdx.x;
     cx<T> *base = fac + F.fac + (long long)k * nf;
+    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < kb * kb; q += blockDim.x) {
         int i = q / kb, j = q % kb;
         L[i * (KB + 1) + j] = base[(long long)i * nf + k + j];
     }
-    if (tid == 0) {
-        for (int i = 0; i < kb; i++) idx[i] = i;
-        for (int j = 0; j < kb; j++) {
-            int pv = ipiv[F.first + k + j] - k;
-            int a = idx[j]; idx[j] = idx[pv]; idx[pv] = a;
-        }
-    }
+    panel_order(ipiv, F.first, k, kb, true, idx, piv_s);
     __syncthreads();
+    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < kb * nc; q += blockDim.x) {
         int i = q / nc, c = q % nc;
         Bt[i * (TRW + 1) + c] = base[(long long)idx[i] * nf + c0 + c];
@@ -342,6 +367,7 @@ __global__ void __launch_bounds__(TCR) k_trsm_col(const ColTask *__restrict__ ta
     const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
     const int tid = threadIdx.x;
     const cx<T> *D = fac + F.fac + (long long)k * nf + k;
+    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < kb * kb; q += blockDim.x) {
         int i = q / kb, j = q % kb;
         U[i * (KB + 1) + j] = D[(long long)i * nf + j];
@@ -358,6 +384,7 @@ __global__ void __launch_bounds__(TCR) k_trsm_col(const ColTask *__restrict__ ta
         ld = F.p;
         nr = min(TCR, F.b - t.r0);
     }
+    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < nr * kb; q += blockDim.x) {
         int r = q / kb, j = q % kb;
         Xs[r * (KB + 1) + j] = xb[(long long)r * ld + j];
@@ -397,25 +424,21 @@ __global__ void __launch_bounds__(TRW) k_trsm_row_reg(const RowTask *__restrict_
     extern __shared__ __align__(16) unsigned char smraw[];
     cx<float> *L = reinterpret_cast<cx<float> *>(smraw);          // KB x (KB+1)
     cx<float> *Bt = L + KB * (KB + 1);                           // KB x (TRW+1)
-    __shared__ int idx[KB];
+    __shared__ int idx[KB], piv_s[KB];
     const RowTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
     const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
     const int c0 = t.c0, nc = min(TRW, nf - c0);
     const int tid = threadIdx.x;
     cx<float> *base = fac + F.fac + (long long)k * nf;
+    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < KB * KB; q += blockDim.x) {
         const int i = q / KB, j = q % KB;
         L[i * (KB + 1) + j] = (i < kb && j < kb) ? base[(long long)i * nf + k + j] : cx<float>(0.f, 0.f);
     }
-    if (tid == 0) {
-        for (int i = 0; i < kb; i++) idx[i] = i;
-        for (int j = 0; j < kb; j++) {
-            int pv = ipiv[F.first + k + j] - k;
-            int a = idx[j]; idx[j] = idx[pv]; idx[pv] = a;
-        }
-    }
+    panel_order(ipiv, F.first, k, kb, true, idx, piv_s);
     __syncthreads();
+    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < kb * nc; q += blockDim.x) {
         const int i = q / nc, c = q % nc;
         Bt[i * (TRW + 1) + c] = base[(long long)idx[i] * nf + c0 + c];
@@ -457,6 +480,7 @@ __global__ void __launch_bounds__(TCR) k_trsm_col_reg(const ColTask *__restrict_
     const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
     const int tid = threadIdx.x;
     const cx<float> *D = fac + F.fac + (long long)k * nf + k;
+    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < KB * KB; q += blockDim.x) {
         const int i = q / KB, j = q % KB;
         U[i * (KB + 1) + j] = (i < kb && j < kb) ? D[(long long)i * nf + j]
@@ -474,6 +498,7 @@ __global__ void __launch_bounds__(TCR) k_trsm_col_reg(const ColTask *__restrict_
         ld = F.p;
         nr = min(TCR, F.b - t.r0);
     }
+    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < nr * kb; q += blockDim.x) {
         const int r = q / kb, j = q % kb;
         Xs[r * (KB + 1) + j] = xb[(long long)r * ld + j];
@@ -719,7 +744,7 @@ __global__ void __launch_bounds__(256) k_diag_solve(const PanelTask *__restrict_
     extern __shared__ __align__(16) unsigned char smraw[];
     cx<T> *Ms = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1): the operator of this mode
     cx<T> *Ys = Ms + KB * (KB + 1);                 // KB x (MAXRHS+1)
-    __shared__ int idx[KB];
+    __shared__ int idx[KB], piv_s[KB];
     const PanelTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
     const int k = t.k, kb = min(KB, F.p - k);
@@ -727,21 +752,16 @@ __global__ void __launch_bounds__(256) k_diag_solve(const PanelTask *__restrict_
     const cx<T> *Li = inv + (long long)(F.pan + k / KB) * (2 * KB * KB);
     const cx<T> *Mi = (mode == 0 || mode == 3) ? Li : Li + KB * KB;
     const bool herm = mode >= 2;
+    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < KB * KB; q += blockDim.x) {
         const int i = q / KB, j = q % KB;
         Ms[i * (KB + 1) + j] = herm ? conj(Mi[j * KB + i]) : Mi[i * KB + j];
     }
-    if (tid == 0) {
-        for (int i = 0; i < kb; i++) idx[i] = i;
-        if (mode == 0 || mode == 3)
-            for (int j = 0; j < kb; j++) {
-                int pv = ipiv[F.first + k + j] - k;
-                int a = idx[j]; idx[j] = idx[pv]; idx[pv] = a;
-            }
-    }
+    panel_order(ipiv, F.first, k, kb, mode == 0 || mode == 3, idx, piv_s);
     __syncthreads();
     cx<T> *Y = X + (long long)(F.first + k) * ldx;
     const int LY = MAXRHS + 1;
+    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < kb * m; q += blockDim.x) {
         const int i = q / m, c = q % m;
         Ys[i * LY + c] = Y[(long long)(mode == 0 ? idx[i] : i) * ldx + c];
@@ -764,6 +784,118 @@ __global__ void __launch_bounds__(256) k_diag_solve(const PanelTask *__restrict_
 #pragma unroll
     for (int r = 0; r < PER; r++)
         if (oi[r] < kb) Y[(long long)(mode == 3 ? idx[oi[r]] : oi[r]) * ldx + oc[r]] = acc[r];
+}
+
+// ---------------------------------------------------------------------------
+// Fused substitution step: the diagonal-tile product of panel k and the update
+// of the outer block's other rows, in one launch per panel step (the panel
+// steps of a block form a dependent chain; one launch instead of two halves
+// its latency).  Every CTA of a front computes the panel's solved rows
+//   mode 0  Z = L_D^{-1} P y          mode 1  Z = U_D^{-1} y
+//   mode 2  Z = U_D^{-H} y            mode 3  Z = P^T L_D^{-H} y
+// from the panel rows y of X (which no CTA of the launch writes) into shared
+// memory; update CTAs then subtract its contribution from their rows,
+//   mode 0  y_r -= L[r, k:k2] Z       mode 1  y_r -= U[r, k:k2] Z
+//   mode 2  y_r -= U[k:k2, r]^H Z     mode 3  y_r -= L[k:k2, r]^H Z
+// (rows below the panel for the forward modes 0/2, above it for 1/3), and the
+// role-0 CTA leaves Z in the front's scratch slot; the next step's role-0 CTA
+// (or a flush) writes it into X once no CTA reads those rows any more.
+// ---------------------------------------------------------------------------
+constexpr int SUB_RB = 64;   // rows per update CTA
+template <class T>
+__global__ void __launch_bounds__(256) k_sub_step(const StepTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
+                                                  const cx<T> *__restrict__ fac, const cx<T> *__restrict__ inv,
+                                                  const int *__restrict__ ipiv, cx<T> *__restrict__ X, int ldx, int m,
+                                                  int mode, cx<T> *__restrict__ zs)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    cx<T> *Ms = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1): the tile operator, then the update block
+    cx<T> *Ys = Ms + KB * (KB + 1);                 // KB x (MAXRHS+1): panel rows, then Z
+    __shared__ int idx[KB], piv_s[KB];
+    const StepTask t = tasks[blockIdx.x];
+    const FrontDev F = fr[t.f];
+    const int tid = threadIdx.x;
+    const int nf = F.p + F.b;
+    const int LY = MAXRHS + 1;
+    cx<T> *Y = X + (long long)F.first * ldx;
+    cx<T> *slot = zs + (long long)t.slot * (KB * MAXRHS);
+    if (t.role != 1 && t.kprev >= 0) {   // roles 0 and 3
+        const int kbp = min(KB, F.p - t.kprev);
+        #pragma unroll 8   // several loads in flight per thread
+        for (int q = tid; q < kbp * m; q += blockDim.x) {
+            const int i = q / m, c = q % m;
+            Y[(long long)(t.kprev + i) * ldx + c] = slot[i * MAXRHS + c];
+        }
+    }
+    const int k = t.k, kb = min(KB, F.p - k);
+    const cx<T> *Li = inv + (long long)(F.pan + k / KB) * (2 * KB * KB);
+    const cx<T> *Mi = (mode == 0 || mode == 3) ? Li : Li + KB * KB;
+    const bool herm = mode >= 2;
+    #pragma unroll 8   // several loads in flight per thread
+    for (int q = tid; q < KB * KB; q += blockDim.x) {
+        const int i = q / KB, j = q % KB;
+        Ms[i * (KB + 1) + j] = herm ? conj(Mi[j * KB + i]) : Mi[i * KB + j];
+    }
+    panel_order(ipiv, F.first, k, kb, mode == 0 || mode == 3, idx, piv_s);
+    __syncthreads();
+    #pragma unroll 8   // several loads in flight per thread
+    for (int q = tid; q < kb * m; q += blockDim.x) {
+        const int i = q / m, c = q % m;
+        Ys[i * LY + c] = Y[(long long)(k + (mode == 0 ? idx[i] : i)) * ldx + c];
+    }
+    __syncthreads();
+    constexpr int PER = (KB * MAXRHS + 255) / 256;
+    cx<T> acc[PER];
+    int oi[PER], oc[PER];
+#pragma unroll
+    for (int r = 0; r < PER; r++) {
+        const int q = tid + r * 256;
+        oi[r] = q / m;
+        oc[r] = q % m;
+        acc[r] = cx<T>(0);
+        if (oi[r] < kb)
+            for (int l = 0; l < kb; l++) acc[r] = acc[r] + Ms[oi[r] * (KB + 1) + l] * Ys[l * LY + oc[r]];
+    }
+    __syncthreads();
+    // Z (with the output permutation of mode 3) replaces the panel rows
+#pragma unroll
+    for (int r = 0; r < PER; r++)
+        if (oi[r] < kb) Ys[(mode == 3 ? idx[oi[r]] : oi[r]) * LY + oc[r]] = acc[r];
+    __syncthreads();
+    if (t.role == 0 || t.role == 3) {
+        // role 3: the front's last panel of the block, which no other CTA of
+        // this launch reads: solved rows straight into X
+        for (int q = tid; q < kb * m; q += blockDim.x) {
+            const int i = q / m, c = q % m;
+            if (t.role == 0) slot[i * MAXRHS + c] = Ys[i * LY + c];
+            else Y[(long long)(k + i) * ldx + c] = Ys[i * LY + c];
+        }
+        return;
+    }
+    // update rows [r0, r1): the block A(r, l) of the factor into Ms
+    const int nr = t.r1 - t.r0;
+    const cx<T> *P = fac + F.fac;
+    if (mode == 0 || mode == 1) {
+        #pragma unroll 8   // several loads in flight per thread
+        for (int q = tid; q < nr * kb; q += blockDim.x) {
+            const int r = q / kb, l = q % kb;
+            Ms[r * (KB + 1) + l] = P[(long long)(t.r0 + r) * nf + k + l];
+        }
+    } else {
+        #pragma unroll 8   // several loads in flight per thread
+        for (int q = tid; q < nr * kb; q += blockDim.x) {
+            const int l = q / nr, r = q % nr;
+            Ms[r * (KB + 1) + l] = conj(P[(long long)(k + l) * nf + t.r0 + r]);
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < nr * m; q += blockDim.x) {
+        const int r = q / m, c = q % m;
+        cx<T> a = cx<T>(0);
+        for (int l = 0; l < kb; l++) a = a + Ms[r * (KB + 1) + l] * Ys[l * LY + c];
+        cx<T> *y = Y + (long long)(t.r0 + r) * ldx + c;
+        *y = *y - a;
+    }
 }
 
 }  // namespace wt3d
