@@ -375,19 +375,31 @@ def run_serve(args):
     grids = ((48, 48, 48), (64, 64, 64), (96, 96, 64))
     for g in grids:          # host analyses of the three grids, computed once per process
         be.bytes_needed((g, 0, 1.0))
-    stream = serve.make_stream(args.serve_requests, rate_hz=args.serve_rate, seed=7, grids=grids)
-    srv = serve.Server(be, budget_bytes=120e9, max_batch=64, workers=4)
-    try:
-        summ = srv.run(stream, timeout_s=900)
-    finally:
-        srv.close()
-    summ = {k: (float("%.4g" % v) if isinstance(v, float) else v) for k, v in summ.items()}
-    summ.update({"workload": "config3 serving: Poisson %.2f req/s, %d requests (seed 7), grids 48^3/64^3/96x96x64 "
-                             "(0.5/0.35/0.15), model pool 8, f in {0.5,1,1.5,2} Hz, 1-64 sources (75%% plane, 25%% "
-                             "point), budget 120 GB resident factors, LRU, RHS batched per factor, 4 workers"
-                             % (args.serve_rate, args.serve_requests),
-                 "hit_rate": round(summ["hits"] / max(1, summ["requests"]), 3)})
-    return summ
+    def one(stream, desc):
+        srv = serve.Server(be, budget_bytes=120e9, max_batch=64, workers=4)
+        try:
+            summ = srv.run(stream, timeout_s=900)
+        finally:
+            srv.close()
+        summ = {k: (float("%.4g" % v) if isinstance(v, float) else v) for k, v in summ.items()}
+        summ.update({"workload": desc, "hit_rate": round(summ["hits"] / max(1, summ["requests"]), 3)})
+        return summ
+
+    out = one(serve.make_stream(args.serve_requests, rate_hz=args.serve_rate, seed=7, grids=grids),
+              "config3 serving: Poisson %.2f req/s, %d requests (seed 7), grids 48^3/64^3/96x96x64 "
+              "(0.5/0.35/0.15), model pool 8, f in {0.5,1,1.5,2} Hz, 1-64 sources (75%% plane, 25%% "
+              "point), budget 120 GB resident factors, LRU, RHS batched per factor, 4 workers"
+              % (args.serve_rate, args.serve_requests))
+    if args.serve_reuse_requests > 0:
+        # a stream whose keys recur, as in a survey where many shots share a
+        # model and a frequency: 2 models, 2 frequencies, 64^3 and 96x96x64
+        out["reuse"] = one(serve.make_stream(args.serve_reuse_requests, rate_hz=args.serve_reuse_rate, seed=8,
+                                             grids=grids[1:], grid_weights=(0.6, 0.4), freqs=(1.0, 2.0),
+                                             n_models=2),
+                           "config3 serving, key reuse: Poisson %.2f req/s, %d requests (seed 8), grids "
+                           "64^3/96x96x64 (0.6/0.4), model pool 2, f in {1,2} Hz, 1-64 sources, same budget "
+                           "and batching" % (args.serve_reuse_rate, args.serve_reuse_requests))
+    return out
 
 
 def run_fp64_leg(args, mixed_solutions):
@@ -500,6 +512,8 @@ def main():
     ap.add_argument("--sm-reserve", type=int, default=0, help="SMs the factorisation GEMM leaves to the other lane")
     ap.add_argument("--serve-requests", type=int, default=30)
     ap.add_argument("--serve-rate", type=float, default=0.3)
+    ap.add_argument("--serve-reuse-requests", type=int, default=30)
+    ap.add_argument("--serve-reuse-rate", type=float, default=0.5)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

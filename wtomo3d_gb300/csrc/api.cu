@@ -564,6 +564,19 @@ int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, d
     }
 }
 
+// Plain refinement continues while a pass cuts the worst residual by at least
+// this factor (WT3D_REFINE_SWITCH, default 0.25); otherwise the solve
+// switches to the flexible GMRES.
+static double refine_switch()
+{
+    static const double v = [] {
+        const char *e = getenv("WT3D_REFINE_SWITCH");
+        const double x = e ? atof(e) : 0.25;
+        return (x > 0 && x < 1) ? x : 0.25;
+    }();
+    return v;
+}
+
 // Refinement driver over m <= MAXRHS columns held in h->Bn; result in h->Xn.
 // Plain iterative refinement while it reduces the worst residual at least
 // fourfold per step; flexible GMRES preconditioned by the same factors
@@ -605,7 +618,7 @@ int refine(wt3d_solver *h, Engine<T> &E, int m, bool adjoint, double tol, int ma
         if (!(worst == worst)) { rc = WT3D_ERR_NOCONV; break; }   // NaN
         if (worst <= tol) break;
         if (it >= maxit) { rc = WT3D_ERR_NOCONV; break; }
-        if (it >= 1 && worst > 0.25 * prev_worst) {
+        if (it >= 1 && worst > refine_switch() * prev_worst) {
             std::vector<double> bn2(hn.begin() + MAXRHS, hn.begin() + MAXRHS + m), rn2(hn.begin(), hn.begin() + m);
             it++;
             rc = fgmres<T>(h, E, sc, m, adjoint, tol, maxit, bn2, rn2, relres, it);
