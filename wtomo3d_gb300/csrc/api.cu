@@ -565,14 +565,15 @@ int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, d
 }
 
 // Plain refinement continues while a pass cuts the worst residual by at least
-// this factor (WT3D_REFINE_SWITCH, default 0.25); otherwise the solve
-// switches to the flexible GMRES.
+// this factor (WT3D_REFINE_SWITCH, default 0.08); otherwise the solve
+// switches to the flexible GMRES, which reaches the tolerance in fewer
+// passes once refinement converges more slowly than that.
 static double refine_switch()
 {
     static const double v = [] {
         const char *e = getenv("WT3D_REFINE_SWITCH");
-        const double x = e ? atof(e) : 0.25;
-        return (x > 0 && x < 1) ? x : 0.25;
+        const double x = e ? atof(e) : 0.08;
+        return (x > 0 && x < 1) ? x : 0.08;
     }();
     return v;
 }

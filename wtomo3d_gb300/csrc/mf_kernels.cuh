@@ -140,14 +140,30 @@ __global__ void k_extend_add(const EATask *__restrict__ tasks, int ntasks, long 
     const int nfP = P.p + P.b;
     cx<T> *pf = fac + P.fac;
     cx<T> *p22 = (P.parity ? upd1 : upd0) + P.upd;
-    for (int j = lane; j < C.b; j += 32) {
-        const int Cc = rl[j];
-        cx<T> v = src[j];
-        cx<T> *dst;
-        if (R < P.p) dst = pf + (long long)R * nfP + Cc;
-        else if (Cc < P.p) dst = pf + (long long)P.p * nfP + (long long)(R - P.p) * P.p + Cc;
-        else dst = p22 + (long long)(R - P.p) * P.b + (Cc - P.p);
-        *dst = *dst + v;
+    // four entries per lane at a time: their loads are issued before the
+    // read-modify-writes (the compiler cannot reorder across the stores)
+    auto target = [&](int Cc) -> cx<T> * {
+        if (R < P.p) return pf + (long long)R * nfP + Cc;
+        if (Cc < P.p) return pf + (long long)P.p * nfP + (long long)(R - P.p) * P.p + Cc;
+        return p22 + (long long)(R - P.p) * P.b + (Cc - P.p);
+    };
+    int j = lane;
+    for (; j + 96 < C.b; j += 128) {
+        cx<T> v[4], d[4];
+        cx<T> *dst[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            v[u] = src[j + 32 * u];
+            dst[u] = target(rl[j + 32 * u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) d[u] = *dst[u];
+#pragma unroll
+        for (int u = 0; u < 4; u++) *dst[u] = d[u] + v[u];
+    }
+    for (; j < C.b; j += 32) {
+        cx<T> *dst = target(rl[j]);
+        *dst = *dst + src[j];
     }
 }
 
@@ -844,23 +860,29 @@ __global__ void __launch_bounds__(256) k_sub_step(const StepTask *__restrict__ t
         Ys[i * LY + c] = Y[(long long)(k + (mode == 0 ? idx[i] : i)) * ldx + c];
     }
     __syncthreads();
-    constexpr int PER = (KB * MAXRHS + 255) / 256;
-    cx<T> acc[PER];
-    int oi[PER], oc[PER];
+    // Z = M y: thread (lane c, warp w) owns rows w, w + 8, ..., w + 56 of
+    // column c; the k loop runs outside, so its eight sums are independent
+    // chains (one shared load of y per k, the M entries are warp broadcasts)
+    const int c = tid & 31, w = tid >> 5;
+    cx<T> acc[KB / 8];
 #pragma unroll
-    for (int r = 0; r < PER; r++) {
-        const int q = tid + r * 256;
-        oi[r] = q / m;
-        oc[r] = q % m;
-        acc[r] = cx<T>(0);
-        if (oi[r] < kb)
-            for (int l = 0; l < kb; l++) acc[r] = acc[r] + Ms[oi[r] * (KB + 1) + l] * Ys[l * LY + oc[r]];
+    for (int j = 0; j < KB / 8; j++) acc[j] = cx<T>(0);
+    if (c < m) {
+        for (int l = 0; l < kb; l++) {
+            const cx<T> y = Ys[l * LY + c];
+#pragma unroll
+            for (int j = 0; j < KB / 8; j++) acc[j] = acc[j] + Ms[(w + 8 * j) * (KB + 1) + l] * y;
+        }
     }
     __syncthreads();
     // Z (with the output permutation of mode 3) replaces the panel rows
+    if (c < m) {
 #pragma unroll
-    for (int r = 0; r < PER; r++)
-        if (oi[r] < kb) Ys[(mode == 3 ? idx[oi[r]] : oi[r]) * LY + oc[r]] = acc[r];
+        for (int j = 0; j < KB / 8; j++) {
+            const int i = w + 8 * j;
+            if (i < kb) Ys[(mode == 3 ? idx[i] : i) * LY + c] = acc[j];
+        }
+    }
     __syncthreads();
     if (t.role == 0 || t.role == 3) {
         // role 3: the front's last panel of the block, which no other CTA of
@@ -889,12 +911,24 @@ __global__ void __launch_bounds__(256) k_sub_step(const StepTask *__restrict__ t
         }
     }
     __syncthreads();
-    for (int q = tid; q < nr * m; q += blockDim.x) {
-        const int r = q / m, c = q % m;
-        cx<T> a = cx<T>(0);
-        for (int l = 0; l < kb; l++) a = a + Ms[r * (KB + 1) + l] * Ys[l * LY + c];
-        cx<T> *y = Y + (long long)(t.r0 + r) * ldx + c;
-        *y = *y - a;
+    // rows w, w + 8, ... of column c, independent sums as above
+    if (c < m) {
+        cx<T> u[SUB_RB / 8];
+#pragma unroll
+        for (int j = 0; j < SUB_RB / 8; j++) u[j] = cx<T>(0);
+        for (int l = 0; l < kb; l++) {
+            const cx<T> z = Ys[l * LY + c];
+#pragma unroll
+            for (int j = 0; j < SUB_RB / 8; j++) u[j] = u[j] + Ms[(w + 8 * j) * (KB + 1) + l] * z;
+        }
+#pragma unroll
+        for (int j = 0; j < SUB_RB / 8; j++) {
+            const int r = w + 8 * j;
+            if (r < nr) {
+                cx<T> *y = Y + (long long)(t.r0 + r) * ldx + c;
+                *y = *y - u[j];
+            }
+        }
     }
 }
 

@@ -59,18 +59,38 @@ constexpr int TC_GROUP = 8;                 // column panels per rasterisation g
 // ---------------------------------------------------------------------------
 // operand split / expansion pre-pass
 // ---------------------------------------------------------------------------
+// Task of work item q, with tasks[i].*w the first item of task i (increasing):
+// one binary search per block, by thread 0 for the block's first item, then
+// each thread steps over the few task boundaries inside its block.  (A
+// binary search per thread costs a chain of ~log2(ntasks) dependent loads.)
+// Every thread of the block must call this.
+__device__ __forceinline__ int block_task(const TcTask *__restrict__ tasks, int ntasks, long long q_first, long long q,
+                                          long long TcTask::*w)
+{
+    __shared__ int s_t;
+    if (threadIdx.x == 0) {
+        int lo_t = 0, hi_t = ntasks - 1;
+        while (lo_t < hi_t) {
+            const int mid = (lo_t + hi_t + 1) >> 1;
+            if (tasks[mid].*w <= q_first) lo_t = mid;
+            else hi_t = mid - 1;
+        }
+        s_t = lo_t;
+    }
+    __syncthreads();
+    int t = s_t;
+    while (t + 1 < ntasks && tasks[t + 1].*w <= q) t++;
+    return t;
+}
+
 // One thread per (row, complex k) of A: Ahi/Alo rows of Kr floats.
 __global__ void k_split_a(const TcTask *__restrict__ tasks, int ntasks, long long total)
 {
-    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long q0 = (long long)blockIdx.x * blockDim.x;
+    long long q = q0 + threadIdx.x;
+    const int ti = block_task(tasks, ntasks, q0, q < total ? q : total - 1, &TcTask::a_work0);
     if (q >= total) return;
-    int lo_t = 0, hi_t = ntasks - 1;
-    while (lo_t < hi_t) {
-        int mid = (lo_t + hi_t + 1) >> 1;
-        if (tasks[mid].a_work0 <= q) lo_t = mid;
-        else hi_t = mid - 1;
-    }
-    const TcTask &t = tasks[lo_t];
+    const TcTask &t = tasks[ti];
     const long long r = q - t.a_work0;
     const int kc = t.Kr / 2;
     const int i = (int)(r / kc), k = (int)(r % kc);
@@ -148,16 +168,12 @@ __device__ __forceinline__ void split_f16(float x, __half &hi, __half &lo)
 // One warp per row of A: the row's largest |re|, |im| over k < K.
 __global__ void k_amax(const TcTask *__restrict__ tasks, int ntasks, long long total_rows)
 {
+    const long long q0 = ((long long)blockIdx.x * blockDim.x) >> 5;
     const long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
+    const int ti = block_task(tasks, ntasks, q0, q < total_rows ? q : total_rows - 1, &TcTask::a_row0);
     if (q >= total_rows) return;
-    int lo_t = 0, hi_t = ntasks - 1;
-    while (lo_t < hi_t) {
-        int mid = (lo_t + hi_t + 1) >> 1;
-        if (tasks[mid].a_row0 <= q) lo_t = mid;
-        else hi_t = mid - 1;
-    }
-    const TcTask &t = tasks[lo_t];
+    const TcTask &t = tasks[ti];
     const int i = (int)(q - t.a_row0);
     const cx<float> *row = t.A + (long long)i * t.lda;
     float m = 0.f;
@@ -209,15 +225,11 @@ __global__ void __launch_bounds__(256) k_bmax(const TcTask *__restrict__ tasks, 
 // (column) also stores the inverse scale for the epilogue.
 __global__ void k_split_a_f16(const TcTask *__restrict__ tasks, int ntasks, long long total)
 {
-    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long q0 = (long long)blockIdx.x * blockDim.x;
+    long long q = q0 + threadIdx.x;
+    const int ti = block_task(tasks, ntasks, q0, q < total ? q : total - 1, &TcTask::a_work0);
     if (q >= total) return;
-    int lo_t = 0, hi_t = ntasks - 1;
-    while (lo_t < hi_t) {
-        int mid = (lo_t + hi_t + 1) >> 1;
-        if (tasks[mid].a_work0 <= q) lo_t = mid;
-        else hi_t = mid - 1;
-    }
-    const TcTask &t = tasks[lo_t];
+    const TcTask &t = tasks[ti];
     const long long r = q - t.a_work0;
     const int kc = t.Kr / 2;
     const int i = (int)(r / kc), k = (int)(r % kc);
