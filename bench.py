@@ -27,11 +27,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "solves/s @96x96x64 mixed vs FP64 GPU at resid<=1e-8; serve p50/p99 ms"
-# ncu capture (--set full) of one k_tc_gemm launch of the GEMM microbenchmark:
-# dram__bytes_read.sum + dram__bytes_write.sum, and the launch's algorithmic
-# bytes (split operands once + C read and written once)
-TC_CAPTURE = {"launch": "M=N=8192, K=512 (python -m wtomo3d_gb300.gemm_bench 8192 8192 512)",
-              "dram_bytes": 1.684584e9 + 0.504824e9, "algorithmic_bytes": 0.201e9 + 2 * 0.5369e9}
+# ncu capture (--set full) of one k_tc_gemm launch of the GEMM microbenchmark
+# (f16 split): dram__bytes_read.sum + dram__bytes_write.sum, and the launch's
+# algorithmic bytes (split operands once + C read and written once)
+TC_CAPTURE = {"launch": "M=N=8192, K=512 (python -m wtomo3d_gb300.gemm_bench 8192 8192 512), k_tc_gemm<true>",
+              "dram_bytes": 0.836472e9 + 0.486964e9, "algorithmic_bytes": 0.1007e9 + 2 * 0.5369e9}
 FREQS = [0.5, 1.0, 1.5, 2.0]
 
 
@@ -278,12 +278,12 @@ def run_ours(args, rank, world, mixed_solutions):
     out = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64 fronts (fp32) + f64 refinement", "data": "synthetic",
+        "vs_baseline": None, "dtype": "c64 fronts (fp32 accumulate, f16-split tensor-core products) + f64 refinement", "data": "synthetic",
         "config": workload_config(args, world),
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "resident": resident,
         "gpu_launches": launches,
-        "roofline": {"bound": "tensor", "kernel": "k_tc_gemm (tcgen05 3xTF32 front Schur/trailing updates)",
+        "roofline": {"bound": "tensor", "kernel": "k_tc_gemm (tcgen05 f16-split front Schur/trailing updates)",
                      "achieved": gemm_tflops, "peak": peak, "unit": "TFLOP/s", "frac": gemm_tflops / peak,
                      "peak_source": "%s bf16_tflops_sustained" % pk_src,
                      "gemm_time_share": gemm_ms / total_ms,
@@ -371,7 +371,8 @@ def run_serve(args):
     with LRU eviction, right-hand sides batched per factorisation.  Latency =
     arrival to solution on the host."""
     from wtomo3d_gb300 import serve
-    be = serve.GpuBackend(dx=20.0, pml_nodes=10, tol=args.tol, maxit=30)
+    # two factorisation workspaces per grid: two keys of one grid factor at once
+    be = serve.GpuBackend(dx=20.0, pml_nodes=10, tol=args.tol, maxit=30, workspaces_per_grid=2)
     grids = ((48, 48, 48), (64, 64, 64), (96, 96, 64))
     for g in grids:          # host analyses of the three grids, computed once per process
         be.bytes_needed((g, 0, 1.0))
@@ -399,6 +400,8 @@ def run_serve(args):
                            "config3 serving, key reuse: Poisson %.2f req/s, %d requests (seed 8), grids "
                            "64^3/96x96x64 (0.6/0.4), model pool 2, f in {1,2} Hz, 1-64 sources, same budget "
                            "and batching" % (args.serve_reuse_rate, args.serve_reuse_requests))
+    import wtomo3d_gb300 as wt
+    wt.lib().wt3d_set_workspaces_per_grid(1)
     return out
 
 

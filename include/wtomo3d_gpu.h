@@ -386,6 +386,16 @@ long long wt3d_gemm_noalloc_max_floats(void);
 int wt3d_gemm_noalloc(int M, int N, int K, const void *dA, int lda, const void *dB, int ldb, void *dC, int ldc,
                       void *stream);
 
+/* Factorisation workspaces per grid (1 to 8, default 1).  The level update
+ * buffers a factorisation needs while it runs (the F22 Schur blocks of two
+ * tree levels) are shared by the handles of a grid, which then factor one at
+ * a time.  With n > 1, handles created later get their own workspace while
+ * fewer than n exist, so up to n factorisations of one grid run at once, at
+ * the cost of one more workspace each (wt3d_solver_bytes out[2]).  Applies to
+ * handles created afterwards.  No counterpart in the reference, which holds a
+ * single solver instance (strumpack_finter.c:15,19-20). */
+int wt3d_set_workspaces_per_grid(int n);
+
 /* Last error message of the calling thread (static storage). */
 const char *wt3d_last_error(void);
 

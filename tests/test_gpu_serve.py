@@ -17,7 +17,8 @@ pytest.importorskip("torch")
 
 def test_serving_same_alone_and_in_the_mix():
     grids = ((20, 20, 16), (24, 22, 18))
-    be = serve.GpuBackend(dx=20.0, pml_nodes=4, tol=1e-10, maxit=30, keep_results=True)
+    # two factorisation workspaces per grid: factorisations of one grid overlap
+    be = serve.GpuBackend(dx=20.0, pml_nodes=4, tol=1e-10, maxit=30, keep_results=True, workspaces_per_grid=2)
     sizes = [be.bytes_needed((g, 0, 1.0)) for g in grids]
     budget = sizes[0] + sizes[1] + 0.5 * sizes[0]            # two or three resident at most
     stream = serve.make_stream(18, rate_hz=40.0, seed=5, grids=grids, grid_weights=(1, 1), n_models=3,
@@ -29,7 +30,7 @@ def test_serving_same_alone_and_in_the_mix():
     assert summ["peak_resident_gb"] * 1e9 <= budget
     assert summ["max_relres"] <= 1e-10
     assert summ["batches"] < summ["requests"]                 # some requests shared a batch
-    alone = serve.GpuBackend(dx=20.0, pml_nodes=4, tol=1e-10, maxit=30, keep_results=True)
+    alone = serve.GpuBackend(dx=20.0, pml_nodes=4, tol=1e-10, maxit=30, keep_results=True, workspaces_per_grid=1)
     worst = 0.0
     for key in {r.key for r in stream}:
         h = alone.open(key)

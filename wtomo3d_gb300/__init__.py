@@ -153,6 +153,7 @@ def lib():
         L.strumpack_serial_finter.argtypes = [ip, ip, ip, vp, vp, vp, vp, vp, ip]
         L.strumpack_serial_finter.restype = None
         L.wt3d_finter_set_refinement.argtypes = [ctypes.c_double, ctypes.c_int]
+        L.wt3d_set_workspaces_per_grid.argtypes = [ctypes.c_int]
         L.wt3d_finter_last_relres.restype = ctypes.c_double
         L.wt3d_finter_last_relres.argtypes = []
         _lib = L

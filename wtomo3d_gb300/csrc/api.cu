@@ -1,6 +1,7 @@
 // C ABI of libwtomo3d_gpu: the drop-in strumpack_serial_finter job protocol,
 // the handle-based wt3d_* solver, and the FP64 iterative refinement that wraps
 // the complex64 multifrontal factorisation.
+#include <atomic>
 #include "engine.cuh"
 #include "wtomo3d_gpu.h"
 #include <array>
@@ -319,8 +320,9 @@ struct GridAnalysis {
     std::vector<long long> map;
     std::vector<int> tpos;
     std::mutex mu;
-    std::weak_ptr<FactorWorkspace<float>> ws32;
-    std::weak_ptr<FactorWorkspace<double>> ws64;
+    // factorisation workspaces of this grid (up to wt3d_set_workspaces_per_grid)
+    std::vector<std::weak_ptr<FactorWorkspace<float>>> ws32;
+    std::vector<std::weak_ptr<FactorWorkspace<double>>> ws64;
 };
 }  // namespace wt3d
 
@@ -694,6 +696,32 @@ int grid_analysis(int nx, int ny, int nz, std::shared_ptr<GridAnalysis> &out)
     return WT3D_OK;
 }
 
+// Factorisation workspaces per grid: handles that share one factor one at a
+// time; up to this many workspaces let handles of one grid factor at once.
+std::atomic<int> g_ws_per_grid{1};
+
+// A new handle's workspace: an unused slot of the grid's pool gets a new
+// workspace (allocated at the handle's first factorisation set-up); with
+// every slot in use, the workspace with the fewest handles is shared.
+template <class T>
+std::shared_ptr<FactorWorkspace<T>> pick_workspace(std::vector<std::weak_ptr<FactorWorkspace<T>>> &pool)
+{
+    const size_t n = (size_t)std::max(1, g_ws_per_grid.load());
+    if (pool.size() < n) pool.resize(n);
+    for (size_t i = 0; i < n; i++)
+        if (pool[i].expired()) {
+            auto w = std::make_shared<FactorWorkspace<T>>();
+            pool[i] = w;
+            return w;
+        }
+    std::shared_ptr<FactorWorkspace<T>> best;
+    for (size_t i = 0; i < n; i++) {
+        auto w = pool[i].lock();
+        if (w && (!best || w.use_count() < best.use_count())) best = w;
+    }
+    return best;
+}
+
 // Device bytes a handle holds on its own once created and factored:
 // out[0] always, out[1] more once plane-wave sources are built, out[2] the
 // level-parity update buffers of the shared factorisation workspace.
@@ -728,6 +756,13 @@ double own_bytes(const wt3d_solver *h)
 extern "C" {
 
 const char *wt3d_last_error(void) { return g_err.c_str(); }
+
+int wt3d_set_workspaces_per_grid(int n)
+{
+    if (n < 1 || n > 8) { set_error("wt3d_set_workspaces_per_grid: need 1 <= n <= 8"); return WT3D_ERR_ARG; }
+    g_ws_per_grid.store(n);
+    return WT3D_OK;
+}
 
 long long wt3d_pattern_nnz(int nx, int ny, int nz)
 {
@@ -850,11 +885,8 @@ int wt3d_solver_create(wt3d_solver **out, const wt3d_grid *g, int precision)
             ga.map.swap(map);
             ga.tpos.swap(tp);
         }
-        if (precision == WT3D_PREC_MIXED) {
-            if (!(w32 = ga.ws32.lock())) { w32 = std::make_shared<FactorWorkspace<float>>(); ga.ws32 = w32; }
-        } else {
-            if (!(w64 = ga.ws64.lock())) { w64 = std::make_shared<FactorWorkspace<double>>(); ga.ws64 = w64; }
-        }
+        if (precision == WT3D_PREC_MIXED) w32 = pick_workspace(ga.ws32);
+        else w64 = pick_workspace(ga.ws64);
     }
     if ((rc = h->tpos.upload(ga.tpos))) return rc;
     if ((rc = h->perm.upload(sym.perm))) return rc;

@@ -82,7 +82,12 @@ public:
     DevVec<unsigned long long> maxabs;
     std::unique_ptr<Schedule<T>> fsched;
     std::map<int, std::unique_ptr<Schedule<T>>> ssched[2];   // [adjoint][m]
-    static constexpr int WB = 512;   // outer block width of the two-level LU
+    // outer block width of the two-level LU (WT3D_WB: a multiple of KB, 512 by default)
+    const int WB = [] {
+        const char *e = getenv("WT3D_WB");
+        const int v = e ? atoi(e) : 512;
+        return (v >= KB && v % KB == 0) ? v : 512;
+    }();
     static constexpr int WS = 512;   // outer block width of the blocked substitutions
     // pivots below pivot_rel times the largest entry are perturbed: only
     // (near-)zero ones, since Dirichlet rows carry unit pivots next to O(1e8)

@@ -313,9 +313,14 @@ class GpuBackend:
     force on component comp.  Solutions (scattered field for plane waves)
     are FP64-refined to `tol`."""
 
-    def __init__(self, dx=20.0, pml_nodes=10, tol=1e-8, maxit=20, keep_results=False, precision=None, max_batch=64):
+    def __init__(self, dx=20.0, pml_nodes=10, tol=1e-8, maxit=20, keep_results=False, precision=None, max_batch=64,
+                 workspaces_per_grid=1):
         import wtomo3d_gb300 as wt
         self.wt = wt
+        # factorisations of one grid run concurrently up to this many at once
+        # (each concurrent one holds its own level update buffers)
+        self.workspaces = int(workspaces_per_grid)
+        wt._check(wt.lib().wt3d_set_workspaces_per_grid(self.workspaces))
         self.dx, self.pml_nodes, self.tol, self.maxit = dx, pml_nodes, tol, maxit
         self.keep = keep_results
         self.max_batch = max_batch
@@ -345,12 +350,13 @@ class GpuBackend:
 
     def can_open(self, key, freeing):
         """Free device memory (plus what the evictions release) covers the new
-        handle, the factorisation workspace of its grid unless another handle
-        of that grid holds it, the Krylov bases of a slow solve and a margin."""
+        handle, a factorisation workspace of its grid unless every workspace
+        the grid may have is held already, the Krylov bases of a slow solve and
+        a margin."""
         g = self.grid(key[0])
         _, _, ws = self.wt.solver_bytes(g, self.precision)
         with self._lock:
-            shared = self._open.get(tuple(key[0]), 0) > 0
+            shared = self._open.get(tuple(key[0]), 0) >= self.workspaces
         transient = (0.0 if shared else 1.25 * ws) + 17.0 * g.n * 32 * 16 + 4e9
         free, _ = self.wt.mem_info()
         return free + freeing >= self.bytes_needed(key) + transient
