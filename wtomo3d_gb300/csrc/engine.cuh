@@ -197,7 +197,7 @@ public:
             cudaFuncSetAttribute(k_diag_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1))));
             cudaFuncSetAttribute(k_sub_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1))));
+                                 (int)(sizeof(cx<T>) * sub_step_smem_elems()));
         });
         return build_factor_schedule();
     }
@@ -586,14 +586,14 @@ public:
         // the rows outside the block then receive one K = WS update, which
         // the tall-skinny tensor-core kernel takes.
         std::vector<StepTask> hs;
-        size_t smd_step = sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1));
+        size_t smd_step = sizeof(cx<T>) * sub_step_smem_elems();
         int maxslots = 0;
         // one fused launch over the step tasks [s0, end)
         auto step_launch = [&](size_t s0, int mode) {
             const int ns = (int)(hs.size() - s0);
             if (!ns) return;
             sc->launches.push_back({[psc, this, s0, ns, smd_step, m, mode, Xp, ldx](cudaStream_t st) {
-                k_sub_step<T><<<ns, 256, smd_step, st>>>(psc->step.p + s0, fr.p, fac.p, dinv.p, ipiv.p, Xp, ldx, m,
+                k_sub_step<T><<<ns, SUB_THREADS, smd_step, st>>>(psc->step.p + s0, fr.p, fac.p, dinv.p, ipiv.p, Xp, ldx, m,
                                                          mode, psc->zs.p);
             }, LK_DIAG, 0, (double)ns * (KB * KB + 2.0 * KB * m) * sizeof(cx<T>)});
         };

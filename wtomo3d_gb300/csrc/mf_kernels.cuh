@@ -423,6 +423,22 @@ __global__ void __launch_bounds__(TCR) k_trsm_col(const ColTask *__restrict__ ta
     }
 }
 
+// Asynchronous global -> shared copy of one complex element (8 or 16 bytes,
+// naturally aligned), and the wait for all of a thread's copies.
+template <class T>
+__device__ __forceinline__ void cp_async_cx(cx<T> *dst, const cx<T> *src)
+{
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(cx<T>) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+}
+
 // ---------------------------------------------------------------------------
 // complex64 variants of the two band solves with the band's vector in
 // registers.  Both are right-looking: once an unknown is final, its multiples
@@ -447,22 +463,23 @@ __global__ void __launch_bounds__(TRW) k_trsm_row_reg(const RowTask *__restrict_
     const int c0 = t.c0, nc = min(TRW, nf - c0);
     const int tid = threadIdx.x;
     cx<float> *base = fac + F.fac + (long long)k * nf;
-    #pragma unroll 8   // several loads in flight per thread
+    // tile and band in one batch of asynchronous copies, band rows as stored
     for (int q = tid; q < KB * KB; q += blockDim.x) {
         const int i = q / KB, j = q % KB;
-        L[i * (KB + 1) + j] = (i < kb && j < kb) ? base[(long long)i * nf + k + j] : cx<float>(0.f, 0.f);
+        if (i < kb && j < kb) cp_async_cx(L + i * (KB + 1) + j, base + (long long)i * nf + k + j);
+        else L[i * (KB + 1) + j] = cx<float>(0.f, 0.f);
     }
-    panel_order(ipiv, F.first, k, kb, true, idx, piv_s);
-    __syncthreads();
-    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < kb * nc; q += blockDim.x) {
         const int i = q / nc, c = q % nc;
-        Bt[i * (TRW + 1) + c] = base[(long long)idx[i] * nf + c0 + c];
+        cp_async_cx(Bt + i * (TRW + 1) + c, base + (long long)i * nf + c0 + c);
     }
+    panel_order(ipiv, F.first, k, kb, true, idx, piv_s);
+    cp_async_wait_all();
     __syncthreads();
+    // the panel's row interchanges applied as the band is read
     cx<float> b[KB];
 #pragma unroll
-    for (int i = 0; i < KB; i++) b[i] = (i < kb) ? Bt[i * (TRW + 1) + tid] : cx<float>(0.f, 0.f);
+    for (int i = 0; i < KB; i++) b[i] = (i < kb) ? Bt[idx[i] * (TRW + 1) + tid] : cx<float>(0.f, 0.f);
 #pragma unroll
     for (int l = 0; l < KB - 1; l++) {
         const cx<float> bl = b[l];
@@ -496,11 +513,10 @@ __global__ void __launch_bounds__(TCR) k_trsm_col_reg(const ColTask *__restrict_
     const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
     const int tid = threadIdx.x;
     const cx<float> *D = fac + F.fac + (long long)k * nf + k;
-    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < KB * KB; q += blockDim.x) {
         const int i = q / KB, j = q % KB;
-        U[i * (KB + 1) + j] = (i < kb && j < kb) ? D[(long long)i * nf + j]
-                                                 : cx<float>(i == j ? 1.f : 0.f, 0.f);
+        if (i < kb && j < kb) cp_async_cx(U + i * (KB + 1) + j, D + (long long)i * nf + j);
+        else U[i * (KB + 1) + j] = cx<float>(i == j ? 1.f : 0.f, 0.f);
     }
     cx<float> *xb;
     long long ld;
@@ -514,11 +530,11 @@ __global__ void __launch_bounds__(TCR) k_trsm_col_reg(const ColTask *__restrict_
         ld = F.p;
         nr = min(TCR, F.b - t.r0);
     }
-    #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < nr * kb; q += blockDim.x) {
         const int r = q / kb, j = q % kb;
-        Xs[r * (KB + 1) + j] = xb[(long long)r * ld + j];
+        cp_async_cx(Xs + r * (KB + 1) + j, xb + (long long)r * ld + j);
     }
+    cp_async_wait_all();
     __syncthreads();
     for (int j = tid; j < KB; j += blockDim.x) invd[j] = cdiv(cx<float>(1.f, 0.f), U[j * (KB + 1) + j]);
     __syncthreads();
@@ -818,15 +834,27 @@ __global__ void __launch_bounds__(256) k_diag_solve(const PanelTask *__restrict_
 // (or a flush) writes it into X once no CTA reads those rows any more.
 // ---------------------------------------------------------------------------
 constexpr int SUB_RB = 64;   // rows per update CTA
+
+// Shared-memory layout of k_sub_step (complex elements).
+__host__ __device__ constexpr int sub_step_smem_elems()
+{
+    return KB * (KB + 1) + KB * (MAXRHS + 1) + SUB_RB * (KB + 1) + SUB_RB * (MAXRHS + 1);
+}
+
+constexpr int SUB_THREADS = 512;   // 16 warps: each thread sums 4 rows of Z and 4 update rows
 template <class T>
-__global__ void __launch_bounds__(256) k_sub_step(const StepTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
+__global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
                                                   const cx<T> *__restrict__ fac, const cx<T> *__restrict__ inv,
                                                   const int *__restrict__ ipiv, cx<T> *__restrict__ X, int ldx, int m,
                                                   int mode, cx<T> *__restrict__ zs)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    cx<T> *Ms = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1): the tile operator, then the update block
-    cx<T> *Ys = Ms + KB * (KB + 1);                 // KB x (MAXRHS+1): panel rows, then Z
+    // every input is fetched in one batch of asynchronous copies, as stored;
+    // the pivot order and the conjugate transposes apply when it is read
+    cx<T> *Ms = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1): the mode's tile inverse as stored
+    cx<T> *Ys = Ms + KB * (KB + 1);                 // KB x (MAXRHS+1): panel rows as stored, then Z
+    cx<T> *As = Ys + KB * (MAXRHS + 1);             // SUB_RB x (KB+1) (modes 0, 1) or KB x (SUB_RB+1)
+    cx<T> *Yr = As + SUB_RB * (KB + 1);             // SUB_RB x (MAXRHS+1): the update CTA's rows of X
     __shared__ int idx[KB], piv_s[KB];
     const StepTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
@@ -835,7 +863,37 @@ __global__ void __launch_bounds__(256) k_sub_step(const StepTask *__restrict__ t
     const int LY = MAXRHS + 1;
     cx<T> *Y = X + (long long)F.first * ldx;
     cx<T> *slot = zs + (long long)t.slot * (KB * MAXRHS);
-    if (t.role != 1 && t.kprev >= 0) {   // roles 0 and 3
+    const int k = t.k, kb = min(KB, F.p - k);
+    const cx<T> *Li = inv + (long long)(F.pan + k / KB) * (2 * KB * KB);
+    const cx<T> *Mi = (mode == 0 || mode == 3) ? Li : Li + KB * KB;
+    const bool herm = mode >= 2;
+    const int nr = t.role == 1 ? t.r1 - t.r0 : 0;
+    const cx<T> *P = fac + F.fac;
+    for (int q = tid; q < KB * KB; q += blockDim.x) cp_async_cx(Ms + (q >> 6) * (KB + 1) + (q & 63), Mi + q);
+    for (int q = tid; q < kb * m; q += blockDim.x) {
+        const int i = q / m, c = q % m;
+        cp_async_cx(Ys + i * LY + c, Y + (long long)(k + i) * ldx + c);
+    }
+    if (nr) {
+        if (mode == 0 || mode == 1) {   // A(r, l) = P[r0 + r][k + l]
+            for (int q = tid; q < nr * kb; q += blockDim.x) {
+                const int r = q / kb, l = q % kb;
+                cp_async_cx(As + r * (KB + 1) + l, P + (long long)(t.r0 + r) * nf + k + l);
+            }
+        } else {                        // A(r, l) = conj(P[k + l][r0 + r]), stored as As[l][r]
+            for (int q = tid; q < kb * nr; q += blockDim.x) {
+                const int l = q / nr, r = q % nr;
+                cp_async_cx(As + l * (SUB_RB + 1) + r, P + (long long)(k + l) * nf + t.r0 + r);
+            }
+        }
+        for (int q = tid; q < nr * m; q += blockDim.x) {
+            const int r = q / m, c = q % m;
+            cp_async_cx(Yr + r * LY + c, Y + (long long)(t.r0 + r) * ldx + c);
+        }
+    }
+    // while the copies fly: the previous panel's solved rows into X (roles
+    // 0 and 3; no CTA of this launch reads those rows) and the pivot order
+    if (t.role != 1 && t.kprev >= 0) {
         const int kbp = min(KB, F.p - t.kprev);
         #pragma unroll 8   // several loads in flight per thread
         for (int q = tid; q < kbp * m; q += blockDim.x) {
@@ -843,43 +901,35 @@ __global__ void __launch_bounds__(256) k_sub_step(const StepTask *__restrict__ t
             Y[(long long)(t.kprev + i) * ldx + c] = slot[i * MAXRHS + c];
         }
     }
-    const int k = t.k, kb = min(KB, F.p - k);
-    const cx<T> *Li = inv + (long long)(F.pan + k / KB) * (2 * KB * KB);
-    const cx<T> *Mi = (mode == 0 || mode == 3) ? Li : Li + KB * KB;
-    const bool herm = mode >= 2;
-    #pragma unroll 8   // several loads in flight per thread
-    for (int q = tid; q < KB * KB; q += blockDim.x) {
-        const int i = q / KB, j = q % KB;
-        Ms[i * (KB + 1) + j] = herm ? conj(Mi[j * KB + i]) : Mi[i * KB + j];
-    }
     panel_order(ipiv, F.first, k, kb, mode == 0 || mode == 3, idx, piv_s);
+    cp_async_wait_all();
     __syncthreads();
-    #pragma unroll 8   // several loads in flight per thread
-    for (int q = tid; q < kb * m; q += blockDim.x) {
-        const int i = q / m, c = q % m;
-        Ys[i * LY + c] = Y[(long long)(k + (mode == 0 ? idx[i] : i)) * ldx + c];
-    }
-    __syncthreads();
-    // Z = M y: thread (lane c, warp w) owns rows w, w + 8, ..., w + 56 of
-    // column c; the k loop runs outside, so its eight sums are independent
-    // chains (one shared load of y per k, the M entries are warp broadcasts)
+    // Z = M y: thread (lane c, warp w) owns rows w, w + NW, w + 2 NW, ... of
+    // column c; the k loop runs outside, so its sums are independent chains
+    // (M entries are warp broadcasts)
+    constexpr int NW = SUB_THREADS / 32, RPT = KB / NW;
     const int c = tid & 31, w = tid >> 5;
-    cx<T> acc[KB / 8];
+    cx<T> acc[RPT];
 #pragma unroll
-    for (int j = 0; j < KB / 8; j++) acc[j] = cx<T>(0);
+    for (int j = 0; j < RPT; j++) acc[j] = cx<T>(0);
     if (c < m) {
         for (int l = 0; l < kb; l++) {
-            const cx<T> y = Ys[l * LY + c];
+            const cx<T> y = Ys[(mode == 0 ? idx[l] : l) * LY + c];
+            if (!herm) {
 #pragma unroll
-            for (int j = 0; j < KB / 8; j++) acc[j] = acc[j] + Ms[(w + 8 * j) * (KB + 1) + l] * y;
+                for (int j = 0; j < RPT; j++) acc[j] = acc[j] + Ms[(w + NW * j) * (KB + 1) + l] * y;
+            } else {
+#pragma unroll
+                for (int j = 0; j < RPT; j++) acc[j] = acc[j] + conj(Ms[l * (KB + 1) + w + NW * j]) * y;
+            }
         }
     }
     __syncthreads();
     // Z (with the output permutation of mode 3) replaces the panel rows
     if (c < m) {
 #pragma unroll
-        for (int j = 0; j < KB / 8; j++) {
-            const int i = w + 8 * j;
+        for (int j = 0; j < RPT; j++) {
+            const int i = w + NW * j;
             if (i < kb) Ys[(mode == 3 ? idx[i] : i) * LY + c] = acc[j];
         }
     }
@@ -888,46 +938,32 @@ __global__ void __launch_bounds__(256) k_sub_step(const StepTask *__restrict__ t
         // role 3: the front's last panel of the block, which no other CTA of
         // this launch reads: solved rows straight into X
         for (int q = tid; q < kb * m; q += blockDim.x) {
-            const int i = q / m, c = q % m;
-            if (t.role == 0) slot[i * MAXRHS + c] = Ys[i * LY + c];
-            else Y[(long long)(k + i) * ldx + c] = Ys[i * LY + c];
+            const int i = q / m, cc = q % m;
+            if (t.role == 0) slot[i * MAXRHS + cc] = Ys[i * LY + cc];
+            else Y[(long long)(k + i) * ldx + cc] = Ys[i * LY + cc];
         }
         return;
     }
-    // update rows [r0, r1): the block A(r, l) of the factor into Ms
-    const int nr = t.r1 - t.r0;
-    const cx<T> *P = fac + F.fac;
-    if (mode == 0 || mode == 1) {
-        #pragma unroll 8   // several loads in flight per thread
-        for (int q = tid; q < nr * kb; q += blockDim.x) {
-            const int r = q / kb, l = q % kb;
-            Ms[r * (KB + 1) + l] = P[(long long)(t.r0 + r) * nf + k + l];
-        }
-    } else {
-        #pragma unroll 8   // several loads in flight per thread
-        for (int q = tid; q < nr * kb; q += blockDim.x) {
-            const int l = q / nr, r = q % nr;
-            Ms[r * (KB + 1) + l] = conj(P[(long long)(k + l) * nf + t.r0 + r]);
-        }
-    }
-    __syncthreads();
-    // rows w, w + 8, ... of column c, independent sums as above
+    // rows w, w + NW, ... of column c, independent sums as above
+    constexpr int UPT = SUB_RB / NW;
     if (c < m) {
-        cx<T> u[SUB_RB / 8];
+        cx<T> u[UPT];
 #pragma unroll
-        for (int j = 0; j < SUB_RB / 8; j++) u[j] = cx<T>(0);
+        for (int j = 0; j < UPT; j++) u[j] = cx<T>(0);
         for (int l = 0; l < kb; l++) {
             const cx<T> z = Ys[l * LY + c];
+            if (mode == 0 || mode == 1) {
 #pragma unroll
-            for (int j = 0; j < SUB_RB / 8; j++) u[j] = u[j] + Ms[(w + 8 * j) * (KB + 1) + l] * z;
+                for (int j = 0; j < UPT; j++) u[j] = u[j] + As[(w + NW * j) * (KB + 1) + l] * z;
+            } else {
+#pragma unroll
+                for (int j = 0; j < UPT; j++) u[j] = u[j] + conj(As[l * (SUB_RB + 1) + w + NW * j]) * z;
+            }
         }
 #pragma unroll
-        for (int j = 0; j < SUB_RB / 8; j++) {
-            const int r = w + 8 * j;
-            if (r < nr) {
-                cx<T> *y = Y + (long long)(t.r0 + r) * ldx + c;
-                *y = *y - u[j];
-            }
+        for (int j = 0; j < UPT; j++) {
+            const int r = w + NW * j;
+            if (r < nr) Y[(long long)(t.r0 + r) * ldx + c] = Yr[r * LY + c] - u[j];
         }
     }
 }

@@ -165,8 +165,12 @@ __device__ __forceinline__ void split_f16(float x, __half &hi, __half &lo)
     lo = __float2half_rn(x - __half2float(hi));
 }
 
-// One warp per row of A: the row's largest |re|, |im| over k < K.
-__global__ void k_amax(const TcTask *__restrict__ tasks, int ntasks, long long total_rows)
+// Fused forms of the f16 split, one read of each operand from DRAM: a warp
+// per row of A reads the row once for its largest magnitude and again (from
+// L2) to split it; a block per 32 complex columns of B does the same over the
+// column group, transposing 32 x 32 tiles of B through shared memory into the
+// expanded K-major rows 2j, 2j+1 of B~.
+__global__ void k_split_a_f16_rows(const TcTask *__restrict__ tasks, int ntasks, long long total_rows)
 {
     const long long q0 = ((long long)blockIdx.x * blockDim.x) >> 5;
     const long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -182,110 +186,75 @@ __global__ void k_amax(const TcTask *__restrict__ tasks, int ntasks, long long t
         m = fmaxf(m, fmaxf(fabsf(v.re), fabsf(v.im)));
     }
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (lane == 0) t.amax[i] = __float_as_uint(m);
+    const float sc = f16_scale(__float_as_uint(m));
+    if (lane == 0) t.sa[i] = 1.f / sc;
+    __half2 *hi = reinterpret_cast<__half2 *>(t.ahi) + ((long long)i * t.Kr >> 1);
+    __half2 *lo = reinterpret_cast<__half2 *>(t.alo) + ((long long)i * t.Kr >> 1);
+    const int kc = t.Kr / 2;
+    for (int k = lane; k < kc; k += 32) {
+        cx<float> v(0.f, 0.f);
+        if (k < t.K) v = row[k];
+        __half h0, l0, h1, l1;
+        split_f16(v.re * sc, h0, l0);
+        split_f16(v.im * sc, h1, l1);
+        hi[k] = __halves2half2(h0, h1);
+        lo[k] = __halves2half2(l0, l1);
+    }
 }
 
-// 32 complex columns x 256 rows of B per block: column maxima by atomicMax on
-// the float bits (non-negative floats order like their bit patterns).
-__global__ void __launch_bounds__(256) k_bmax(const TcTask *__restrict__ tasks, int ntasks, long long total_tiles)
+__global__ void __launch_bounds__(256) k_split_b_f16_cols(const TcTask *__restrict__ tasks, int ntasks,
+                                                          long long total_groups)
 {
+    __shared__ float2 tile[32][33];
     __shared__ float red[8][33];
     const long long q = blockIdx.x;
-    if (q >= total_tiles) return;
-    int lo_t = 0, hi_t = ntasks - 1;
-    while (lo_t < hi_t) {
-        int mid = (lo_t + hi_t + 1) >> 1;
-        if (tasks[mid].b_work0 <= q) lo_t = mid;
-        else hi_t = mid - 1;
-    }
-    const TcTask &t = tasks[lo_t];
-    const long long r = q - t.b_work0;
-    const int kt = t.Kr / 64;                 // 32-complex k tiles
-    const int j0 = (int)(r / kt) * 32, k0 = (int)(r % kt) * 32;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int ti = block_task(tasks, ntasks, q, q, &TcTask::b_col0);
+    if (q >= total_groups) return;
+    const TcTask &t = tasks[ti];
+    const int j0 = (int)(q - t.b_col0) * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+    const int jx = j0 + tx;
     float m = 0.f;
-    const int j = j0 + tx;
-    if (j < t.N)
-        for (int kk = ty; kk < 32; kk += 8) {
-            const int k = k0 + kk;
-            if (k < t.K) {
-                const cx<float> v = t.B[(long long)k * t.ldb + j];
-                m = fmaxf(m, fmaxf(fabsf(v.re), fabsf(v.im)));
-            }
+    if (jx < t.N)
+        for (int k = ty; k < t.K; k += 8) {
+            const cx<float> v = t.B[(long long)k * t.ldb + jx];
+            m = fmaxf(m, fmaxf(fabsf(v.re), fabsf(v.im)));
         }
     red[ty][tx] = m;
     __syncthreads();
-    if (ty == 0 && j < t.N) {
+    if (ty == 0) {
         for (int y = 1; y < 8; y++) m = fmaxf(m, red[y][tx]);
-        atomicMax(t.bmax + j, __float_as_uint(m));
-    }
-}
-
-// As k_split_a / k_split_b with scaled FP16 halves; the first k of each row
-// (column) also stores the inverse scale for the epilogue.
-__global__ void k_split_a_f16(const TcTask *__restrict__ tasks, int ntasks, long long total)
-{
-    const long long q0 = (long long)blockIdx.x * blockDim.x;
-    long long q = q0 + threadIdx.x;
-    const int ti = block_task(tasks, ntasks, q0, q < total ? q : total - 1, &TcTask::a_work0);
-    if (q >= total) return;
-    const TcTask &t = tasks[ti];
-    const long long r = q - t.a_work0;
-    const int kc = t.Kr / 2;
-    const int i = (int)(r / kc), k = (int)(r % kc);
-    const float sc = f16_scale(t.amax[i]);
-    if (k == 0) t.sa[i] = 1.f / sc;
-    cx<float> v(0.f, 0.f);
-    if (k < t.K) v = t.A[(long long)i * t.lda + k];
-    __half h0, l0, h1, l1;
-    split_f16(v.re * sc, h0, l0);
-    split_f16(v.im * sc, h1, l1);
-    const long long o = (long long)i * t.Kr + 2 * k;      // in halves
-    reinterpret_cast<__half2 *>(t.ahi)[o >> 1] = __halves2half2(h0, h1);
-    reinterpret_cast<__half2 *>(t.alo)[o >> 1] = __halves2half2(l0, l1);
-}
-
-__global__ void __launch_bounds__(256) k_split_b_f16(const TcTask *__restrict__ tasks, int ntasks,
-                                                     long long total_tiles)
-{
-    __shared__ float2 tile[32][33];
-    long long q = blockIdx.x;
-    if (q >= total_tiles) return;
-    int lo_t = 0, hi_t = ntasks - 1;
-    while (lo_t < hi_t) {
-        int mid = (lo_t + hi_t + 1) >> 1;
-        if (tasks[mid].b_work0 <= q) lo_t = mid;
-        else hi_t = mid - 1;
-    }
-    const TcTask &t = tasks[lo_t];
-    const long long r = q - t.b_work0;
-    const int kt = t.Kr / 64;
-    const int j0 = (int)(r / kt) * 32, k0 = (int)(r % kt) * 32;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int kk = ty; kk < 32; kk += 8) {
-        int k = k0 + kk, j = j0 + tx;
-        cx<float> v(0.f, 0.f);
-        if (k < t.K && j < t.N) v = t.B[(long long)k * t.ldb + j];
-        tile[kk][tx] = make_float2(v.re, v.im);
+        red[0][tx] = f16_scale(__float_as_uint(m));
+        if (jx < t.N) t.sb[jx] = 1.f / red[0][tx];
     }
     __syncthreads();
-    for (int jj = ty; jj < 32; jj += 8) {
-        const int j = j0 + jj;
-        if (j >= t.N) continue;
-        const float sc = f16_scale(t.bmax[j]);
-        const int k = k0 + tx;
-        if (k == 0) t.sb[j] = 1.f / sc;
-        const float br = tile[tx][jj].x * sc, bi = tile[tx][jj].y * sc;
-        __half rh, rl, ih, il, nih, nil;
-        split_f16(br, rh, rl);
-        split_f16(bi, ih, il);
-        split_f16(-bi, nih, nil);
-        const long long o0 = (long long)(2 * j) * t.Kr + 2 * k, o1 = o0 + t.Kr;   // in halves
-        __half2 *bh = reinterpret_cast<__half2 *>(t.bhi), *bl = reinterpret_cast<__half2 *>(t.blo);
-        bh[o0 >> 1] = __halves2half2(rh, nih);
-        bl[o0 >> 1] = __halves2half2(rl, nil);
-        bh[o1 >> 1] = __halves2half2(ih, rh);
-        bl[o1 >> 1] = __halves2half2(il, rl);
+    __half2 *bh = reinterpret_cast<__half2 *>(t.bhi), *bl = reinterpret_cast<__half2 *>(t.blo);
+    for (int k0 = 0; k0 < t.Kr / 2; k0 += 32) {
+        for (int kk = ty; kk < 32; kk += 8) {
+            const int k = k0 + kk;
+            cx<float> v(0.f, 0.f);
+            if (k < t.K && jx < t.N) v = t.B[(long long)k * t.ldb + jx];
+            tile[kk][tx] = make_float2(v.re, v.im);
+        }
+        __syncthreads();
+        for (int jj = ty; jj < 32; jj += 8) {
+            const int j = j0 + jj;
+            if (j < t.N) {
+                const float sc = red[0][jj];
+                const float br = tile[tx][jj].x * sc, bi = tile[tx][jj].y * sc;
+                const int k = k0 + tx;
+                __half rh, rl, ih, il, nih, nil;
+                split_f16(br, rh, rl);
+                split_f16(bi, ih, il);
+                split_f16(-bi, nih, nil);
+                const long long o0 = ((long long)(2 * j) * t.Kr + 2 * k) >> 1, o1 = o0 + (t.Kr >> 1);
+                bh[o0] = __halves2half2(rh, nih);
+                bl[o0] = __halves2half2(rl, nil);
+                bh[o1] = __halves2half2(ih, rh);
+                bl[o1] = __halves2half2(il, rl);
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -537,7 +506,7 @@ int tc_build_launch(TcLaunch &L, const GemmTask<float> *g, int n, float *ws)
     std::vector<TcTask> tasks(n);
     std::vector<CUtensorMap> maps(4 * n);
     const bool f16 = tc_f16_mode();
-    long long off = 0, tiles = 0, aw = 0, bw = 0, arows = 0;
+    long long off = 0, tiles = 0, aw = 0, bw = 0, arows = 0, bcols = 0;
     for (int i = 0; i < n; i++) {
         TcTask &t = tasks[i];
         t.A = g[i].A; t.lda = g[i].lda;
@@ -561,6 +530,8 @@ int tc_build_launch(TcLaunch &L, const GemmTask<float> *g, int n, float *ws)
         bw += (long long)((t.N + 31) / 32) * (t.Kr / 64);
         t.a_row0 = arows;
         arows += t.M;
+        t.b_col0 = bcols;
+        bcols += (t.N + 31) / 32;
         t.map0 = 4 * i;
         int rc;
         if (f16) {
@@ -576,27 +547,19 @@ int tc_build_launch(TcLaunch &L, const GemmTask<float> *g, int n, float *ws)
             return rc;
         }
     }
-    // f16 mode: the scale words of all tasks after the operands, column
-    // maxima contiguous (one memset clears them)
-    L.bmax0 = nullptr;
-    L.nbmax = 0;
-    if (f16) {
-        unsigned *bm = reinterpret_cast<unsigned *>(ws + off);
-        for (auto &t : tasks) { t.bmax = bm + L.nbmax; L.nbmax += t.N; }
-        L.bmax0 = bm;
-        off += align_up(L.nbmax, 64);
+    // f16 mode: the inverse scales of all tasks after the operands
+    if (f16)
         for (auto &t : tasks) {
-            t.amax = reinterpret_cast<unsigned *>(ws + off); off += align_up(t.M, 64);
             t.sa = ws + off; off += align_up(t.M, 64);
             t.sb = ws + off; off += align_up(t.N, 64);
         }
-    }
     L.f16 = f16;
     L.ntasks = n;
     L.tiles = tiles;
     L.a_work = aw;
     L.b_tiles = bw;
     L.a_rows = arows;
+    L.b_cols = bcols;
     int rc;
     if ((rc = L.tasks.upload(tasks))) return rc;
     std::vector<unsigned char> raw(maps.size() * sizeof(CUtensorMap));
@@ -609,11 +572,8 @@ void tc_split(const TcLaunch &L, cudaStream_t st)
 {
     if (L.ntasks == 0) return;
     if (L.f16) {
-        cudaMemsetAsync(L.bmax0, 0, sizeof(unsigned) * L.nbmax, st);
-        k_amax<<<ceil_div(L.a_rows * 32, 256), 256, 0, st>>>(L.tasks.p, L.ntasks, L.a_rows);
-        k_bmax<<<(unsigned)L.b_tiles, 256, 0, st>>>(L.tasks.p, L.ntasks, L.b_tiles);
-        k_split_a_f16<<<ceil_div(L.a_work, 256), 256, 0, st>>>(L.tasks.p, L.ntasks, L.a_work);
-        k_split_b_f16<<<(unsigned)L.b_tiles, 256, 0, st>>>(L.tasks.p, L.ntasks, L.b_tiles);
+        k_split_a_f16_rows<<<ceil_div(L.a_rows * 32, 256), 256, 0, st>>>(L.tasks.p, L.ntasks, L.a_rows);
+        k_split_b_f16_cols<<<(unsigned)L.b_cols, 256, 0, st>>>(L.tasks.p, L.ntasks, L.b_cols);
         return;
     }
     k_split_a<<<ceil_div(L.a_work, 256), 256, 0, st>>>(L.tasks.p, L.ntasks, L.a_work);

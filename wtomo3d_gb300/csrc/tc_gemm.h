@@ -11,24 +11,21 @@ struct TcTask {
     const cx<float> *B;
     cx<float> *C;
     float *ahi, *alo, *bhi, *blo;   // split operands in the launch workspace (FP16 pairs in the f16 mode)
-    // f16 mode: per row of A and per complex column of B, the largest |re|, |im|
-    // (float bits, for atomicMax) and the inverse of the power-of-two scale
-    unsigned *amax, *bmax;
+    // f16 mode: per row of A and per complex column of B, the inverse of the
+    // power-of-two scale
     float *sa, *sb;
     int lda, ldb, ldc, M, N, K, Kr;
     int tiles_n;
     int map0;                       // first of this task's 4 tensor maps
-    long long tile0, a_work0, b_work0, a_row0;
+    long long tile0, a_work0, b_work0, a_row0, b_col0;   // b_col0: first 32-column group of B (f16 split)
 };
 
 struct TcLaunch {
     DevVec<TcTask> tasks;
     DevVec<unsigned char> maps;    // CUtensorMap array (4 per task)
     int ntasks = 0;
-    long long tiles = 0, a_work = 0, b_tiles = 0, a_rows = 0;
+    long long tiles = 0, a_work = 0, b_tiles = 0, a_rows = 0, b_cols = 0;
     bool f16 = false;              // 2 x FP16 split with power-of-two row/column scales (else 3 x TF32)
-    unsigned *bmax0 = nullptr;     // the launch's column-maximum words (cleared before each split)
-    long long nbmax = 0;
 };
 
 // One GEMM of a tall-skinny tensor-core launch (substitution passes: N <= 32).
