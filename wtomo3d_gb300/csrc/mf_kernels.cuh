@@ -140,30 +140,14 @@ __global__ void k_extend_add(const EATask *__restrict__ tasks, int ntasks, long 
     const int nfP = P.p + P.b;
     cx<T> *pf = fac + P.fac;
     cx<T> *p22 = (P.parity ? upd1 : upd0) + P.upd;
-    // four entries per lane at a time: their loads are issued before the
-    // read-modify-writes (the compiler cannot reorder across the stores)
-    auto target = [&](int Cc) -> cx<T> * {
-        if (R < P.p) return pf + (long long)R * nfP + Cc;
-        if (Cc < P.p) return pf + (long long)P.p * nfP + (long long)(R - P.p) * P.p + Cc;
-        return p22 + (long long)(R - P.p) * P.b + (Cc - P.p);
-    };
-    int j = lane;
-    for (; j + 96 < C.b; j += 128) {
-        cx<T> v[4], d[4];
-        cx<T> *dst[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            v[u] = src[j + 32 * u];
-            dst[u] = target(rl[j + 32 * u]);
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++) d[u] = *dst[u];
-#pragma unroll
-        for (int u = 0; u < 4; u++) *dst[u] = d[u] + v[u];
-    }
-    for (; j < C.b; j += 32) {
-        cx<T> *dst = target(rl[j]);
-        *dst = *dst + src[j];
+    for (int j = lane; j < C.b; j += 32) {
+        const int Cc = rl[j];
+        cx<T> v = src[j];
+        cx<T> *dst;
+        if (R < P.p) dst = pf + (long long)R * nfP + Cc;
+        else if (Cc < P.p) dst = pf + (long long)P.p * nfP + (long long)(R - P.p) * P.p + Cc;
+        else dst = p22 + (long long)(R - P.p) * P.b + (Cc - P.p);
+        *dst = *dst + v;
     }
 }
 
