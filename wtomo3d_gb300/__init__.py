@@ -408,7 +408,7 @@ class Solver:
 
     def profile_factor(self):
         """Per-kernel-kind milliseconds of one factorisation (no graph)."""
-        kinds = ["memset", "scatter", "extend_add", "panel", "trsm", "gemm_simt", "diag_solve", "tc_split",
+        kinds = ["memset", "scatter", "extend_add", "panel", "trsm", "gemm_simt", "sub_step", "tc_split",
                  "gemm_tc"]
         out = np.zeros(len(kinds) + 2)
         _check(lib().wt3d_profile_factor(self._h, _ptr(out)))
@@ -454,7 +454,7 @@ class Solver:
     def profile_solve(self, m):
         """Per-kernel-kind milliseconds of one substitution pass over m columns
         and of one FP64 residual."""
-        kinds = ["memset", "scatter", "extend_add", "panel", "trsm", "gemm_simt", "diag_solve", "tc_split",
+        kinds = ["memset", "scatter", "extend_add", "panel", "trsm", "gemm_simt", "sub_step", "tc_split",
                  "gemm_tc"]
         out = np.zeros(12)
         _check(lib().wt3d_profile_solve(self._h, int(m), _ptr(out)))

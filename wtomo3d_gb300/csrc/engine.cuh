@@ -17,7 +17,7 @@ namespace wt3d {
 using Launch = std::function<void(cudaStream_t)>;
 
 // Launch kinds, for the per-kernel profile.
-enum LaunchKind { LK_MEMSET = 0, LK_SCATTER, LK_EXTEND_ADD, LK_PANEL, LK_TRSM, LK_GEMM, LK_DIAG, LK_SPLIT,
+enum LaunchKind { LK_MEMSET = 0, LK_SCATTER, LK_EXTEND_ADD, LK_PANEL, LK_TRSM, LK_GEMM, LK_SUBSTEP, LK_SPLIT,
                   LK_TCGEMM, LK_NKINDS };
 
 struct LaunchRec {
@@ -75,6 +75,7 @@ public:
     DevVec<cx<T>> fac, X, dinv;   // dinv: per KB panel L_D^{-1}, U_D^{-1} (KB x KB each)
     std::shared_ptr<FactorWorkspace<T>> ws;
     DevVec<int> ipiv, border;
+    DevVec<int> pord;   // per KB panel: the stored row at each position after its interchanges
     DevVec<int> rel;
     DevVec<FrontDev> fr;
     DevVec<long long> map;
@@ -110,7 +111,7 @@ public:
         size_t sw = 0;   // the solve schedules' tall-skinny workspaces
         for (const auto &m : ssched)
             for (const auto &kv : m) sw += kv.second->tsws.n * sizeof(float);
-        return (fac.n + X.n + dinv.n) * sizeof(cx<T>) + (ipiv.n + border.n + rel.n) * 4 + fr.n * sizeof(FrontDev) +
+        return (fac.n + X.n + dinv.n) * sizeof(cx<T>) + (ipiv.n + border.n + rel.n + pord.n) * 4 + fr.n * sizeof(FrontDev) +
                map.n * 8 + scale.n * 8 + own_tcws.n * sizeof(float) + sw;
     }
 
@@ -176,6 +177,7 @@ public:
         }
         if ((rc = fr.upload(h))) return rc;
         if ((rc = dinv.alloc((size_t)npan * 2 * KB * KB))) return rc;
+        if ((rc = pord.alloc((size_t)npan * KB))) return rc;
         // kernel attributes are per device: once for each device this process uses
         static std::once_flag attr_once[64];
         int dev = 0;
@@ -189,13 +191,11 @@ public:
             cudaFuncSetAttribute(k_trsm_col<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1))));
             if constexpr (std::is_same<T, float>::value) {
-                cudaFuncSetAttribute(k_trsm_row_reg<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (TRW + 1))));
-                cudaFuncSetAttribute(k_trsm_col_reg<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1))));
+                cudaFuncSetAttribute(k_trsm_row_h<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)band_row_smem());
+                cudaFuncSetAttribute(k_trsm_col_h<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)band_col_smem());
             }
-            cudaFuncSetAttribute(k_diag_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(cx<T>) * (KB * (KB + 1) + KB * (MAXRHS + 1))));
             cudaFuncSetAttribute(k_sub_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(cx<T>) * sub_step_smem_elems()));
         });
@@ -491,19 +491,19 @@ public:
                     size_t smc = sizeof(cx<T>) * (KB * (KB + 1) + TCR * (KB + 1));
                     sc->launches.push_back({[psc, this, p0, np, smp](cudaStream_t st) {
                         k_panel<T><<<np, 256, smp, st>>>(psc->panel.p + p0, fr.p, fac.p, ipiv.p, maxabs.p, pivot_rel,
-                                                         npert.p);
+                                                         npert.p, pord.p);
                     }, LK_PANEL, 0});
                     if (nr)
                         sc->launches.push_back({[psc, this, r0, nr, smr](cudaStream_t st) {
                             if constexpr (std::is_same<T, float>::value)
-                                k_trsm_row_reg<0><<<nr, TRW, smr, st>>>(psc->row.p + r0, fr.p, fac.p, ipiv.p);
+                                k_trsm_row_h<0><<<nr, TRW, band_row_smem(), st>>>(psc->row.p + r0, fr.p, fac.p, pord.p);
                             else
-                                k_trsm_row<T><<<nr, TRW, smr, st>>>(psc->row.p + r0, fr.p, fac.p, ipiv.p);
+                                k_trsm_row<T><<<nr, TRW, smr, st>>>(psc->row.p + r0, fr.p, fac.p, pord.p);
                         }, LK_TRSM, 0});
                     if (ncl)
                         sc->launches.push_back({[psc, this, cc0, ncl, smc](cudaStream_t st) {
                             if constexpr (std::is_same<T, float>::value)
-                                k_trsm_col_reg<0><<<ncl, TCR, smc, st>>>(psc->col.p + cc0, fr.p, fac.p);
+                                k_trsm_col_h<0><<<ncl, TCR, band_col_smem(), st>>>(psc->col.p + cc0, fr.p, fac.p);
                             else
                                 k_trsm_col<T><<<ncl, TCR, smc, st>>>(psc->col.p + cc0, fr.p, fac.p);
                         }, LK_TRSM, 0});
@@ -593,9 +593,9 @@ public:
             const int ns = (int)(hs.size() - s0);
             if (!ns) return;
             sc->launches.push_back({[psc, this, s0, ns, smd_step, m, mode, Xp, ldx](cudaStream_t st) {
-                k_sub_step<T><<<ns, SUB_THREADS, smd_step, st>>>(psc->step.p + s0, fr.p, fac.p, dinv.p, ipiv.p, Xp, ldx, m,
+                k_sub_step<T><<<ns, SUB_THREADS, smd_step, st>>>(psc->step.p + s0, fr.p, fac.p, dinv.p, pord.p, Xp, ldx, m,
                                                          mode, psc->zs.p);
-            }, LK_DIAG, 0, (double)ns * (KB * KB + 2.0 * KB * m) * sizeof(cx<T>)});
+            }, LK_SUBSTEP, 0, (double)ns * (KB * KB + 2.0 * KB * m) * sizeof(cx<T>)});
         };
         // the tasks of one panel step of front f (slot = its position in the level)
         auto add_step = [&](int f, int slot, int k, int kprev, int u0, int u1) {

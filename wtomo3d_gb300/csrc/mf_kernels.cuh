@@ -152,39 +152,64 @@ __global__ void k_extend_add(const EATask *__restrict__ tasks, int ntasks, long 
 }
 
 // Row order of panel k after its LINPACK-style interchanges: idx[i] is the
-// stored row that lands at position i.  The kb pivots are read in parallel
-// into piv_s first (one load each, not a chain of dependent loads by one
-// thread); all threads of the block must call this.
-__device__ __forceinline__ void panel_order(const int *__restrict__ ipiv, int first, int k, int kb, bool pivoted,
-                                            int *idx, int *piv_s)
+// stored row that lands at position i (the panel kernel stores it per panel
+// in pord; identity when not pivoted).  Threads tid < KB write idx; callers
+// synchronise before reading it.
+__device__ __forceinline__ void panel_rows(const int *__restrict__ pord, int pan, int kb, bool pivoted, int *idx)
 {
     const int tid = threadIdx.x;
-    if (pivoted && tid < kb) piv_s[tid] = ipiv[first + k + tid] - k;
-    __syncthreads();
-    if (tid == 0) {
-        for (int i = 0; i < kb; i++) idx[i] = i;
-        if (pivoted)
-            for (int j = 0; j < kb; j++) {
-                const int pv = piv_s[j];
-                const int a = idx[j]; idx[j] = idx[pv]; idx[pv] = a;
-            }
-    }
+    if (tid < KB) idx[tid] = (pivoted && tid < kb) ? pord[(long long)pan * KB + tid] : tid;
 }
 
 // ---------------------------------------------------------------------------
 // panel: LU of the KB x KB diagonal tile with partial pivoting inside the tile
 // ---------------------------------------------------------------------------
+// Columns of L_D^{-1} (thread c < KB) and U_D^{-1} (KB <= c < 2 KB) of the
+// factored kb x kb tile held in S (row stride KB + 1), padded to KB x KB with
+// the identity, stored row-major into Li and Ui.  Scratch: 2 KB columns of
+// KB + 1 elements after the tile.
+template <class T>
+__device__ __forceinline__ void tile_inverse_cols(const cx<T> *S, int kb, cx<T> *Li, cx<T> *Ui, int c)
+{
+    const int LD = KB + 1;
+    const bool up = c >= KB;
+    const int cc = up ? c - KB : c;
+    cx<T> *x = const_cast<cx<T> *>(S) + KB * LD + c * (KB + 1);
+    if (!up) {
+        for (int i = 0; i < KB; i++) {
+            cx<T> s = (i == cc) ? cx<T>(1) : cx<T>(0);
+            if (i < kb && cc < kb)
+                for (int l = cc; l < i; l++) s = s - S[i * LD + l] * x[l];
+            x[i] = s;
+        }
+    } else {
+        for (int i = KB - 1; i >= 0; i--) {
+            cx<T> s = (i == cc) ? cx<T>(1) : cx<T>(0);
+            if (i < kb && cc < kb) {
+                for (int l = i + 1; l <= cc; l++) s = s - S[i * LD + l] * x[l];
+                s = cdiv(s, S[i * LD + i]);
+            }
+            x[i] = s;
+        }
+    }
+    cx<T> *dst = up ? Ui : Li;
+    for (int i = 0; i < KB; i++) dst[i * KB + cc] = x[i];
+}
+
+// The stored row at each position after the tile's interchanges goes to the
+// panel's slot of pord (the row band and the substitution passes read it).
 template <class T>
 __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
                                                cx<T> *__restrict__ fac, int *__restrict__ ipiv,
                                                const unsigned long long *__restrict__ amax2, double pivot_rel,
-                                               int *__restrict__ npert)
+                                               int *__restrict__ npert, int *__restrict__ pord)
 {
     // static-pivot threshold: pivot_rel * max |a_ij| of the assembled operator
     const T thresh = (T)(pivot_rel * sqrt(__longlong_as_double((long long)*amax2)));
     extern __shared__ __align__(16) unsigned char smraw[];
     cx<T> *S = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1), then 2 KB scratch columns
     __shared__ int s_piv;
+    __shared__ int prow[KB];   // stored row at each position, as the interchanges go
     const PanelTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
     const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
@@ -196,6 +221,7 @@ __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tas
         int i = idx / kb, j = idx % kb;
         S[i * LD + j] = D[(long long)i * nf + j];
     }
+    if (tid < KB) prow[tid] = tid;
     __syncthreads();
     for (int j = 0; j < kb; j++) {
         if (tid < 32) {
@@ -222,6 +248,9 @@ __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tas
         __syncthreads();
         if (tid == 0) {
             ipiv[F.first + k + j] = k + pv;
+            const int a = prow[j];
+            prow[j] = prow[pv];
+            prow[pv] = a;
             cx<T> d = S[j * LD + j];
             T m2 = cabs2(d);
             if (!(m2 >= thresh * thresh)) {   // also catches NaN
@@ -246,6 +275,7 @@ __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tas
         int i = idx / kb, j = idx % kb;
         D[(long long)i * nf + j] = S[i * LD + j];
     }
+    if (tid < KB) pord[(long long)(F.pan + k / KB) * KB + tid] = prow[tid];
 }
 
 // ---------------------------------------------------------------------------
@@ -278,31 +308,7 @@ __global__ void __launch_bounds__(2 * KB) k_tile_inverse(const PanelTask *__rest
     }
     __syncthreads();
     cx<T> *Li = inv + (long long)(F.pan + k / KB) * (2 * KB * KB);
-    cx<T> *Ui = Li + KB * KB;
-    cx<T> *col = S + KB * LD;            // per-thread scratch column, 2 KB x (KB + 1)
-    const int c = tid;
-    const bool up = c >= KB;
-    const int cc = up ? c - KB : c;
-    cx<T> *x = col + c * (KB + 1);
-    if (!up) {
-        for (int i = 0; i < KB; i++) {
-            cx<T> s = (i == cc) ? cx<T>(1) : cx<T>(0);
-            if (i < kb && cc < kb)
-                for (int l = cc; l < i; l++) s = s - S[i * LD + l] * x[l];
-            x[i] = s;
-        }
-    } else {
-        for (int i = KB - 1; i >= 0; i--) {
-            cx<T> s = (i == cc) ? cx<T>(1) : cx<T>(0);
-            if (i < kb && cc < kb) {
-                for (int l = i + 1; l <= cc; l++) s = s - S[i * LD + l] * x[l];
-                s = cdiv(s, S[i * LD + i]);
-            }
-            x[i] = s;
-        }
-    }
-    cx<T> *dst = up ? Ui : Li;
-    for (int i = 0; i < KB; i++) dst[i * KB + cc] = x[i];
+    tile_inverse_cols<T>(S, kb, Li, Li + KB * KB, tid);
 }
 
 // ---------------------------------------------------------------------------
@@ -311,12 +317,12 @@ __global__ void __launch_bounds__(2 * KB) k_tile_inverse(const PanelTask *__rest
 constexpr int TRW = 128;   // columns per CTA
 template <class T>
 __global__ void __launch_bounds__(TRW) k_trsm_row(const RowTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
-                                                  cx<T> *__restrict__ fac, const int *__restrict__ ipiv)
+                                                  cx<T> *__restrict__ fac, const int *__restrict__ pord)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     cx<T> *L = reinterpret_cast<cx<T> *>(smraw);          // KB x (KB+1)
     cx<T> *Bt = L + KB * (KB + 1);                       // KB x (TRW+1)
-    __shared__ int idx[KB], piv_s[KB];
+    __shared__ int idx[KB];
     const RowTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
     const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
@@ -328,7 +334,7 @@ __global__ void __launch_bounds__(TRW) k_trsm_row(const RowTask *__restrict__ ta
         int i = q / kb, j = q % kb;
         L[i * (KB + 1) + j] = base[(long long)i * nf + k + j];
     }
-    panel_order(ipiv, F.first, k, kb, true, idx, piv_s);
+    panel_rows(pord, F.pan + k / KB, kb, true, idx);
     __syncthreads();
     #pragma unroll 8   // several loads in flight per thread
     for (int q = tid; q < kb * nc; q += blockDim.x) {
@@ -424,73 +430,98 @@ __device__ __forceinline__ void cp_async_wait_all()
 }
 
 // ---------------------------------------------------------------------------
-// complex64 variants of the two band solves with the band's vector in
-// registers.  Both are right-looking: once an unknown is final, its multiples
-// are subtracted from all later ones, which are independent of each other, so
-// the 64 x 64 / 2 multiply-adds per column (row) run as independent chains
-// instead of one dependent recurrence.  The KB x KB triangle is padded with the
-// identity beyond kb (a last, narrower panel), so the loops are fixed-length
-// and unroll completely.
+// complex64 band solves by substitution with the band's vector in registers,
+// one column (row band) or one row (column band) per thread.  Right-looking:
+// once an unknown is final, its multiples are subtracted from all later ones,
+// which are independent of each other, so the multiply-adds run as independent
+// chains instead of one dependent recurrence.  The 64 unknowns are taken in two
+// halves of 32 so that a thread never holds more than 32 complex values (a
+// 64-value vector plus the hoisted tile entries does not fit the register
+// file); the first half is parked in shared memory, in the thread's own column
+// (row), while the second half is updated with it.  The KB x KB tile is padded
+// with the identity beyond kb (a last, narrower panel), so every loop is
+// fixed-length and unrolls completely.
 // ---------------------------------------------------------------------------
+constexpr int HB = KB / 2;
+__host__ __device__ constexpr size_t band_row_smem() { return sizeof(cx<float>) * (KB * (KB + 1) + KB * (TRW + 1)); }
+__host__ __device__ constexpr size_t band_col_smem() { return sizeof(cx<float>) * (KB * (KB + 1) + TCR * (KB + 1)); }
+
+__device__ __forceinline__ void cfms(cx<float> &d, const cx<float> a, const cx<float> b)   // d -= a b
+{
+    d.re = fmaf(-a.re, b.re, fmaf(a.im, b.im, d.re));
+    d.im = fmaf(-a.re, b.im, fmaf(-a.im, b.re, d.im));
+}
+
 template <int UNUSED = 0>
-__global__ void __launch_bounds__(TRW) k_trsm_row_reg(const RowTask *__restrict__ tasks,
-                                                             const FrontDev *__restrict__ fr, cx<float> *__restrict__ fac,
-                                                      const int *__restrict__ ipiv)
+__global__ void __launch_bounds__(TRW) k_trsm_row_h(const RowTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
+                                                    cx<float> *__restrict__ fac, const int *__restrict__ pord)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    cx<float> *L = reinterpret_cast<cx<float> *>(smraw);          // KB x (KB+1)
-    cx<float> *Bt = L + KB * (KB + 1);                           // KB x (TRW+1)
-    __shared__ int idx[KB], piv_s[KB];
+    cx<float> *L = reinterpret_cast<cx<float> *>(smraw);   // KB x (KB+1)
+    cx<float> *Bt = L + KB * (KB + 1);                    // KB x (TRW+1): band rows as stored
+    __shared__ int idx[KB];
     const RowTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
     const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
     const int c0 = t.c0, nc = min(TRW, nf - c0);
     const int tid = threadIdx.x;
     cx<float> *base = fac + F.fac + (long long)k * nf;
-    // tile and band in one batch of asynchronous copies, band rows as stored
     for (int q = tid; q < KB * KB; q += blockDim.x) {
         const int i = q / KB, j = q % KB;
         if (i < kb && j < kb) cp_async_cx(L + i * (KB + 1) + j, base + (long long)i * nf + k + j);
-        else L[i * (KB + 1) + j] = cx<float>(0.f, 0.f);
+        else L[i * (KB + 1) + j] = cx<float>(i == j ? 1.f : 0.f, 0.f);
     }
     for (int q = tid; q < kb * nc; q += blockDim.x) {
         const int i = q / nc, c = q % nc;
         cp_async_cx(Bt + i * (TRW + 1) + c, base + (long long)i * nf + c0 + c);
     }
-    panel_order(ipiv, F.first, k, kb, true, idx, piv_s);
+    panel_rows(pord, F.pan + k / KB, kb, true, idx);
     cp_async_wait_all();
     __syncthreads();
-    // the panel's row interchanges applied as the band is read
-    cx<float> b[KB];
+    // Row i of the result is kept in the stored slot idx[i] of the row it
+    // came from: the slots of rows not yet read stay untouched.
+    if (tid < nc) {
+        cx<float> *col = Bt + tid;
+        cx<float> b[HB];
 #pragma unroll
-    for (int i = 0; i < KB; i++) b[i] = (i < kb) ? Bt[idx[i] * (TRW + 1) + tid] : cx<float>(0.f, 0.f);
+        for (int i = 0; i < HB; i++) b[i] = i < kb ? col[idx[i] * (TRW + 1)] : cx<float>(0.f, 0.f);
 #pragma unroll
-    for (int l = 0; l < KB - 1; l++) {
-        const cx<float> bl = b[l];
+        for (int l = 0; l < HB - 1; l++)
 #pragma unroll
-        for (int i = l + 1; i < KB; i++) {
-            const cx<float> a = L[i * (KB + 1) + l];
-            b[i].re = fmaf(-a.re, bl.re, fmaf(a.im, bl.im, b[i].re));
-            b[i].im = fmaf(-a.re, bl.im, fmaf(-a.im, bl.re, b[i].im));
+            for (int i = l + 1; i < HB; i++) cfms(b[i], L[i * (KB + 1) + l], b[l]);
+#pragma unroll
+        for (int i = 0; i < HB; i++)
+            if (i < kb) col[idx[i] * (TRW + 1)] = b[i];
+#pragma unroll
+        for (int i = 0; i < HB; i++) b[i] = HB + i < kb ? col[idx[HB + i] * (TRW + 1)] : cx<float>(0.f, 0.f);
+#pragma unroll 4
+        for (int l = 0; l < HB; l++) {
+            const cx<float> xl = l < kb ? col[idx[l] * (TRW + 1)] : cx<float>(0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < HB; i++) cfms(b[i], L[(HB + i) * (KB + 1) + l], xl);
         }
-    }
 #pragma unroll
-    for (int i = 0; i < KB; i++)
-        if (i < kb) Bt[i * (TRW + 1) + tid] = b[i];
+        for (int l = 0; l < HB - 1; l++)
+#pragma unroll
+            for (int i = l + 1; i < HB; i++) cfms(b[i], L[(HB + i) * (KB + 1) + HB + l], b[l]);
+#pragma unroll
+        for (int i = 0; i < HB; i++)
+            if (HB + i < kb) col[idx[HB + i] * (TRW + 1)] = b[i];
+    }
     __syncthreads();
     for (int q = tid; q < kb * nc; q += blockDim.x) {
         const int i = q / nc, c = q % nc;
-        base[(long long)i * nf + c0 + c] = Bt[i * (TRW + 1) + c];
+        base[(long long)i * nf + c0 + c] = Bt[idx[i] * (TRW + 1) + c];
     }
 }
 
 template <int UNUSED = 0>
-__global__ void __launch_bounds__(TCR) k_trsm_col_reg(const ColTask *__restrict__ tasks,
-                                                      const FrontDev *__restrict__ fr, cx<float> *__restrict__ fac)
+__global__ void __launch_bounds__(TCR) k_trsm_col_h(const ColTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
+                                                    cx<float> *__restrict__ fac)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    cx<float> *U = reinterpret_cast<cx<float> *>(smraw);          // KB x (KB+1)
-    cx<float> *Xs = U + KB * (KB + 1);                           // TCR x (KB+1)
+    cx<float> *U = reinterpret_cast<cx<float> *>(smraw);   // KB x (KB+1)
+    cx<float> *Xs = U + KB * (KB + 1);                    // TCR x (KB+1)
     __shared__ cx<float> invd[KB];
     const ColTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
@@ -522,24 +553,35 @@ __global__ void __launch_bounds__(TCR) k_trsm_col_reg(const ColTask *__restrict_
     __syncthreads();
     for (int j = tid; j < KB; j += blockDim.x) invd[j] = cdiv(cx<float>(1.f, 0.f), U[j * (KB + 1) + j]);
     __syncthreads();
-    cx<float> x[KB];
-#pragma unroll
-    for (int j = 0; j < KB; j++) x[j] = (j < kb && tid < nr) ? Xs[tid * (KB + 1) + j] : cx<float>(0.f, 0.f);
-#pragma unroll
-    for (int j = 0; j < KB; j++) {
-        x[j] = x[j] * invd[j];
-        const cx<float> xj = x[j];
-#pragma unroll
-        for (int j2 = j + 1; j2 < KB; j2++) {
-            const cx<float> u = U[j * (KB + 1) + j2];
-            x[j2].re = fmaf(-xj.re, u.re, fmaf(xj.im, u.im, x[j2].re));
-            x[j2].im = fmaf(-xj.re, u.im, fmaf(-xj.im, u.re, x[j2].im));
-        }
-    }
     if (tid < nr) {
+        cx<float> *row = Xs + tid * (KB + 1);
+        cx<float> x[HB];
 #pragma unroll
-        for (int j = 0; j < KB; j++)
-            if (j < kb) Xs[tid * (KB + 1) + j] = x[j];
+        for (int j = 0; j < HB; j++) x[j] = j < kb ? row[j] : cx<float>(0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < HB; j++) {
+            x[j] = x[j] * invd[j];
+#pragma unroll
+            for (int j2 = j + 1; j2 < HB; j2++) cfms(x[j2], x[j], U[j * (KB + 1) + j2]);
+        }
+#pragma unroll
+        for (int j = 0; j < HB; j++) row[j] = x[j];
+#pragma unroll
+        for (int j = 0; j < HB; j++) x[j] = HB + j < kb ? row[HB + j] : cx<float>(0.f, 0.f);
+#pragma unroll 4
+        for (int l = 0; l < HB; l++) {
+            const cx<float> xl = row[l];
+#pragma unroll
+            for (int j = 0; j < HB; j++) cfms(x[j], xl, U[l * (KB + 1) + HB + j]);
+        }
+#pragma unroll
+        for (int j = 0; j < HB; j++) {
+            x[j] = x[j] * invd[HB + j];
+#pragma unroll
+            for (int j2 = j + 1; j2 < HB; j2++) cfms(x[j2], x[j], U[(HB + j) * (KB + 1) + HB + j2]);
+        }
+#pragma unroll
+        for (int j = 0; j < HB; j++) row[HB + j] = x[j];
     }
     __syncthreads();
     for (int q = tid; q < nr * kb; q += blockDim.x) {
@@ -744,65 +786,6 @@ __global__ void __launch_bounds__(256, 2) k_gemm_ts(const GemmTask<T> *__restric
 }
 
 // ---------------------------------------------------------------------------
-// solve: diagonal-tile substitution on the RHS block of a front, as a dense
-// product with the tile inverses the panel kernel stored (L_D^{-1}, U_D^{-1}):
-// mode 0: forward   Y <- L_D^{-1} P Y        (P: the tile's row interchanges)
-// mode 1: backward  Y <- U_D^{-1} Y
-// mode 2: adjoint forward  Y <- U_D^{-H} Y
-// mode 3: adjoint backward Y <- P^T L_D^{-H} Y
-// ---------------------------------------------------------------------------
-template <class T>
-__global__ void __launch_bounds__(256) k_diag_solve(const PanelTask *__restrict__ tasks,
-                                                    const FrontDev *__restrict__ fr,
-                                                    const cx<T> *__restrict__ inv, const int *__restrict__ ipiv,
-                                                    cx<T> *__restrict__ X, int ldx, int m, int mode)
-{
-    extern __shared__ __align__(16) unsigned char smraw[];
-    cx<T> *Ms = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1): the operator of this mode
-    cx<T> *Ys = Ms + KB * (KB + 1);                 // KB x (MAXRHS+1)
-    __shared__ int idx[KB], piv_s[KB];
-    const PanelTask t = tasks[blockIdx.x];
-    const FrontDev F = fr[t.f];
-    const int k = t.k, kb = min(KB, F.p - k);
-    const int tid = threadIdx.x;
-    const cx<T> *Li = inv + (long long)(F.pan + k / KB) * (2 * KB * KB);
-    const cx<T> *Mi = (mode == 0 || mode == 3) ? Li : Li + KB * KB;
-    const bool herm = mode >= 2;
-    #pragma unroll 8   // several loads in flight per thread
-    for (int q = tid; q < KB * KB; q += blockDim.x) {
-        const int i = q / KB, j = q % KB;
-        Ms[i * (KB + 1) + j] = herm ? conj(Mi[j * KB + i]) : Mi[i * KB + j];
-    }
-    panel_order(ipiv, F.first, k, kb, mode == 0 || mode == 3, idx, piv_s);
-    __syncthreads();
-    cx<T> *Y = X + (long long)(F.first + k) * ldx;
-    const int LY = MAXRHS + 1;
-    #pragma unroll 8   // several loads in flight per thread
-    for (int q = tid; q < kb * m; q += blockDim.x) {
-        const int i = q / m, c = q % m;
-        Ys[i * LY + c] = Y[(long long)(mode == 0 ? idx[i] : i) * ldx + c];
-    }
-    __syncthreads();
-    // out[i][c] = sum_l M[i][l] Y[l][c]; each thread keeps its outputs in registers
-    constexpr int PER = (KB * MAXRHS + 255) / 256;
-    cx<T> acc[PER];
-    int oi[PER], oc[PER];
-#pragma unroll
-    for (int r = 0; r < PER; r++) {
-        const int q = tid + r * 256;
-        oi[r] = q / m;
-        oc[r] = q % m;
-        acc[r] = cx<T>(0);
-        if (oi[r] < kb)
-            for (int l = 0; l < kb; l++) acc[r] = acc[r] + Ms[oi[r] * (KB + 1) + l] * Ys[l * LY + oc[r]];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < PER; r++)
-        if (oi[r] < kb) Y[(long long)(mode == 3 ? idx[oi[r]] : oi[r]) * ldx + oc[r]] = acc[r];
-}
-
-// ---------------------------------------------------------------------------
 // Fused substitution step: the diagonal-tile product of panel k and the update
 // of the outer block's other rows, in one launch per panel step (the panel
 // steps of a block form a dependent chain; one launch instead of two halves
@@ -822,24 +805,41 @@ constexpr int SUB_RB = 64;   // rows per update CTA
 // Shared-memory layout of k_sub_step (complex elements).
 __host__ __device__ constexpr int sub_step_smem_elems()
 {
-    return KB * (KB + 1) + KB * (MAXRHS + 1) + SUB_RB * (KB + 1) + SUB_RB * (MAXRHS + 1);
+    return KB * KB + KB * (MAXRHS + 1) + KB * SUB_RB + SUB_RB * (MAXRHS + 1);
+}
+
+// four consecutive complex values from 16-byte-aligned shared memory
+__device__ __forceinline__ void lds4(const cx<float> *p, cx<float> (&a)[4])
+{
+    const float4 u = reinterpret_cast<const float4 *>(p)[0], v = reinterpret_cast<const float4 *>(p)[1];
+    a[0] = cx<float>(u.x, u.y); a[1] = cx<float>(u.z, u.w); a[2] = cx<float>(v.x, v.y); a[3] = cx<float>(v.z, v.w);
+}
+__device__ __forceinline__ void lds4(const cx<double> *p, cx<double> (&a)[4])
+{
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const double2 u = reinterpret_cast<const double2 *>(p)[j];
+        a[j] = cx<double>(u.x, u.y);
+    }
 }
 
 constexpr int SUB_THREADS = 512;   // 16 warps: each thread sums 4 rows of Z and 4 update rows
 template <class T>
 __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
                                                   const cx<T> *__restrict__ fac, const cx<T> *__restrict__ inv,
-                                                  const int *__restrict__ ipiv, cx<T> *__restrict__ X, int ldx, int m,
+                                                  const int *__restrict__ pord, cx<T> *__restrict__ X, int ldx, int m,
                                                   int mode, cx<T> *__restrict__ zs)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    // every input is fetched in one batch of asynchronous copies, as stored;
-    // the pivot order and the conjugate transposes apply when it is read
-    cx<T> *Ms = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1): the mode's tile inverse as stored
-    cx<T> *Ys = Ms + KB * (KB + 1);                 // KB x (MAXRHS+1): panel rows as stored, then Z
-    cx<T> *As = Ys + KB * (MAXRHS + 1);             // SUB_RB x (KB+1) (modes 0, 1) or KB x (SUB_RB+1)
-    cx<T> *Yr = As + SUB_RB * (KB + 1);             // SUB_RB x (MAXRHS+1): the update CTA's rows of X
-    __shared__ int idx[KB], piv_s[KB];
+    // every input is fetched in one batch of asynchronous copies, laid out so
+    // that the four rows a thread sums are adjacent: Ms[l][i] is the mode's
+    // tile-inverse entry (i, l) (conjugated on read for modes 2, 3), As[l][r]
+    // the update CTA's factor entry (r, l) (likewise)
+    cx<T> *Ms = reinterpret_cast<cx<T> *>(smraw);   // KB x KB
+    cx<T> *Ys = Ms + KB * KB;                       // KB x (MAXRHS+1): panel rows as stored, then Z
+    cx<T> *As = Ys + KB * (MAXRHS + 1);             // KB x SUB_RB
+    cx<T> *Yr = As + KB * SUB_RB;                   // SUB_RB x (MAXRHS+1): the update CTA's rows of X
+    __shared__ int idx[KB];
     const StepTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
     const int tid = threadIdx.x;
@@ -853,7 +853,10 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
     const bool herm = mode >= 2;
     const int nr = t.role == 1 ? t.r1 - t.r0 : 0;
     const cx<T> *P = fac + F.fac;
-    for (int q = tid; q < KB * KB; q += blockDim.x) cp_async_cx(Ms + (q >> 6) * (KB + 1) + (q & 63), Mi + q);
+    // stored inverse entry q = (a, b): (i, l) = (a, b) transposed into Ms[l][i],
+    // or (l, i) = (a, b) as stored for the conjugate transposes
+    for (int q = tid; q < KB * KB; q += blockDim.x)
+        cp_async_cx(herm ? Ms + q : Ms + (q & (KB - 1)) * KB + (q >> 6), Mi + q);
     for (int q = tid; q < kb * m; q += blockDim.x) {
         const int i = q / m, c = q % m;
         cp_async_cx(Ys + i * LY + c, Y + (long long)(k + i) * ldx + c);
@@ -862,12 +865,12 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
         if (mode == 0 || mode == 1) {   // A(r, l) = P[r0 + r][k + l]
             for (int q = tid; q < nr * kb; q += blockDim.x) {
                 const int r = q / kb, l = q % kb;
-                cp_async_cx(As + r * (KB + 1) + l, P + (long long)(t.r0 + r) * nf + k + l);
+                cp_async_cx(As + l * SUB_RB + r, P + (long long)(t.r0 + r) * nf + k + l);
             }
-        } else {                        // A(r, l) = conj(P[k + l][r0 + r]), stored as As[l][r]
+        } else {                        // A(r, l) = conj(P[k + l][r0 + r])
             for (int q = tid; q < kb * nr; q += blockDim.x) {
                 const int l = q / nr, r = q % nr;
-                cp_async_cx(As + l * (SUB_RB + 1) + r, P + (long long)(k + l) * nf + t.r0 + r);
+                cp_async_cx(As + l * SUB_RB + r, P + (long long)(k + l) * nf + t.r0 + r);
             }
         }
         for (int q = tid; q < nr * m; q += blockDim.x) {
@@ -885,27 +888,25 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
             Y[(long long)(t.kprev + i) * ldx + c] = slot[i * MAXRHS + c];
         }
     }
-    panel_order(ipiv, F.first, k, kb, mode == 0 || mode == 3, idx, piv_s);
+    panel_rows(pord, F.pan + k / KB, kb, mode == 0 || mode == 3, idx);
     cp_async_wait_all();
     __syncthreads();
-    // Z = M y: thread (lane c, warp w) owns rows w, w + NW, w + 2 NW, ... of
-    // column c; the k loop runs outside, so its sums are independent chains
-    // (M entries are warp broadcasts)
+    // Z = M y: thread (lane c, warp w) owns rows 4w .. 4w+3 of column c; the
+    // l loop runs outside, so its sums are independent chains (M entries are
+    // warp broadcasts, two 16-byte loads per l for complex64)
     constexpr int NW = SUB_THREADS / 32, RPT = KB / NW;
-    const int c = tid & 31, w = tid >> 5;
+    static_assert(RPT == 4 && SUB_RB / NW == 4, "four rows per thread");
+    const int c = tid & 31, w = tid >> 5, i0 = RPT * w;
     cx<T> acc[RPT];
 #pragma unroll
     for (int j = 0; j < RPT; j++) acc[j] = cx<T>(0);
     if (c < m) {
         for (int l = 0; l < kb; l++) {
             const cx<T> y = Ys[(mode == 0 ? idx[l] : l) * LY + c];
-            if (!herm) {
+            cx<T> a[4];
+            lds4(Ms + l * KB + i0, a);
 #pragma unroll
-                for (int j = 0; j < RPT; j++) acc[j] = acc[j] + Ms[(w + NW * j) * (KB + 1) + l] * y;
-            } else {
-#pragma unroll
-                for (int j = 0; j < RPT; j++) acc[j] = acc[j] + conj(Ms[l * (KB + 1) + w + NW * j]) * y;
-            }
+            for (int j = 0; j < RPT; j++) acc[j] = acc[j] + (herm ? conj(a[j]) : a[j]) * y;
         }
     }
     __syncthreads();
@@ -913,7 +914,7 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
     if (c < m) {
 #pragma unroll
         for (int j = 0; j < RPT; j++) {
-            const int i = w + NW * j;
+            const int i = i0 + j;
             if (i < kb) Ys[(mode == 3 ? idx[i] : i) * LY + c] = acc[j];
         }
     }
@@ -928,25 +929,21 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
         }
         return;
     }
-    // rows w, w + NW, ... of column c, independent sums as above
-    constexpr int UPT = SUB_RB / NW;
+    // rows 4w .. 4w+3 of column c, independent sums as above
     if (c < m) {
-        cx<T> u[UPT];
+        cx<T> u[RPT];
 #pragma unroll
-        for (int j = 0; j < UPT; j++) u[j] = cx<T>(0);
+        for (int j = 0; j < RPT; j++) u[j] = cx<T>(0);
         for (int l = 0; l < kb; l++) {
             const cx<T> z = Ys[l * LY + c];
-            if (mode == 0 || mode == 1) {
+            cx<T> a[4];
+            lds4(As + l * SUB_RB + i0, a);
 #pragma unroll
-                for (int j = 0; j < UPT; j++) u[j] = u[j] + As[(w + NW * j) * (KB + 1) + l] * z;
-            } else {
-#pragma unroll
-                for (int j = 0; j < UPT; j++) u[j] = u[j] + conj(As[l * (SUB_RB + 1) + w + NW * j]) * z;
-            }
+            for (int j = 0; j < RPT; j++) u[j] = u[j] + (herm ? conj(a[j]) : a[j]) * z;
         }
 #pragma unroll
-        for (int j = 0; j < UPT; j++) {
-            const int r = w + NW * j;
+        for (int j = 0; j < RPT; j++) {
+            const int r = i0 + j;
             if (r < nr) Y[(long long)(t.r0 + r) * ldx + c] = Yr[r * LY + c] - u[j];
         }
     }

@@ -416,10 +416,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // q = w mod 4) in 32-column chunks; each chunk goes through a 32 x 33
         // transpose buffer so that C is read-modified-written one row segment
         // (32 floats, 128 bytes) per warp instruction.
+        // Each lane also prefetches its row of the CTA's next C tile into L2
+        // (128-byte lines, none outside the row's own span), so that the
+        // read-modify-write of a short-K tile finds C there.
         const int q = warp & 3;
         float *tb = epi + (warp - 2) * (32 * 33);
+        auto prefetch_c = [&](long long g) {
+            if (g >= ntiles) return;
+            int pm0, pn0r;
+            const TcTask *pt = tc_tile(tasks, ntasks, g, pm0, pn0r);
+            const int r = pm0 + 32 * q + lane, c0 = pn0r >> 1;
+            if (r >= pt->M || c0 >= pt->N) return;
+            const char *p = reinterpret_cast<const char *>(pt->C + (long long)r * pt->ldc + c0);
+            const int nb = 8 * min(TC_BNR / 2, pt->N - c0);
+            for (int off = 0; off < nb; off += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + off));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(p + nb - 1));
+        };
+        prefetch_c(blockIdx.x);
         int it = 0;
         for (long long gt = blockIdx.x; gt < ntiles; gt += gridDim.x, it++) {
+            prefetch_c(gt + gridDim.x);
             int m0, n0r;
             const TcTask *t = tc_tile(tasks, ntasks, gt, m0, n0r);
             const int b = it & 1;
