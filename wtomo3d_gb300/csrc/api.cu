@@ -569,7 +569,10 @@ int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, d
 // Plain refinement continues while a pass cuts the worst residual by at least
 // this factor (WT3D_REFINE_SWITCH, default 0.08); otherwise the solve
 // switches to the flexible GMRES, which reaches the tolerance in fewer
-// passes once refinement converges more slowly than that.
+// passes once refinement converges more slowly than that.  The first pass
+// counts as a refinement step from x = 0 (relative residual 1), so a
+// preconditioner that leaves more than that fraction of the right-hand side
+// goes to GMRES after one pass.
 static double refine_switch()
 {
     static const double v = [] {
@@ -581,8 +584,8 @@ static double refine_switch()
 }
 
 // Refinement driver over m <= MAXRHS columns held in h->Bn; result in h->Xn.
-// Plain iterative refinement while it reduces the worst residual at least
-// fourfold per step; flexible GMRES preconditioned by the same factors
+// Plain iterative refinement while each step reduces the worst residual by
+// the switch factor; flexible GMRES preconditioned by the same factors
 // otherwise (a few near-singular modes of the preconditioned operator slow
 // refinement down, and the Krylov solver removes them in a few steps).
 template <class T>
@@ -597,7 +600,8 @@ int refine(wt3d_solver *h, Engine<T> &E, int m, bool adjoint, double tol, int ma
     WT_CUDA(cudaMemcpyAsync(h->Rn.p, h->Bn.p, sizeof(double2) * n * MAXRHS, cudaMemcpyDeviceToDevice, st));
     std::vector<double> hn(2 * MAXRHS);
     int it = 0, rc = WT3D_OK;
-    double prev_worst = INFINITY;
+    // the first pass is a refinement step from x = 0, whose relative residual is 1
+    double prev_worst = 1.0;
     const int th = 256;
     const unsigned nb = (unsigned)ceil_div(n * m, th);
     for (;;) {
@@ -621,7 +625,7 @@ int refine(wt3d_solver *h, Engine<T> &E, int m, bool adjoint, double tol, int ma
         if (!(worst == worst)) { rc = WT3D_ERR_NOCONV; break; }   // NaN
         if (worst <= tol) break;
         if (it >= maxit) { rc = WT3D_ERR_NOCONV; break; }
-        if (it >= 1 && worst > refine_switch() * prev_worst) {
+        if (worst > refine_switch() * prev_worst) {
             std::vector<double> bn2(hn.begin() + MAXRHS, hn.begin() + MAXRHS + m), rn2(hn.begin(), hn.begin() + m);
             it++;
             rc = fgmres<T>(h, E, sc, m, adjoint, tol, maxit, bn2, rn2, relres, it);

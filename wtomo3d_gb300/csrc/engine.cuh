@@ -593,8 +593,20 @@ public:
             const int ns = (int)(hs.size() - s0);
             if (!ns) return;
             sc->launches.push_back({[psc, this, s0, ns, smd_step, m, mode, Xp, ldx](cudaStream_t st) {
-                k_sub_step<T><<<ns, SUB_THREADS, smd_step, st>>>(psc->step.p + s0, fr.p, fac.p, dinv.p, pord.p, Xp, ldx, m,
-                                                         mode, psc->zs.p);
+                // programmatic dependent launch: see k_sub_step
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3((unsigned)ns);
+                cfg.blockDim = dim3(SUB_THREADS);
+                cfg.dynamicSmemBytes = smd_step;
+                cfg.stream = st;
+                cudaLaunchAttribute at[1];
+                at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+                at[0].val.programmaticStreamSerializationAllowed = 1;
+                cfg.attrs = at;
+                cfg.numAttrs = 1;
+                cudaLaunchKernelEx(&cfg, k_sub_step<T>, (const StepTask *)(psc->step.p + s0), (const FrontDev *)fr.p,
+                                   (const cx<T> *)fac.p, (const cx<T> *)dinv.p, (const int *)pord.p, Xp, ldx, m, mode,
+                                   psc->zs.p);
             }, LK_SUBSTEP, 0, (double)ns * (KB * KB + 2.0 * KB * m) * sizeof(cx<T>)});
         };
         // the tasks of one panel step of front f (slot = its position in the level)

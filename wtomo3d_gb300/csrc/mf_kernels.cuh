@@ -830,6 +830,11 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
                                                   const int *__restrict__ pord, cx<T> *__restrict__ X, int ldx, int m,
                                                   int mode, cx<T> *__restrict__ zs)
 {
+    // Launched as a programmatic dependent of the previous step: the next
+    // step may start as soon as every CTA of this one is running; it fetches
+    // what no step writes (task, tile inverse, factor rows, row order) and
+    // then waits for this grid's completion before it touches X or the slots.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     extern __shared__ __align__(16) unsigned char smraw[];
     // every input is fetched in one batch of asynchronous copies, laid out so
     // that the four rows a thread sums are adjacent: Ms[l][i] is the mode's
@@ -857,10 +862,6 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
     // or (l, i) = (a, b) as stored for the conjugate transposes
     for (int q = tid; q < KB * KB; q += blockDim.x)
         cp_async_cx(herm ? Ms + q : Ms + (q & (KB - 1)) * KB + (q >> 6), Mi + q);
-    for (int q = tid; q < kb * m; q += blockDim.x) {
-        const int i = q / m, c = q % m;
-        cp_async_cx(Ys + i * LY + c, Y + (long long)(k + i) * ldx + c);
-    }
     if (nr) {
         if (mode == 0 || mode == 1) {   // A(r, l) = P[r0 + r][k + l]
             for (int q = tid; q < nr * kb; q += blockDim.x) {
@@ -873,13 +874,22 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
                 cp_async_cx(As + l * SUB_RB + r, P + (long long)(k + l) * nf + t.r0 + r);
             }
         }
+    }
+    panel_rows(pord, F.pan + k / KB, kb, mode == 0 || mode == 3, idx);
+    // everything below reads or writes rows of X or the slots
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    for (int q = tid; q < kb * m; q += blockDim.x) {
+        const int i = q / m, c = q % m;
+        cp_async_cx(Ys + i * LY + c, Y + (long long)(k + i) * ldx + c);
+    }
+    if (nr) {
         for (int q = tid; q < nr * m; q += blockDim.x) {
             const int r = q / m, c = q % m;
             cp_async_cx(Yr + r * LY + c, Y + (long long)(t.r0 + r) * ldx + c);
         }
     }
     // while the copies fly: the previous panel's solved rows into X (roles
-    // 0 and 3; no CTA of this launch reads those rows) and the pivot order
+    // 0 and 3; no CTA of this launch reads those rows)
     if (t.role != 1 && t.kprev >= 0) {
         const int kbp = min(KB, F.p - t.kprev);
         #pragma unroll 8   // several loads in flight per thread
@@ -888,7 +898,6 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
             Y[(long long)(t.kprev + i) * ldx + c] = slot[i * MAXRHS + c];
         }
     }
-    panel_rows(pord, F.pan + k / KB, kb, mode == 0 || mode == 3, idx);
     cp_async_wait_all();
     __syncthreads();
     // Z = M y: thread (lane c, warp w) owns rows 4w .. 4w+3 of column c; the

@@ -440,7 +440,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const TcTask *t = tc_tile(tasks, ntasks, gt, m0, n0r);
             const int b = it & 1;
             const uint32_t use = (uint32_t)(it >> 1);
-            if (!mbar_wait(&tfull[b], use & 1u)) { atomicCAS(err, 0, 3); break; }
+            const bool got = mbar_wait(&tfull[b], use & 1u);
+            if (!__all_sync(0xffffffffu, got)) { atomicCAS(err, 0, 3); break; }   // warp-uniform: tcgen05.ld below
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * TC_BNR);
             const int row0 = m0 + 32 * q;

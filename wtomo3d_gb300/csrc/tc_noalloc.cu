@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(NB_THREADS, 1)
     } else if (warp >= 2) {
         if (!bar_wait(accum, 0)) {
             atomicCAS(&g_err, 0, 3);
-            if (lane == 0) atomicOr(epi_fail, 1);
+            atomicOr(epi_fail, 1);
         }
         __syncwarp();
         // every epilogue warp learns whether any of them gave up before the

@@ -188,10 +188,11 @@ inline int make_map_f16(CUtensorMap *m, void *base, long long rows, int Kr, int 
 }
 
 // 2-D FP32 tensor map of rows x width floats with a row stride in bytes (a
-// multiple of 16), boxes of 32 floats x box_rows, no swizzle; reads outside the
-// tensor return zeros.
+// multiple of 16), boxes of 32 floats x box_rows, in the 128-byte swizzle when
+// swz128 (16-byte chunk c of box row r lands at chunk c ^ (r mod 8)), else
+// unswizzled; reads outside the tensor return zeros.
 inline int make_map_plain(CUtensorMap *m, const float *base, long long rows, long long width, long long stride_bytes,
-                          int box_rows)
+                          int box_rows, bool swz128 = false)
 {
     auto fn = encode_fn();
     if (!fn) { set_error("cuTensorMapEncodeTiled unavailable"); return WT3D_ERR_CUDA; }
@@ -200,7 +201,8 @@ inline int make_map_plain(CUtensorMap *m, const float *base, long long rows, lon
     cuuint32_t box[2] = {32u, (cuuint32_t)box_rows};
     cuuint32_t es[2] = {1, 1};
     CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), gdim, gstr, box, es,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, swz128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));

@@ -1,59 +1,65 @@
 // Tall-skinny complex64 GEMM  C -= A B  on the tcgen05 tensor cores, for the
 // substitution passes of the solve: A is a factor block (M x K, K-major rows
 // in the front storage, any leading dimension) or, in the adjoint passes, the
-// conjugate transpose of one, and B and C hold at most 32 right-hand sides.  Each factor entry is used for 32 complex multiply-adds
-// only, so the kernel is meant to run at the speed of reading A from HBM.
+// conjugate transpose of one, and B and C hold at most 32 right-hand sides.
+// Each factor entry is used for 32 complex multiply-adds only, so the kernel
+// is meant to run at the speed of reading A from HBM.
 //
-// A is not copied or pre-split: front blocks start and stride at arbitrary
-// 8-byte boundaries, which rules out TMA, so eight loader warps stream A with
-// 8-byte asynchronous copies (cp.async, one 128-byte row segment per
-// half-warp) into a ring of TS_RAW raw stages (~112 KB per SM in flight),
-// then split every value into TF32 hi + lo (x = hi + lo to ~2^-24)
-// and store both halves into the 128-byte-swizzled K-major tiles the MMA
-// reads.  B is expanded once per
-// launch into the 64 x 2K real matrix B~ (rows 2j, 2j+1 of column j, as in the
-// square tensor-core GEMM), split into hi and lo, and fetched by TMA.  The
-// complex product is the real product A_r B~^T into a 128 x 64 FP32 TMEM
-// accumulator with D = Ahi Bhi + Ahi Blo + Alo Bhi.
+// A is not copied or pre-split.  It is streamed into a ring of TS_RAW raw
+// stages in shared memory (128 rows x 16 complex k, 16 KB, in the 128-byte
+// swizzle): by TMA when the task's block is 16-byte aligned with an even row
+// stride, otherwise by 8-byte asynchronous copies of the loader warps (one
+// 128-byte row segment per half-warp, or 32 consecutive stored entries per
+// warp for the conjugate transpose).  The loader warps then split every value
+// into TF32 hi + lo (x = hi + lo to ~2^-24) and store both halves into tensor
+// memory: the MMA takes A from TMEM (row i of the tile in lane i), so the
+// split operand never goes through shared memory, whose bandwidth bounded the
+// kernel when it did.  B is expanded once per launch into the 64 x 2K real
+// matrix B~ (rows 2j, 2j+1 of column j, as in the square tensor-core GEMM),
+// split into hi and lo, and fetched by TMA.  The complex product is the real
+// product A_r B~^T into a 128 x 64 FP32 TMEM accumulator with
+// D = Ahi Bhi + Ahi Blo + Alo Bhi.
 //
 // Work unit = (task, 128-row tile, K-chunk); persistent CTAs, one per SM.
-// Warps 0-15 load and split A, warp 16 issues the TMA copies of B~ (and owns
-// the TMEM allocation), warp 17 (one lane) issues the MMAs, warp 18 streams A
-// by TMA in the variant for 16-byte-aligned blocks with even strides (the
-// loaders then only convert), warps 19-22 drain the double-buffered
-// accumulator: C -= D in place, or with atomics when the task is split along K
-// or its rows are scattered (border updates).  Every mbarrier wait is bounded;
-// on expiry the kernel records an error code and winds down as the square
-// kernel does.
+// Warps 0-15 convert A (warp w: TMEM lanes 32 (w mod 4) .., complex k
+// 4 (w / 4) .. of each stage) and, in the copy variant, copy it; warp 16
+// issues the TMA copies of B~ and owns the TMEM allocation; warp 17 (one lane)
+// issues the MMAs; warp 18 streams A by TMA in the aligned variant; warps
+// 19-22 drain the double-buffered accumulator: C -= D in place, or with
+// atomics when the task is split along K or its rows are scattered (border
+// updates).  Every mbarrier wait is bounded; on expiry the kernel records an
+// error code and winds down as the square kernel does.
 #include "tc_gemm.h"
 #include "tc_ptx.cuh"
 #include <cstring>
 
 namespace wt3d {
 
-constexpr int TS_BM = 128;                        // complex rows per tile (MMA M)
+constexpr int TS_BM = 128;                        // complex rows per tile (MMA M, TMEM lanes)
 constexpr int TS_NR = 64;                         // real accumulator columns: 32 complex (MMA N)
 constexpr int TS_KC = 16;                         // complex k per stage: one 128-byte swizzle row
-constexpr int TS_STAGES = 2;                      // split A stages (hi + lo)
+constexpr int TS_TSTAGES = 4;                     // split A stages in TMEM (hi + lo: 64 columns each)
 constexpr int TS_BSTAGES = 2;                     // B~ stages (TMA from L2)
-constexpr int TS_A_BYTES = TS_BM * 128;           // 16 KB per split half
 constexpr int TS_B_BYTES = TS_NR * 128;           // 8 KB per split half
-constexpr int TS_ASTAGE_BYTES = 2 * TS_A_BYTES;
 constexpr int TS_BSTAGE_BYTES = 2 * TS_B_BYTES;
-constexpr int TS_RAW = 8;                         // raw A stages in flight (asynchronous copies)
+constexpr int TS_RAW = 10;                        // raw A stages in flight
 constexpr int TS_RAW_BYTES = TS_BM * TS_KC * 8;   // 16 KB
-constexpr int TS_B_OFF = TS_STAGES * TS_ASTAGE_BYTES;
+constexpr int TS_B_OFF = 0;
 constexpr int TS_RAW_OFF = TS_B_OFF + TS_BSTAGES * TS_BSTAGE_BYTES;
 constexpr int TS_BAR_OFF = TS_RAW_OFF + TS_RAW * TS_RAW_BYTES;
 constexpr int TS_SMEM = TS_BAR_OFF + 1024 + 512;
+constexpr int TS_ACC_COLS = 2 * TS_NR;            // TMEM columns of the two accumulators
+constexpr int TS_TMEM_COLS = 512;                 // accumulators + TS_TSTAGES x 64 (power of two)
+static_assert(TS_ACC_COLS + TS_TSTAGES * 64 <= TS_TMEM_COLS, "TMEM budget");
 constexpr int TS_LOADERS = 16;                    // loader warps
 constexpr int TS_WB = TS_LOADERS, TS_WM = TS_LOADERS + 1, TS_WA = TS_LOADERS + 2, TS_WE = TS_LOADERS + 3;
 constexpr int TS_THREADS = (TS_LOADERS + 7) * 32; // + B producer, MMA, A producer (TMA variant), 4 epilogue warps
 constexpr int TS_LT = TS_LOADERS * 32;            // loader threads
-constexpr int TS_PER_THREAD = TS_BM * TS_KC / TS_LT;   // complex elements per loader thread per stage
-constexpr int TS_QROWS = TS_LT / TS_KC;           // rows between a thread's elements
+constexpr int TS_PER_THREAD = TS_BM * TS_KC / TS_LT;   // complex elements a loader thread copies per stage
+constexpr int TS_QROWS = TS_LT / TS_KC;           // rows between a thread's copied elements
 static_assert(TS_PER_THREAD * TS_LT == TS_BM * TS_KC && TS_QROWS % 8 == 0, "loader mapping");
 static_assert((TS_LT / TS_BM) * TS_PER_THREAD == TS_KC, "conjugate-transposed loader mapping");
+static_assert(TS_LOADERS == 16, "conversion mapping: 4 lane quarters x 4 k parts");
 
 // Unit u of a launch: its task, first row, and K range [k0, k1).
 __device__ __forceinline__ const TsTask *ts_unit(const TsTask *__restrict__ tasks, int ntasks, long long u, int &m0,
@@ -114,106 +120,131 @@ __global__ void __launch_bounds__(256) k_ts_expand_b(const TsTask *__restrict__ 
     }
 }
 
-// Position of a CTA's loaders in its sequence of stages: unit u (every
-// gridDim.x-th unit from blockIdx.x), its K range and stage i within it, with
-// the per-thread quantities of the unit precomputed.  A stage is 128 rows x
-// 16 k of the operand; loader thread l owns TS_PER_THREAD of its elements:
-//   A as stored (row-major, K-major): row TS_QROWS q + l / 16, column l % 16:
-//     a half-warp reads one contiguous 128-byte row segment, and all of a
-//     thread's elements share one column;
-//   A^H (conjugate transpose of a stored K x M block, MN-major): row l % 128,
-//     column l / 128 + 4 q: a warp reads 32 consecutive stored entries of one
-//     stored row, and all of a thread's elements share one row.
-struct TsCursor {
+// byte offset of element (row r, complex column k) of a raw stage in the
+// 128-byte swizzle: 16-byte chunk c of row r sits at chunk c ^ (r mod 8)
+__device__ __forceinline__ int ts_swz(int r, int k)
+{
+    return r * 128 + ((((k >> 1) ^ (r & 7))) << 4) + ((k & 1) << 3);
+}
+
+// Position in the CTA's sequence of stages: unit u (every gridDim.x-th unit
+// from blockIdx.x), its K range and stage i within it.
+struct TsStage {
     const TsTask *t;
-    const cx<float> *src;   // element q = 0 of stage 0 of this thread
-    long long u, qstep;     // complex elements between the thread's elements q and q + 1
-    long long sstep;        // complex elements between consecutive stages
-    int k0, k1, nsub, i;
-    int nq;                 // A: elements in range (rows); A^H: 4 if the row is in range, else 0
-    int kq;                 // first column of this thread within a stage
-    bool valid, conj;
+    long long u;
+    int m0, k0, k1, nsub, i;
+    bool valid;
 };
 
-__device__ __forceinline__ void ts_cursor_at(TsCursor &c, const TsTask *__restrict__ tasks, int ntasks, long long nunits,
-                                             long long u, int l)
+__device__ __forceinline__ void ts_stage_at(TsStage &c, const TsTask *__restrict__ tasks, int ntasks, long long nunits,
+                                            long long u)
 {
     c.u = u;
     c.valid = u < nunits;
     if (!c.valid) return;
-    int m0;
-    c.t = ts_unit(tasks, ntasks, u, m0, c.k0, c.k1);
+    c.t = ts_unit(tasks, ntasks, u, c.m0, c.k0, c.k1);
     c.nsub = (c.k1 - c.k0 + TS_KC - 1) / TS_KC;
     c.i = 0;
-    const int M = c.t->M;
-    const long long lda = c.t->lda;
-    c.conj = c.t->conjA != 0;
-    if (!c.conj) {
-        const int r0 = m0 + (l >> 4);
-        c.kq = l & 15;
-        c.nq = r0 < M ? min(TS_PER_THREAD, (M - r0 + TS_QROWS - 1) / TS_QROWS) : 0;
-        c.qstep = (long long)TS_QROWS * lda;
-        c.sstep = TS_KC;
-        c.src = c.t->A + (long long)r0 * lda + c.k0 + c.kq;
+}
+
+__device__ __forceinline__ void ts_stage_next(TsStage &c, const TsTask *__restrict__ tasks, int ntasks,
+                                              long long nunits)
+{
+    if (++c.i == c.nsub) ts_stage_at(c, tasks, ntasks, nunits, c.u + gridDim.x);
+}
+
+// The loader thread l's asynchronous 8-byte copies of one stage into the
+// swizzled raw slot at shared address raw:
+//   A as stored (row-major, K-major): row TS_QROWS q + l / 16, column l % 16 -
+//     a half-warp reads one contiguous 128-byte row segment;
+//   A^H (conjugate transpose of a stored K x M block): row l % 128, column
+//     l / 128 + 4 q - a warp reads 32 consecutive stored entries of one
+//     stored row.
+// Elements outside the operand are not copied; the conversion zeroes them.
+__device__ __forceinline__ void ts_copy(const TsStage &c, int l, uint32_t raw)
+{
+    const TsTask *t = c.t;
+    const int kb = c.k0 + c.i * TS_KC;
+    const int M = t->M;
+    const long long lda = t->lda;
+    if (!t->conjA) {
+        const int kc = l & 15, k = kb + kc;
+        if (k >= c.k1) return;
+#pragma unroll
+        for (int q = 0; q < TS_PER_THREAD; q++) {
+            const int r = TS_QROWS * q + (l >> 4);
+            if (c.m0 + r < M)
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(raw + (uint32_t)ts_swz(r, kc)),
+                             "l"(t->A + (long long)(c.m0 + r) * lda + k)
+                             : "memory");
+        }
     } else {
-        const int r = m0 + (l & (TS_BM - 1));
-        c.kq = l / TS_BM;
-        c.nq = r < M ? TS_PER_THREAD : 0;
-        c.qstep = (long long)(TS_LT / TS_BM) * lda;
-        c.sstep = (long long)TS_KC * lda;
-        c.src = c.t->A + (long long)(c.k0 + c.kq) * lda + r;
+        const int r = l & (TS_BM - 1);
+        if (c.m0 + r >= M) return;
+#pragma unroll
+        for (int q = 0; q < TS_PER_THREAD; q++) {
+            const int kc = (l / TS_BM) + (TS_LT / TS_BM) * q, k = kb + kc;
+            if (k < c.k1)
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(raw + (uint32_t)ts_swz(r, kc)),
+                             "l"(t->A + (long long)k * lda + c.m0 + r)
+                             : "memory");
+        }
     }
 }
 
-__device__ __forceinline__ void ts_cursor_next(TsCursor &c, const TsTask *__restrict__ tasks, int ntasks,
-                                               long long nunits, int l)
-{
-    if (++c.i == c.nsub) ts_cursor_at(c, tasks, ntasks, nunits, c.u + gridDim.x, l);
-}
-
-// elements q < ts_count of the cursor's stage lie in the operand
-__device__ __forceinline__ int ts_count(const TsCursor &c)
-{
-    const int kb = c.k0 + c.i * TS_KC + c.kq;   // column of element q = 0
-    if (!c.conj) return kb < c.k1 ? c.nq : 0;
-    constexpr int kstep = TS_LT / TS_BM;         // columns between a thread's elements
-    return c.nq ? max(0, min(TS_PER_THREAD, (c.k1 - kb + kstep - 1) / kstep)) : 0;
-}
-
-// asynchronous 8-byte copies of the thread's elements into its slots raw[q][l]
-__device__ __forceinline__ void ts_issue(const TsCursor &c, int l, uint32_t raw)
-{
-    const int n = ts_count(c);
-    const cx<float> *src = c.src + c.i * c.sstep;
-#pragma unroll
-    for (int q = 0; q < TS_PER_THREAD; q++)
-        if (q < n)
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(raw + (uint32_t)((q * TS_LT + l) * 8)),
-                         "l"(src + q * c.qstep)
-                         : "memory");
-}
-
-// byte offset of element (row r, column k) of a stage in a 128-byte-swizzled
-// K-major tile: 16-byte chunk c of row r sits at chunk c ^ (r mod 8)
-__device__ __forceinline__ int ts_swz(int r, int k)
-{
-    return (r >> 3) * 1024 + (r & 7) * 128 + ((((k >> 1) ^ (r & 7))) << 4) + ((k & 1) << 3);
-}
-
 // hi = TF32 rounding of x (to nearest), lo = TF32 rounding of x - hi
-__device__ __forceinline__ void split_cvt(float x, float &hi, float &lo)
+__device__ __forceinline__ void split_cvt(float x, uint32_t &hi, uint32_t &lo)
 {
-    uint32_t h, lw;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
-    hi = __uint_as_float(h);
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lw) : "f"(x - hi));
-    lo = __uint_as_float(lw);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(x - __uint_as_float(hi)));
 }
 
-// TMA = false: loaders copy A with cp.async (any alignment, as stored or
-// conjugate-transposed).  TMA = true: every task's A is 16-byte aligned with an
-// even row stride, as stored; warp TS_WA streams raw 128 x 16 complex tiles of
-// A into the ring by TMA and the loaders only convert.
+// The loader thread's part of a stage: tile row r = 32 (w mod 4) + lane,
+// complex k 4 (w / 4) .. + 3, read from the raw slot, conjugated for A^H,
+// zero outside the operand, split and stored into TMEM columns col_hi + 0..7
+// (hi) and col_hi + 32 + 0..7 (lo) of the thread's lane.
+__device__ __forceinline__ void ts_convert(const TsStage &c, const uint8_t *rs, uint32_t tmem_lane, int col_hi,
+                                           int r, int kpart)
+{
+    const int kbase = c.k0 + c.i * TS_KC + 4 * kpart;
+    const bool rv = c.m0 + r < c.t->M;
+    float v[8];
+    const float4 a = rv ? *reinterpret_cast<const float4 *>(rs + r * 128 + (((2 * kpart) ^ (r & 7)) << 4))
+                        : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 b = rv ? *reinterpret_cast<const float4 *>(rs + r * 128 + (((2 * kpart + 1) ^ (r & 7)) << 4))
+                        : make_float4(0.f, 0.f, 0.f, 0.f);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    const float ys = c.t->conjA ? -1.f : 1.f;
+    uint32_t h[8], lw[8];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const bool kv = kbase + j < c.k1;
+        split_cvt(kv ? v[2 * j] : 0.f, h[2 * j], lw[2 * j]);
+        split_cvt(kv ? ys * v[2 * j + 1] : 0.f, h[2 * j + 1], lw[2 * j + 1]);
+    }
+    const uint32_t th = tmem_lane + (uint32_t)col_hi, tl = th + 32;
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(th),
+                 "r"(h[0]), "r"(h[1]), "r"(h[2]), "r"(h[3]), "r"(h[4]), "r"(h[5]), "r"(h[6]), "r"(h[7])
+                 : "memory");
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(tl),
+                 "r"(lw[0]), "r"(lw[1]), "r"(lw[2]), "r"(lw[3]), "r"(lw[4]), "r"(lw[5]), "r"(lw[6]), "r"(lw[7])
+                 : "memory");
+}
+
+// D (+)= A B with A in tensor memory (kind::tf32, M = 128: row i in lane i)
+__device__ __forceinline__ void umma_tf32_ta(uint32_t tmem_d, uint32_t tmem_a, uint64_t db, uint32_t idesc,
+                                             uint32_t acc)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "r"(tmem_a), "l"(db), "r"(idesc), "r"(acc));
+}
+
+// TMA = false: the loader warps copy A with cp.async (any alignment, as
+// stored or conjugate-transposed).  TMA = true: every task's A is 16-byte
+// aligned with an even row stride, as stored; warp TS_WA streams the raw
+// 128 x 16 complex tiles by TMA.
 template <bool TMA>
 __global__ void __launch_bounds__(TS_THREADS, 1)
     k_tc_ts(const TsTask *__restrict__ tasks, int ntasks, long long nunits, const CUtensorMap *__restrict__ maps,
@@ -221,9 +252,9 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + TS_BAR_OFF);   // split A stage written (8 loader warps)
-    uint64_t *empty = full + TS_STAGES;                                  // split A stage consumed (MMA commit)
-    uint64_t *bfull = empty + TS_STAGES;                                 // B~ stage landed (TMA)
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + TS_BAR_OFF);   // TMEM A stage written (16 loader warps)
+    uint64_t *empty = full + TS_TSTAGES;                                 // TMEM A stage consumed (MMA commit)
+    uint64_t *bfull = empty + TS_TSTAGES;                                // B~ stage landed (TMA)
     uint64_t *bempty = bfull + TS_BSTAGES;                               // B~ stage consumed (MMA commit)
     uint64_t *tfull = bempty + TS_BSTAGES;
     uint64_t *tempty = tfull + 2;
@@ -235,11 +266,11 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == TS_WB) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
-                     "r"(2 * TS_NR));
+                     "r"(TS_TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (threadIdx.x == TS_WM * 32) {
-        for (int s = 0; s < TS_STAGES; s++) {
+        for (int s = 0; s < TS_TSTAGES; s++) {
             mbar_init(&full[s], TS_LOADERS);
             mbar_init(&empty[s], 1);
         }
@@ -264,22 +295,28 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
     const uint32_t tmem = *tmem_holder;
 
     if (warp < TS_LOADERS) {
-        // ---------------- A loaders: global -> raw ring -> split -> swizzled tiles ----------------
+        // ---------------- A loaders: (copy) -> raw ring -> split -> TMEM ----------------
         // The copy cursor runs TS_RAW - 1 stages ahead of the conversion
         // cursor, across unit boundaries; one commit group per stage (empty
-        // groups past the end keep the count uniform).
+        // groups past the end keep the count uniform).  In the copy variant
+        // the loaders read each other's copies, so every stage passes one
+        // named barrier of the 512 loader threads; a loader whose wait timed
+        // out keeps looping (without converting) so that none is left at it.
         const int l = threadIdx.x;
+        const int r = 32 * (warp & 3) + lane, kpart = warp >> 2;
+        const uint32_t tlane = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
         uint8_t *rawb = smem + TS_RAW_OFF;
         const uint32_t raw0 = smem_u32(rawb);
-        TsCursor cp, cs;
-        ts_cursor_at(cs, tasks, ntasks, nunits, blockIdx.x, l);
-        long long gc = 0, g = 0;
+        TsStage cp, cs;
+        ts_stage_at(cs, tasks, ntasks, nunits, blockIdx.x);
+        long long g = 0;
+        bool ok = true;
         if constexpr (!TMA) {
-            ts_cursor_at(cp, tasks, ntasks, nunits, blockIdx.x, l);
-            for (int p = 0; p < TS_RAW - 1; p++, gc++) {
+            ts_stage_at(cp, tasks, ntasks, nunits, blockIdx.x);
+            for (int p = 0; p < TS_RAW - 1; p++) {
                 if (cp.valid) {
-                    ts_issue(cp, l, raw0 + (uint32_t)((gc % TS_RAW) * TS_RAW_BYTES));
-                    ts_cursor_next(cp, tasks, ntasks, nunits, l);
+                    ts_copy(cp, l, raw0 + (uint32_t)(p * TS_RAW_BYTES));
+                    ts_stage_next(cp, tasks, ntasks, nunits);
                 }
                 asm volatile("cp.async.commit_group;" ::: "memory");
             }
@@ -287,49 +324,32 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
         while (cs.valid) {
             const int slot = (int)(g % TS_RAW);
             if constexpr (!TMA) {
+                asm volatile("cp.async.wait_group %0;" ::"n"(TS_RAW - 2) : "memory");   // own copies of stage g
+                asm volatile("bar.sync 1, %0;" ::"n"(TS_LT) : "memory");                // everyone's; slot g-1 free
                 if (cp.valid) {
-                    ts_issue(cp, l, raw0 + (uint32_t)((gc % TS_RAW) * TS_RAW_BYTES));
-                    ts_cursor_next(cp, tasks, ntasks, nunits, l);
+                    ts_copy(cp, l, raw0 + (uint32_t)(((g + TS_RAW - 1) % TS_RAW) * TS_RAW_BYTES));
+                    ts_stage_next(cp, tasks, ntasks, nunits);
                 }
                 asm volatile("cp.async.commit_group;" ::: "memory");
-                gc++;
-                asm volatile("cp.async.wait_group %0;" ::"n"(TS_RAW - 1) : "memory");   // stage g has landed
             } else {
-                if (!mbar_wait(&rfull[slot], (uint32_t)((g / TS_RAW) & 1))) { atomicCAS(err, 0, 16); break; }
+                if (ok && !mbar_wait(&rfull[slot], (uint32_t)((g / TS_RAW) & 1))) { atomicCAS(err, 0, 16); ok = false; }
             }
-            const uint8_t *rs = rawb + slot * TS_RAW_BYTES;
-            const int s = (int)(g % TS_STAGES);
-            const uint32_t ph = (uint32_t)((g / TS_STAGES) & 1) ^ 1u;
-            if (!mbar_wait(&empty[s], ph)) { atomicCAS(err, 0, 11); break; }
-            uint8_t *ahi = smem + s * TS_ASTAGE_BYTES, *alo = ahi + TS_A_BYTES;
-            const int nq = ts_count(cs);
-            const float ysign = cs.conj ? -1.f : 1.f;
-#pragma unroll
-            for (int q = 0; q < TS_PER_THREAD; q++) {
-                float2 v = make_float2(0.f, 0.f);
-                if (q < nq) {
-                    if constexpr (TMA)   // the TMA box: row r of the stage at r * 128 bytes
-                        v = *reinterpret_cast<const float2 *>(rs + (TS_QROWS * q + (l >> 4)) * 128 + (l & 15) * 8);
-                    else                 // the thread's own slots raw[q][l]
-                        v = reinterpret_cast<const float2 *>(rs)[q * TS_LT + l];
-                }
-                v.y *= ysign;
-                const int off = cs.conj ? ts_swz(l & (TS_BM - 1), cs.kq + q * (TS_LT / TS_BM))
-                                        : ts_swz(TS_QROWS * q + (l >> 4), l & 15);
-                float h0, l0, h1, l1;
-                split_cvt(v.x, h0, l0);
-                split_cvt(v.y, h1, l1);
-                *reinterpret_cast<float2 *>(ahi + off) = make_float2(h0, h1);
-                *reinterpret_cast<float2 *>(alo + off) = make_float2(l0, l1);
+            const int s = (int)(g % TS_TSTAGES);
+            if (ok && !mbar_wait(&empty[s], (uint32_t)((g / TS_TSTAGES) & 1) ^ 1u)) { atomicCAS(err, 0, 11); ok = false; }
+            ok = __all_sync(0xffffffffu, ok);   // the tcgen05 stores below are warp-collective
+            if (ok) {
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                ts_convert(cs, rawb + slot * TS_RAW_BYTES, tlane, TS_ACC_COLS + 64 * s + 8 * kpart, r, kpart);
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;");
             }
-            // generic-proxy stores become visible to the tensor core's async proxy
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
-            if (lane == 0) {
+            if (ok && lane == 0) {
                 mbar_arrive(&full[s]);
                 if constexpr (TMA) mbar_arrive(&rempty[slot]);
             }
-            ts_cursor_next(cs, tasks, ntasks, nunits, l);
+            if (TMA && !ok) break;
+            ts_stage_next(cs, tasks, ntasks, nunits);
             g++;
         }
         if constexpr (!TMA) asm volatile("cp.async.wait_all;" ::: "memory");   // no copy into shared memory outlives the CTA
@@ -398,24 +418,22 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t dacc = tmem + (uint32_t)(b * TS_NR);
             for (int i = 0; i < nsub; i++, g++) {
-                const int s = (int)(g % TS_STAGES), sb = (int)(g % TS_BSTAGES);
-                if (!mbar_wait(&full[s], (uint32_t)((g / TS_STAGES) & 1)) ||
+                const int s = (int)(g % TS_TSTAGES), sb = (int)(g % TS_BSTAGES);
+                if (!mbar_wait(&full[s], (uint32_t)((g / TS_TSTAGES) & 1)) ||
                     !mbar_wait(&bfull[sb], (uint32_t)((g / TS_BSTAGES) & 1))) {
                     atomicCAS(err, 0, 13);
                     ok = false;
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t a_hi = smem_u32(smem + s * TS_ASTAGE_BYTES), a_lo = a_hi + TS_A_BYTES;
+                const uint32_t a_hi = tmem + (uint32_t)(TS_ACC_COLS + 64 * s), a_lo = a_hi + 32;
                 const uint32_t b_hi = smem_u32(smem + TS_B_OFF + sb * TS_BSTAGE_BYTES), b_lo = b_hi + TS_B_BYTES;
 #pragma unroll
-                for (int kk = 0; kk < 4; kk++) {
-                    const uint32_t off = kk * 32;   // 8 TF32 values along K
-                    const uint64_t dah = sw128_desc(a_hi + off), dal = sw128_desc(a_lo + off);
-                    const uint64_t dbh = sw128_desc(b_hi + off), dbl = sw128_desc(b_lo + off);
-                    umma_tf32(dacc, dah, dbh, idesc, (i | kk) != 0);
-                    umma_tf32(dacc, dah, dbl, idesc, 1);
-                    umma_tf32(dacc, dal, dbh, idesc, 1);
+                for (int kk = 0; kk < 4; kk++) {   // 8 TF32 values along K: 8 TMEM columns, 32 bytes of B~
+                    const uint64_t dbh = sw128_desc(b_hi + kk * 32), dbl = sw128_desc(b_lo + kk * 32);
+                    umma_tf32_ta(dacc, a_hi + 8 * kk, dbh, idesc, (i | kk) != 0);
+                    umma_tf32_ta(dacc, a_hi + 8 * kk, dbl, idesc, 1);
+                    umma_tf32_ta(dacc, a_lo + 8 * kk, dbh, idesc, 1);
                 }
                 umma_commit(&empty[s]);
                 umma_commit(&bempty[sb]);
@@ -436,7 +454,8 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
             const TsTask *t = ts_unit(tasks, ntasks, u, m0, k0, k1);
             const int b = it & 1;
             const uint32_t use = (uint32_t)(it >> 1);
-            if (!mbar_wait(&tfull[b], use & 1u)) { atomicCAS(err, 0, 15); break; }
+            const bool got = mbar_wait(&tfull[b], use & 1u);
+            if (!__all_sync(0xffffffffu, got)) { atomicCAS(err, 0, 15); break; }   // warp-uniform: tcgen05.ld below
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * TS_NR);
             const int r = m0 + 32 * q + lane;
@@ -482,7 +501,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
     __syncthreads();
     if (warp == TS_WB) {
         asm volatile("tcgen05.fence::after_thread_sync;");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TS_NR));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TS_TMEM_COLS));
     }
 }
 
@@ -558,7 +577,7 @@ int ts_build_launch(TsLaunch &L, const GemmTask<float> *g, int n, float *ws, boo
         if (tma) {
             if (!ts_tma_ok(g[i])) { set_error("ts_build_launch: task not addressable by TMA"); return WT3D_ERR_ARG; }
             if ((rc = make_map_plain(&maps[3 * i + 2], reinterpret_cast<const float *>(t.A), t.M, 2LL * t.K,
-                                     8LL * t.lda, TS_BM)))
+                                     8LL * t.lda, TS_BM, true)))
                 return rc;
         }
     }
