@@ -507,7 +507,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=2.0, help="seconds of sampled fronts per CPU step")
     ap.add_argument("--no-c1", action="store_true", help="reference arm: skip the full 40^3 CPU factor and solve")
     ap.add_argument("--fp64-freqs", type=lambda t: [float(x) for x in t.split(",") if x],
-                    default=[0.5, 2.0], help="frequencies of the FP64 GPU factorisation leg ('' skips it)")
+                    default=[0.5], help="frequencies of the FP64 GPU factorisation leg (one factorisation takes "
+                    "~6 min; 0.5 Hz is the frequency where the mixed solve needs GMRES; '' skips it)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--clocks-log", default=None, help="file for the nvidia-smi samples of the timed region")

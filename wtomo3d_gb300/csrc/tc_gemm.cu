@@ -415,10 +415,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // Lane l of warp w reads accumulator row 32 q + l (TMEM lane quarter
         // q = w mod 4) in 32-column chunks; each chunk goes through a 32 x 33
         // transpose buffer so that C is read-modified-written one row segment
-        // (32 floats, 128 bytes) per warp instruction.
+        // (32 floats, 128 bytes) per warp instruction.  C does not depend on
+        // the accumulator, so the loads of a tile's first two chunks are issued
+        // before its MMAs are waited for, and every later chunk's loads one
+        // chunk ahead of its stores (64 row segments in flight per warp).
         // Each lane also prefetches its row of the CTA's next C tile into L2
-        // (128-byte lines, none outside the row's own span), so that the
-        // read-modify-write of a short-K tile finds C there.
+        // (128-byte lines, none outside the row's own span).
         const int q = warp & 3;
         float *tb = epi + (warp - 2) * (32 * 33);
         auto prefetch_c = [&](long long g) {
@@ -440,35 +442,43 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const TcTask *t = tc_tile(tasks, ntasks, gt, m0, n0r);
             const int b = it & 1;
             const uint32_t use = (uint32_t)(it >> 1);
+            const int row0 = m0 + 32 * q;
+            const int nr = min(32, t->M - row0);
+            const long long ldf = 2LL * t->ldc;
+            // this lane's real column of chunk 0 (real column = 2 * complex column + (re, im))
+            float *cl = reinterpret_cast<float *>(t->C + (long long)row0 * t->ldc) + n0r + lane;
+            const int cf0 = n0r + lane;
+            auto load_c = [&](float(&cv)[32], int ch) {
+                const bool colok = ((cf0 + 32 * ch) >> 1) < t->N;
+#pragma unroll
+                for (int r = 0; r < 32; r++) cv[r] = (colok && r < nr) ? cl[r * ldf + 32 * ch] : 0.f;
+            };
+            float ca[32], cb[32];
+            load_c(ca, 0);
+            load_c(cb, 1);
+            // f16 mode: the row scales of the quarter's 32 rows in the transpose
+            // buffer's spare column (read back as warp broadcasts)
+            if constexpr (F16) tb[lane * 33 + 32] = lane < nr ? t->sa[row0 + lane] : 0.f;
             const bool got = mbar_wait(&tfull[b], use & 1u);
             if (!__all_sync(0xffffffffu, got)) { atomicCAS(err, 0, 3); break; }   // warp-uniform: tcgen05.ld below
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * TC_BNR);
-            const int row0 = m0 + 32 * q;
-#pragma unroll 1
-            for (int ch = 0; ch < TC_BNR / 32; ch++) {
+            auto emit = [&](const float(&cv)[32], int ch) {
                 uint32_t v[32];
                 TMEM_LD32(taddr + ch * 32, v);
                 asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
                 for (int i = 0; i < 32; i++) tb[lane * 33 + i] = __uint_as_float(v[i]);
-                __syncwarp();
-                const int cf = n0r + ch * 32 + lane;          // real column = 2 * complex column + (re, im)
-                const int nr = min(32, t->M - row0);
+                __syncwarp();   // also orders the row scales written before the first chunk
+                const int cf = cf0 + 32 * ch;
                 if ((cf >> 1) < t->N) {
-                    // all 32 row loads in flight before the first store
-                    float *cp = reinterpret_cast<float *>(t->C + (long long)row0 * t->ldc) + cf;
-                    const long long ldf = 2LL * t->ldc;
-                    float cv[32];
-#pragma unroll
-                    for (int r = 0; r < 32; r++) cv[r] = r < nr ? cp[r * ldf] : 0.f;
+                    float *cp = cl + 32 * ch;
                     if constexpr (F16) {
                         // undo the row and column scales (powers of two: exact)
                         const float sbj = t->sb[cf >> 1];
-                        const float *sar = t->sa + row0;
 #pragma unroll
                         for (int r = 0; r < 32; r++)
-                            if (r < nr) cp[r * ldf] = cv[r] - tb[r * 33 + lane] * (sar[r] * sbj);
+                            if (r < nr) cp[r * ldf] = cv[r] - tb[r * 33 + lane] * (tb[r * 33 + 32] * sbj);
                     } else {
 #pragma unroll
                         for (int r = 0; r < 32; r++)
@@ -476,6 +486,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     }
                 }
                 __syncwarp();
+            };
+#pragma unroll 1
+            for (int ch = 0; ch < TC_BNR / 32; ch += 2) {
+                emit(ca, ch);
+                if (ch + 2 < TC_BNR / 32) load_c(ca, ch + 2);
+                emit(cb, ch + 1);
+                if (ch + 3 < TC_BNR / 32) load_c(cb, ch + 3);
             }
             // accumulator b may be overwritten by the tile after next
             asm volatile("tcgen05.fence::before_thread_sync;");
