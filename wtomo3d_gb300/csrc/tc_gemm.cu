@@ -24,14 +24,16 @@
 // half the operand bytes per K step; the epilogue multiplies each accumulator
 // entry by 1/(s_row s_col) (exact: powers of two).
 //
-// Kernel structure (one 128 x 128-complex output tile per CTA, 6 warps):
+// Kernel structure (one 128 x 128-complex output tile per CTA, 10 warps):
 //   warp 0      TMA producer (cp.async.bulk.tensor, SWIZZLE_128B tiles) and
 //               TMEM allocator;
-//   warp 1      single-thread tcgen05.mma issuer (kind::tf32, M=128, N=256),
-//               tcgen05.commit releases smem stages and signals the epilogue;
-//   warps 2..5  epilogue: tcgen05.ld of the 128 x 256 FP32 accumulator,
-//               staged through shared memory, C -= D with coalesced
-//               256-byte warp accesses.
+//   warp 1      single-thread tcgen05.mma issuer (kind::f16 or kind::tf32,
+//               M=128, N=256), tcgen05.commit releases smem stages and
+//               signals the epilogue;
+//   warps 2..9  epilogue (two warps per TMEM lane quarter, half of the
+//               columns each): tcgen05.ld of the 128 x 256 FP32 accumulator,
+//               staged through shared memory, C -= D with coalesced 128-byte
+//               warp accesses.
 // Every mbarrier wait has an iteration limit; on expiry the kernel records an
 // error code, skips ahead, frees its TMEM and returns.
 #include <cuda.h>
@@ -51,9 +53,11 @@ constexpr int TC_STAGES = 2;
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 4;     // 16 KB
 constexpr int TC_B_BYTES = TC_BNR * TC_BK * 4;    // 32 KB
 constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;
-constexpr int TC_EPI_BYTES = 4 * 32 * 33 * 4;        // per epilogue warp a 32 x 33 float transpose buffer
+constexpr int TC_EPI_WARPS = 8;            // two per TMEM lane quarter, each half of the columns
+constexpr int TC_EPI_BYTES = TC_EPI_WARPS * 32 * 33 * 4;   // per epilogue warp a 32 x 33 float transpose buffer
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256 + TC_EPI_BYTES;
-constexpr int TC_THREADS = 192;
+static_assert(TC_SMEM <= 232448, "shared memory per CTA");
+constexpr int TC_THREADS = 64 + 32 * TC_EPI_WARPS;
 constexpr int TC_GROUP = 8;                 // column panels per rasterisation group
 
 // ---------------------------------------------------------------------------
@@ -327,7 +331,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(&tfull[b], 1);
-            mbar_init(&tempty[b], 4);
+            mbar_init(&tempty[b], TC_EPI_WARPS);
         }
         mbar_init(drain, 1);
         asm volatile("fence.mbarrier_init.release.cluster;");
@@ -421,16 +425,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // chunk ahead of its stores (64 row segments in flight per warp).
         // Each lane also prefetches its row of the CTA's next C tile into L2
         // (128-byte lines, none outside the row's own span).
-        const int q = warp & 3;
+        // Warps 2-5 take the first half of the tile's columns (chunks 0-3),
+        // warps 6-9 the second; warp w serves TMEM lane quarter w mod 4.
+        constexpr int NCH = TC_BNR / 32 / 2;    // chunks per epilogue warp
+        const int q = warp & 3, ch0 = NCH * ((warp - 2) >> 2);
         float *tb = epi + (warp - 2) * (32 * 33);
         auto prefetch_c = [&](long long g) {
             if (g >= ntiles) return;
             int pm0, pn0r;
             const TcTask *pt = tc_tile(tasks, ntasks, g, pm0, pn0r);
-            const int r = pm0 + 32 * q + lane, c0 = pn0r >> 1;
+            const int r = pm0 + 32 * q + lane, c0 = (pn0r >> 1) + 16 * ch0;
             if (r >= pt->M || c0 >= pt->N) return;
             const char *p = reinterpret_cast<const char *>(pt->C + (long long)r * pt->ldc + c0);
-            const int nb = 8 * min(TC_BNR / 2, pt->N - c0);
+            const int nb = 8 * min(16 * NCH, pt->N - c0);
             for (int off = 0; off < nb; off += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + off));
             asm volatile("prefetch.global.L2 [%0];" ::"l"(p + nb - 1));
         };
@@ -454,8 +461,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 for (int r = 0; r < 32; r++) cv[r] = (colok && r < nr) ? cl[r * ldf + 32 * ch] : 0.f;
             };
             float ca[32], cb[32];
-            load_c(ca, 0);
-            load_c(cb, 1);
+            load_c(ca, ch0);
+            load_c(cb, ch0 + 1);
             // f16 mode: the row scales of the quarter's 32 rows in the transpose
             // buffer's spare column (read back as warp broadcasts)
             if constexpr (F16) tb[lane * 33 + 32] = lane < nr ? t->sa[row0 + lane] : 0.f;
@@ -488,11 +495,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 __syncwarp();
             };
 #pragma unroll 1
-            for (int ch = 0; ch < TC_BNR / 32; ch += 2) {
+            for (int ch = ch0; ch < ch0 + NCH; ch += 2) {
                 emit(ca, ch);
-                if (ch + 2 < TC_BNR / 32) load_c(ca, ch + 2);
+                if (ch + 2 < ch0 + NCH) load_c(ca, ch + 2);
                 emit(cb, ch + 1);
-                if (ch + 3 < TC_BNR / 32) load_c(cb, ch + 3);
+                if (ch + 3 < ch0 + NCH) load_c(cb, ch + 3);
             }
             // accumulator b may be overwritten by the tile after next
             asm volatile("tcgen05.fence::before_thread_sync;");

@@ -133,6 +133,8 @@ struct TsStage {
     const TsTask *t;
     long long u;
     int m0, k0, k1, nsub, i;
+    int M;       // the task's row count and conjugation, kept in registers
+    bool conj;
     bool valid;
 };
 
@@ -145,6 +147,8 @@ __device__ __forceinline__ void ts_stage_at(TsStage &c, const TsTask *__restrict
     c.t = ts_unit(tasks, ntasks, u, c.m0, c.k0, c.k1);
     c.nsub = (c.k1 - c.k0 + TS_KC - 1) / TS_KC;
     c.i = 0;
+    c.M = c.t->M;
+    c.conj = c.t->conjA != 0;
 }
 
 __device__ __forceinline__ void ts_stage_next(TsStage &c, const TsTask *__restrict__ tasks, int ntasks,
@@ -192,11 +196,15 @@ __device__ __forceinline__ void ts_copy(const TsStage &c, int l, uint32_t raw)
     }
 }
 
-// hi = TF32 rounding of x (to nearest), lo = TF32 rounding of x - hi
+// hi = TF32 rounding of x (to nearest, ties away from zero), lo = the same
+// rounding of x - hi (exact in FP32), so x = hi + lo to ~2^-22 |x|.  The
+// rounding is done on the bit pattern (add half a TF32 unit to the magnitude,
+// clear the 13 low bits) on the integer pipe; finite inputs only.
+__device__ __forceinline__ uint32_t rna_tf32_bits(uint32_t u) { return (u + 0x1000u) & 0xFFFFE000u; }
 __device__ __forceinline__ void split_cvt(float x, uint32_t &hi, uint32_t &lo)
 {
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(x - __uint_as_float(hi)));
+    hi = rna_tf32_bits(__float_as_uint(x));
+    lo = rna_tf32_bits(__float_as_uint(x - __uint_as_float(hi)));
 }
 
 // The loader thread's part of a stage: tile row r = 32 (w mod 4) + lane,
@@ -207,14 +215,14 @@ __device__ __forceinline__ void ts_convert(const TsStage &c, const uint8_t *rs, 
                                            int r, int kpart)
 {
     const int kbase = c.k0 + c.i * TS_KC + 4 * kpart;
-    const bool rv = c.m0 + r < c.t->M;
+    const bool rv = c.m0 + r < c.M;
     float v[8];
     const float4 a = rv ? *reinterpret_cast<const float4 *>(rs + r * 128 + (((2 * kpart) ^ (r & 7)) << 4))
                         : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 b = rv ? *reinterpret_cast<const float4 *>(rs + r * 128 + (((2 * kpart + 1) ^ (r & 7)) << 4))
                         : make_float4(0.f, 0.f, 0.f, 0.f);
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-    const float ys = c.t->conjA ? -1.f : 1.f;
+    const float ys = c.conj ? -1.f : 1.f;
     uint32_t h[8], lw[8];
 #pragma unroll
     for (int j = 0; j < 4; j++) {
