@@ -430,21 +430,23 @@ __device__ __forceinline__ void cp_async_wait_all()
 }
 
 // ---------------------------------------------------------------------------
-// complex64 band solves by substitution with the band's vector in registers,
-// one column (row band) or one row (column band) per thread.  Right-looking:
-// once an unknown is final, its multiples are subtracted from all later ones,
-// which are independent of each other, so the multiply-adds run as independent
-// chains instead of one dependent recurrence.  The 64 unknowns are taken in two
-// halves of 32 so that a thread never holds more than 32 complex values (a
-// 64-value vector plus the hoisted tile entries does not fit the register
-// file); the first half is parked in shared memory, in the thread's own column
-// (row), while the second half is updated with it.  The KB x KB tile is padded
-// with the identity beyond kb (a last, narrower panel), so every loop is
-// fixed-length and unrolls completely.
+// complex64 band solves by substitution, one column (row band) or one row
+// (column band) per thread, in eight groups of eight unknowns.  For group G
+// the thread solves its eight unknowns in registers with the diagonal 8 x 8
+// block of the tile, writes them back to its own column (row) in shared
+// memory, and then subtracts their multiples from every later group H, one
+// 8 x 8 block of the tile at a time (the tile's rows are read as 16-byte
+// broadcasts).  The loops over G and H are not unrolled, so the kernel's code
+// stays small: fully unrolled, the 2,016 multiply-adds of a 64-vector are
+// some 12k instructions per thread, and the warps then wait on instruction
+// fetch (ncu: 1.7 cycles per issue stalled on no_instruction, 24 % issue
+// activity).  The tile is padded with the identity beyond kb (a last,
+// narrower panel).
 // ---------------------------------------------------------------------------
-constexpr int HB = KB / 2;
-__host__ __device__ constexpr size_t band_row_smem() { return sizeof(cx<float>) * (KB * (KB + 1) + KB * (TRW + 1)); }
-__host__ __device__ constexpr size_t band_col_smem() { return sizeof(cx<float>) * (KB * (KB + 1) + TCR * (KB + 1)); }
+constexpr int TG = 8;                       // unknowns per group
+constexpr int LDT = KB + 2;                 // tile row stride: 16-byte-aligned rows
+__host__ __device__ constexpr size_t band_row_smem() { return sizeof(cx<float>) * (KB * LDT + KB * (TRW + 1)); }
+__host__ __device__ constexpr size_t band_col_smem() { return sizeof(cx<float>) * (KB * LDT + TCR * (KB + 1)); }
 
 __device__ __forceinline__ void cfms(cx<float> &d, const cx<float> a, const cx<float> b)   // d -= a b
 {
@@ -452,13 +454,35 @@ __device__ __forceinline__ void cfms(cx<float> &d, const cx<float> a, const cx<f
     d.im = fmaf(-a.re, b.im, fmaf(-a.im, b.re, d.im));
 }
 
+// eight consecutive complex values of a 16-byte-aligned shared-memory row
+__device__ __forceinline__ void lds8(const cx<float> *p, cx<float> (&a)[TG])
+{
+#pragma unroll
+    for (int j = 0; j < TG; j += 2) {
+        const float4 u = reinterpret_cast<const float4 *>(p)[j / 2];
+        a[j] = cx<float>(u.x, u.y);
+        a[j + 1] = cx<float>(u.z, u.w);
+    }
+}
+
+// the KB x KB diagonal tile into shared memory (row stride LDT), identity
+// beyond kb
+__device__ __forceinline__ void load_tile_padded(cx<float> *T, const cx<float> *D, long long nf, int kb)
+{
+    for (int q = threadIdx.x; q < KB * KB; q += blockDim.x) {
+        const int i = q / KB, j = q % KB;
+        if (i < kb && j < kb) cp_async_cx(T + i * LDT + j, D + (long long)i * nf + j);
+        else T[i * LDT + j] = cx<float>(i == j ? 1.f : 0.f, 0.f);
+    }
+}
+
 template <int UNUSED = 0>
 __global__ void __launch_bounds__(TRW) k_trsm_row_h(const RowTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
                                                     cx<float> *__restrict__ fac, const int *__restrict__ pord)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    cx<float> *L = reinterpret_cast<cx<float> *>(smraw);   // KB x (KB+1)
-    cx<float> *Bt = L + KB * (KB + 1);                    // KB x (TRW+1): band rows as stored
+    cx<float> *L = reinterpret_cast<cx<float> *>(smraw);   // KB x LDT
+    cx<float> *Bt = L + KB * LDT;                         // KB x (TRW+1): band rows as stored
     __shared__ int idx[KB];
     const RowTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
@@ -466,11 +490,7 @@ __global__ void __launch_bounds__(TRW) k_trsm_row_h(const RowTask *__restrict__ 
     const int c0 = t.c0, nc = min(TRW, nf - c0);
     const int tid = threadIdx.x;
     cx<float> *base = fac + F.fac + (long long)k * nf;
-    for (int q = tid; q < KB * KB; q += blockDim.x) {
-        const int i = q / KB, j = q % KB;
-        if (i < kb && j < kb) cp_async_cx(L + i * (KB + 1) + j, base + (long long)i * nf + k + j);
-        else L[i * (KB + 1) + j] = cx<float>(i == j ? 1.f : 0.f, 0.f);
-    }
+    load_tile_padded(L, base + k, nf, kb);
     for (int q = tid; q < kb * nc; q += blockDim.x) {
         const int i = q / nc, c = q % nc;
         cp_async_cx(Bt + i * (TRW + 1) + c, base + (long long)i * nf + c0 + c);
@@ -479,34 +499,42 @@ __global__ void __launch_bounds__(TRW) k_trsm_row_h(const RowTask *__restrict__ 
     cp_async_wait_all();
     __syncthreads();
     // Row i of the result is kept in the stored slot idx[i] of the row it
-    // came from: the slots of rows not yet read stay untouched.
+    // came from: the slots of rows not yet read stay untouched.  Unknowns at
+    // or beyond kb are zero and stay zero (identity padding).
     if (tid < nc) {
         cx<float> *col = Bt + tid;
-        cx<float> b[HB];
+        const int ng = (kb + TG - 1) / TG;
+#pragma unroll 1
+        for (int G = 0; G < ng; G++) {
+            cx<float> b[TG];
 #pragma unroll
-        for (int i = 0; i < HB; i++) b[i] = i < kb ? col[idx[i] * (TRW + 1)] : cx<float>(0.f, 0.f);
+            for (int i = 0; i < TG; i++) b[i] = TG * G + i < kb ? col[idx[TG * G + i] * (TRW + 1)] : cx<float>(0.f, 0.f);
 #pragma unroll
-        for (int l = 0; l < HB - 1; l++)
+            for (int i = 1; i < TG; i++) {
+                cx<float> lr[TG];
+                lds8(L + (TG * G + i) * LDT + TG * G, lr);
 #pragma unroll
-            for (int i = l + 1; i < HB; i++) cfms(b[i], L[i * (KB + 1) + l], b[l]);
+                for (int l = 0; l < i; l++) cfms(b[i], lr[l], b[l]);
+            }
 #pragma unroll
-        for (int i = 0; i < HB; i++)
-            if (i < kb) col[idx[i] * (TRW + 1)] = b[i];
+            for (int i = 0; i < TG; i++)
+                if (TG * G + i < kb) col[idx[TG * G + i] * (TRW + 1)] = b[i];
+#pragma unroll 1
+            for (int H = G + 1; H < ng; H++) {
 #pragma unroll
-        for (int i = 0; i < HB; i++) b[i] = HB + i < kb ? col[idx[HB + i] * (TRW + 1)] : cx<float>(0.f, 0.f);
-#pragma unroll 4
-        for (int l = 0; l < HB; l++) {
-            const cx<float> xl = l < kb ? col[idx[l] * (TRW + 1)] : cx<float>(0.f, 0.f);
+                for (int i = 0; i < TG; i++) {
+                    const int row = TG * H + i;
+                    if (row < kb) {
+                        cx<float> lr[TG];
+                        lds8(L + row * LDT + TG * G, lr);
+                        cx<float> c = col[idx[row] * (TRW + 1)];
 #pragma unroll
-            for (int i = 0; i < HB; i++) cfms(b[i], L[(HB + i) * (KB + 1) + l], xl);
+                        for (int l = 0; l < TG; l++) cfms(c, lr[l], b[l]);
+                        col[idx[row] * (TRW + 1)] = c;
+                    }
+                }
+            }
         }
-#pragma unroll
-        for (int l = 0; l < HB - 1; l++)
-#pragma unroll
-            for (int i = l + 1; i < HB; i++) cfms(b[i], L[(HB + i) * (KB + 1) + HB + l], b[l]);
-#pragma unroll
-        for (int i = 0; i < HB; i++)
-            if (HB + i < kb) col[idx[HB + i] * (TRW + 1)] = b[i];
     }
     __syncthreads();
     for (int q = tid; q < kb * nc; q += blockDim.x) {
@@ -520,19 +548,14 @@ __global__ void __launch_bounds__(TCR) k_trsm_col_h(const ColTask *__restrict__ 
                                                     cx<float> *__restrict__ fac)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    cx<float> *U = reinterpret_cast<cx<float> *>(smraw);   // KB x (KB+1)
-    cx<float> *Xs = U + KB * (KB + 1);                    // TCR x (KB+1)
+    cx<float> *U = reinterpret_cast<cx<float> *>(smraw);   // KB x LDT
+    cx<float> *Xs = U + KB * LDT;                         // TCR x (KB+1)
     __shared__ cx<float> invd[KB];
     const ColTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
     const int nf = F.p + F.b, k = t.k, kb = min(KB, F.p - k);
     const int tid = threadIdx.x;
-    const cx<float> *D = fac + F.fac + (long long)k * nf + k;
-    for (int q = tid; q < KB * KB; q += blockDim.x) {
-        const int i = q / KB, j = q % KB;
-        if (i < kb && j < kb) cp_async_cx(U + i * (KB + 1) + j, D + (long long)i * nf + j);
-        else U[i * (KB + 1) + j] = cx<float>(i == j ? 1.f : 0.f, 0.f);
-    }
+    load_tile_padded(U, fac + F.fac + (long long)k * nf + k, nf, kb);
     cx<float> *xb;
     long long ld;
     int nr;
@@ -551,37 +574,44 @@ __global__ void __launch_bounds__(TCR) k_trsm_col_h(const ColTask *__restrict__ 
     }
     cp_async_wait_all();
     __syncthreads();
-    for (int j = tid; j < KB; j += blockDim.x) invd[j] = cdiv(cx<float>(1.f, 0.f), U[j * (KB + 1) + j]);
+    for (int j = tid; j < KB; j += blockDim.x) invd[j] = cdiv(cx<float>(1.f, 0.f), U[j * LDT + j]);
     __syncthreads();
     if (tid < nr) {
         cx<float> *row = Xs + tid * (KB + 1);
-        cx<float> x[HB];
+        const int ng = (kb + TG - 1) / TG;
+#pragma unroll 1
+        for (int G = 0; G < ng; G++) {
+            cx<float> x[TG];
 #pragma unroll
-        for (int j = 0; j < HB; j++) x[j] = j < kb ? row[j] : cx<float>(0.f, 0.f);
+            for (int j = 0; j < TG; j++) x[j] = TG * G + j < kb ? row[TG * G + j] : cx<float>(0.f, 0.f);
 #pragma unroll
-        for (int j = 0; j < HB; j++) {
-            x[j] = x[j] * invd[j];
+            for (int j = 0; j < TG; j++) {
+                x[j] = x[j] * invd[TG * G + j];
+                cx<float> ur[TG];
+                lds8(U + (TG * G + j) * LDT + TG * G, ur);
 #pragma unroll
-            for (int j2 = j + 1; j2 < HB; j2++) cfms(x[j2], x[j], U[j * (KB + 1) + j2]);
+                for (int j2 = j + 1; j2 < TG; j2++) cfms(x[j2], x[j], ur[j2]);
+            }
+#pragma unroll
+            for (int j = 0; j < TG; j++)
+                if (TG * G + j < kb) row[TG * G + j] = x[j];
+#pragma unroll 1
+            for (int H = G + 1; H < ng; H++) {
+                cx<float> y[TG];
+#pragma unroll
+                for (int j = 0; j < TG; j++) y[j] = TG * H + j < kb ? row[TG * H + j] : cx<float>(0.f, 0.f);
+#pragma unroll
+                for (int l = 0; l < TG; l++) {
+                    cx<float> ur[TG];
+                    lds8(U + (TG * G + l) * LDT + TG * H, ur);
+#pragma unroll
+                    for (int j = 0; j < TG; j++) cfms(y[j], x[l], ur[j]);
+                }
+#pragma unroll
+                for (int j = 0; j < TG; j++)
+                    if (TG * H + j < kb) row[TG * H + j] = y[j];
+            }
         }
-#pragma unroll
-        for (int j = 0; j < HB; j++) row[j] = x[j];
-#pragma unroll
-        for (int j = 0; j < HB; j++) x[j] = HB + j < kb ? row[HB + j] : cx<float>(0.f, 0.f);
-#pragma unroll 4
-        for (int l = 0; l < HB; l++) {
-            const cx<float> xl = row[l];
-#pragma unroll
-            for (int j = 0; j < HB; j++) cfms(x[j], xl, U[l * (KB + 1) + HB + j]);
-        }
-#pragma unroll
-        for (int j = 0; j < HB; j++) {
-            x[j] = x[j] * invd[HB + j];
-#pragma unroll
-            for (int j2 = j + 1; j2 < HB; j2++) cfms(x[j2], x[j], U[(HB + j) * (KB + 1) + HB + j2]);
-        }
-#pragma unroll
-        for (int j = 0; j < HB; j++) row[HB + j] = x[j];
     }
     __syncthreads();
     for (int q = tid; q < nr * kb; q += blockDim.x) {

@@ -208,28 +208,34 @@ __device__ __forceinline__ void split_cvt(float x, uint32_t &hi, uint32_t &lo)
 }
 
 // The loader thread's part of a stage: tile row r = 32 (w mod 4) + lane,
-// complex k 4 (w / 4) .. + 3, read from the raw slot, conjugated for A^H,
-// zero outside the operand, split and stored into TMEM columns col_hi + 0..7
-// (hi) and col_hi + 32 + 0..7 (lo) of the thread's lane.
+// complex k 4 (w / 4) .. + 3, read from the raw slot, split and stored into
+// TMEM columns col_hi + 0..7 (hi) and col_hi + 32 + 0..7 (lo) of the thread's
+// lane.  COPY (the cp.async variant): the raw slot holds stale values outside
+// the operand, which are zeroed, and A^H is conjugated.  The TMA variant needs
+// neither: TMA fills outside the tensor with zeros and serves only blocks as
+// stored.
+template <bool COPY>
 __device__ __forceinline__ void ts_convert(const TsStage &c, const uint8_t *rs, uint32_t tmem_lane, int col_hi,
                                            int r, int kpart)
 {
-    const int kbase = c.k0 + c.i * TS_KC + 4 * kpart;
-    const bool rv = c.m0 + r < c.M;
-    float v[8];
-    const float4 a = rv ? *reinterpret_cast<const float4 *>(rs + r * 128 + (((2 * kpart) ^ (r & 7)) << 4))
-                        : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 b = rv ? *reinterpret_cast<const float4 *>(rs + r * 128 + (((2 * kpart + 1) ^ (r & 7)) << 4))
-                        : make_float4(0.f, 0.f, 0.f, 0.f);
-    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-    const float ys = c.conj ? -1.f : 1.f;
-    uint32_t h[8], lw[8];
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-        const bool kv = kbase + j < c.k1;
-        split_cvt(kv ? v[2 * j] : 0.f, h[2 * j], lw[2 * j]);
-        split_cvt(kv ? ys * v[2 * j + 1] : 0.f, h[2 * j + 1], lw[2 * j + 1]);
+    float4 a = *reinterpret_cast<const float4 *>(rs + r * 128 + (((2 * kpart) ^ (r & 7)) << 4));
+    float4 b = *reinterpret_cast<const float4 *>(rs + r * 128 + (((2 * kpart + 1) ^ (r & 7)) << 4));
+    if constexpr (COPY) {
+        const int kbase = c.k0 + c.i * TS_KC + 4 * kpart;
+        if (c.m0 + r >= c.M || kbase + 3 >= c.k1) {   // the operand's last rows or columns
+            const bool rv = c.m0 + r < c.M;
+            const bool k0v = rv && kbase < c.k1, k1v = rv && kbase + 1 < c.k1, k2v = rv && kbase + 2 < c.k1,
+                       k3v = rv && kbase + 3 < c.k1;
+            a = make_float4(k0v ? a.x : 0.f, k0v ? a.y : 0.f, k1v ? a.z : 0.f, k1v ? a.w : 0.f);
+            b = make_float4(k2v ? b.x : 0.f, k2v ? b.y : 0.f, k3v ? b.z : 0.f, k3v ? b.w : 0.f);
+        }
+        if (c.conj) {
+            a.y = -a.y; a.w = -a.w; b.y = -b.y; b.w = -b.w;
+        }
     }
+    uint32_t h[8], lw[8];
+    split_cvt(a.x, h[0], lw[0]); split_cvt(a.y, h[1], lw[1]); split_cvt(a.z, h[2], lw[2]); split_cvt(a.w, h[3], lw[3]);
+    split_cvt(b.x, h[4], lw[4]); split_cvt(b.y, h[5], lw[5]); split_cvt(b.z, h[6], lw[6]); split_cvt(b.w, h[7], lw[7]);
     const uint32_t th = tmem_lane + (uint32_t)col_hi, tl = th + 32;
     asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(th),
                  "r"(h[0]), "r"(h[1]), "r"(h[2]), "r"(h[3]), "r"(h[4]), "r"(h[5]), "r"(h[6]), "r"(h[7])
@@ -347,7 +353,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
             ok = __all_sync(0xffffffffu, ok);   // the tcgen05 stores below are warp-collective
             if (ok) {
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                ts_convert(cs, rawb + slot * TS_RAW_BYTES, tlane, TS_ACC_COLS + 64 * s + 8 * kpart, r, kpart);
+                ts_convert<!TMA>(cs, rawb + slot * TS_RAW_BYTES, tlane, TS_ACC_COLS + 64 * s + 8 * kpart, r, kpart);
                 asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;");
             }
