@@ -244,7 +244,9 @@ def run_ours(args, rank, world, mixed_solutions):
     d2h = Xh[0].numel() * 16
 
     # ---- (ii) resident-factor rate: each lane's last factorisation stays
-    # resident and its right-hand sides are solved again, alone on the GPU ----
+    # resident and its right-hand sides are solved again, alone on the GPU
+    # (with every SM: the reserve only serves overlapped lanes) ----
+    wt.set_sm_reserve(0)
     resident = []
     for l in sorted(last_f):
         torch.cuda.synchronize()

@@ -208,7 +208,6 @@ __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tas
     const T thresh = (T)(pivot_rel * sqrt(__longlong_as_double((long long)*amax2)));
     extern __shared__ __align__(16) unsigned char smraw[];
     cx<T> *S = reinterpret_cast<cx<T> *>(smraw);   // KB x (KB+1), then 2 KB scratch columns
-    __shared__ int s_piv;
     __shared__ int prow[KB];   // stored row at each position, as the interchanges go
     const PanelTask t = tasks[blockIdx.x];
     const FrontDev F = fr[t.f];
@@ -223,6 +222,11 @@ __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tas
     }
     if (tid < KB) prow[tid] = tid;
     __syncthreads();
+    // Column j: warp 0 finds the pivot, swaps the two rows, applies the
+    // static-pivot threshold and scales the column below the diagonal (one
+    // block barrier); then all threads update the trailing block, thread
+    // (tid / 16, tid % 16) taking every 16th row and column (a second one).
+    const int ty = tid >> 4, tx = tid & 15;
     for (int j = 0; j < kb; j++) {
         if (tid < 32) {
             T best = -1; int bi = j;
@@ -230,44 +234,40 @@ __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tas
                 T v = cabs2(S[i * LD + j]);
                 if (v > best) { best = v; bi = i; }
             }
-            for (int o = 16; o > 0; o >>= 1) {
+            for (int o = 16; o > 0; o >>= 1) {   // every lane ends with the same (best, bi)
                 T ov = __shfl_xor_sync(0xffffffffu, best, o);
                 int oi = __shfl_xor_sync(0xffffffffu, bi, o);
                 if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
             }
-            if (tid == 0) s_piv = bi;
+            const int pv = bi;
+            if (pv != j)
+                for (int c = tid; c < kb; c += 32) {
+                    cx<T> a = S[j * LD + c];
+                    S[j * LD + c] = S[pv * LD + c];
+                    S[pv * LD + c] = a;
+                }
+            __syncwarp();
+            if (tid == 0) {
+                ipiv[F.first + k + j] = k + pv;
+                const int a = prow[j];
+                prow[j] = prow[pv];
+                prow[pv] = a;
+                cx<T> d = S[j * LD + j];
+                T m2 = cabs2(d);
+                if (!(m2 >= thresh * thresh)) {   // also catches NaN
+                    T m = sqrt(m2);
+                    S[j * LD + j] = (m > 0 && m == m) ? d * (thresh / m) : cx<T>(thresh);
+                    atomicAdd(npert, 1);
+                }
+            }
+            __syncwarp();
+            const cx<T> inv = cdiv(cx<T>(1), S[j * LD + j]);
+            for (int i = j + 1 + tid; i < kb; i += 32) S[i * LD + j] = S[i * LD + j] * inv;
         }
         __syncthreads();
-        const int pv = s_piv;
-        if (pv != j)
-            for (int c = tid; c < kb; c += blockDim.x) {
-                cx<T> a = S[j * LD + c];
-                S[j * LD + c] = S[pv * LD + c];
-                S[pv * LD + c] = a;
-            }
-        __syncthreads();
-        if (tid == 0) {
-            ipiv[F.first + k + j] = k + pv;
-            const int a = prow[j];
-            prow[j] = prow[pv];
-            prow[pv] = a;
-            cx<T> d = S[j * LD + j];
-            T m2 = cabs2(d);
-            if (!(m2 >= thresh * thresh)) {   // also catches NaN
-                T m = sqrt(m2);
-                S[j * LD + j] = (m > 0 && m == m) ? d * (thresh / m) : cx<T>(thresh);
-                atomicAdd(npert, 1);
-            }
-        }
-        __syncthreads();
-        const cx<T> d = S[j * LD + j];
-        const cx<T> inv = cdiv(cx<T>(1), d);
-        for (int i = j + 1 + tid; i < kb; i += blockDim.x) S[i * LD + j] = S[i * LD + j] * inv;
-        __syncthreads();
-        const int rem = kb - j - 1;
-        for (int idx = tid; idx < rem * rem; idx += blockDim.x) {
-            int i = j + 1 + idx / rem, c = j + 1 + idx % rem;
-            S[i * LD + c] = S[i * LD + c] - S[i * LD + j] * S[j * LD + c];
+        for (int i = j + 1 + ty; i < kb; i += 16) {
+            const cx<T> l = S[i * LD + j];
+            for (int c = j + 1 + tx; c < kb; c += 16) S[i * LD + c] = S[i * LD + c] - l * S[j * LD + c];
         }
         __syncthreads();
     }
@@ -830,7 +830,7 @@ __global__ void __launch_bounds__(256, 2) k_gemm_ts(const GemmTask<T> *__restric
 // role-0 CTA leaves Z in the front's scratch slot; the next step's role-0 CTA
 // (or a flush) writes it into X once no CTA reads those rows any more.
 // ---------------------------------------------------------------------------
-constexpr int SUB_RB = 64;   // rows per update CTA
+constexpr int SUB_RB = 32;   // rows per update CTA
 
 // Shared-memory layout of k_sub_step (complex elements).
 __host__ __device__ constexpr int sub_step_smem_elems()
@@ -853,7 +853,19 @@ __device__ __forceinline__ void lds4(const cx<double> *p, cx<double> (&a)[4])
     }
 }
 
-constexpr int SUB_THREADS = 512;   // 16 warps: each thread sums 4 rows of Z and 4 update rows
+// two consecutive complex values from 16-byte-aligned shared memory
+__device__ __forceinline__ void lds2(const cx<float> *p, cx<float> (&a)[2])
+{
+    const float4 u = reinterpret_cast<const float4 *>(p)[0];
+    a[0] = cx<float>(u.x, u.y); a[1] = cx<float>(u.z, u.w);
+}
+__device__ __forceinline__ void lds2(const cx<double> *p, cx<double> (&a)[2])
+{
+    const double2 u = reinterpret_cast<const double2 *>(p)[0], v = reinterpret_cast<const double2 *>(p)[1];
+    a[0] = cx<double>(u.x, u.y); a[1] = cx<double>(v.x, v.y);
+}
+
+constexpr int SUB_THREADS = 512;   // 16 warps: each thread sums 4 rows of Z and 2 update rows
 template <class T>
 __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__restrict__ tasks, const FrontDev *__restrict__ fr,
                                                   const cx<T> *__restrict__ fac, const cx<T> *__restrict__ inv,
@@ -933,8 +945,8 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
     // Z = M y: thread (lane c, warp w) owns rows 4w .. 4w+3 of column c; the
     // l loop runs outside, so its sums are independent chains (M entries are
     // warp broadcasts, two 16-byte loads per l for complex64)
-    constexpr int NW = SUB_THREADS / 32, RPT = KB / NW;
-    static_assert(RPT == 4 && SUB_RB / NW == 4, "four rows per thread");
+    constexpr int NW = SUB_THREADS / 32, RPT = KB / NW, UPT = SUB_RB / NW;
+    static_assert(RPT == 4 && UPT == 2, "four rows of Z, two update rows per thread");
     const int c = tid & 31, w = tid >> 5, i0 = RPT * w;
     cx<T> acc[RPT];
 #pragma unroll
@@ -968,21 +980,22 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
         }
         return;
     }
-    // rows 4w .. 4w+3 of column c, independent sums as above
+    // update rows 2w, 2w+1 of column c, independent sums as above
     if (c < m) {
-        cx<T> u[RPT];
+        const int u0 = UPT * w;
+        cx<T> u[UPT];
 #pragma unroll
-        for (int j = 0; j < RPT; j++) u[j] = cx<T>(0);
+        for (int j = 0; j < UPT; j++) u[j] = cx<T>(0);
         for (int l = 0; l < kb; l++) {
             const cx<T> z = Ys[l * LY + c];
-            cx<T> a[4];
-            lds4(As + l * SUB_RB + i0, a);
+            cx<T> a[UPT];
+            lds2(As + l * SUB_RB + u0, a);
 #pragma unroll
-            for (int j = 0; j < RPT; j++) u[j] = u[j] + (herm ? conj(a[j]) : a[j]) * z;
+            for (int j = 0; j < UPT; j++) u[j] = u[j] + (herm ? conj(a[j]) : a[j]) * z;
         }
 #pragma unroll
-        for (int j = 0; j < RPT; j++) {
-            const int r = i0 + j;
+        for (int j = 0; j < UPT; j++) {
+            const int r = u0 + j;
             if (r < nr) Y[(long long)(t.r0 + r) * ldx + c] = Yr[r * LY + c] - u[j];
         }
     }
