@@ -346,7 +346,8 @@ struct wt3d_solver {
     DevVec<double> norms;
     DevVec<double> gscr;                  // per-row derivative records of the gradient
     DevVec<double2> batF, batX;           // caller batch buffers (wt3d_batch_buffers)
-    DevVec<double2> gmV, gmZ, gmH;        // flexible GMRES: Krylov basis, preconditioned basis, projections
+    StreamBuf<double2> gmV, gmZ;          // flexible GMRES: Krylov basis, preconditioned basis (per call)
+    DevVec<double2> gmH;                  // flexible GMRES: projections
     DevVec<double2> gmPart;
     DevVec<double> gmNorm, gmScale;
     std::unique_ptr<Engine<float>> e32;
@@ -431,18 +432,20 @@ int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, d
     const long long n = h->n, blk = n * MAXRHS;
     const int kr = gmres_restart();
     int rc;
-    if (!h->gmV.p) {
-        if ((rc = h->gmV.alloc((size_t)blk * (kr + 1))) || (rc = h->gmZ.alloc((size_t)blk * kr)) ||
-            (rc = h->gmH.alloc((size_t)(GM_KMAX + 1) * MAXRHS)) ||
+    if (!h->gmH.p) {
+        if ((rc = h->gmH.alloc((size_t)(GM_KMAX + 1) * MAXRHS)) ||
             (rc = h->gmPart.alloc((size_t)GM_BLOCKS * (GM_KMAX + 1) * MAXRHS)) ||
             (rc = h->gmNorm.alloc(MAXRHS)) || (rc = h->gmScale.alloc(MAXRHS)))
             return rc;
     }
-    // the Krylov bases are released with the call: they are not part of a
-    // handle's resident memory
+    // the Krylov bases live for the call only (they are not part of a
+    // handle's resident memory), in stream order on the handle's solve
+    // stream, so that taking and returning them never waits for work of
+    // other handles
+    if ((rc = h->gmV.alloc((size_t)blk * (kr + 1), st)) || (rc = h->gmZ.alloc((size_t)blk * kr, st))) return rc;
     struct Release {
         wt3d_solver *h;
-        ~Release() { h->gmV.free(); h->gmZ.free(); }
+        ~Release() { h->gmV.release(); h->gmZ.release(); }
     } release{h};
     double2 *V = h->gmV.p, *Z = h->gmZ.p;
     const int th = 256;
@@ -1022,8 +1025,8 @@ int wt3d_set_background(wt3d_solver *h, const float *vp, const float *vs, const 
     const long long nn = h->n / 3;
     int rc;
     if (!h->bgro.p && ((rc = h->bgda.alloc(nn)) || (rc = h->bgmu.alloc(nn)) || (rc = h->bgro.alloc(nn)))) return rc;
-    DevVec<float> dvp, dvs, drho;
-    if ((rc = dvp.alloc(nn)) || (rc = dvs.alloc(nn)) || (rc = drho.alloc(nn))) return rc;
+    StreamBuf<float> dvp, dvs, drho;   // per-call temporaries in stream order (see StreamBuf)
+    if ((rc = dvp.alloc(nn, h->st)) || (rc = dvs.alloc(nn, h->st)) || (rc = drho.alloc(nn, h->st))) return rc;
     WT_CUDA(cudaMemcpyAsync(dvp.p, vp, sizeof(float) * nn, cudaMemcpyHostToDevice, h->st));
     WT_CUDA(cudaMemcpyAsync(dvs.p, vs, sizeof(float) * nn, cudaMemcpyHostToDevice, h->st));
     WT_CUDA(cudaMemcpyAsync(drho.p, rho, sizeof(float) * nn, cudaMemcpyHostToDevice, h->st));
@@ -1071,15 +1074,16 @@ int wt3d_rhs_planewave(wt3d_solver *h, const wt3d_layered1d *m, int nsrc, const 
             kx[j] = h->om_re * p * rx[j];
             ky[j] = h->om_re * p * ry[j];
         }
-        DevVec<double2> dU, dW;
-        DevVec<double> dkx, dky, drx, dry;
+        // per-call tables in stream order (see StreamBuf)
+        StreamBuf<double2> dU, dW;
+        StreamBuf<double> dkx, dky, drx, dry;
         std::vector<double2> hu(Uz.size()), hw(Wz.size());
         for (size_t i = 0; i < Uz.size(); i++) {
             hu[i] = make_double2(Uz[i].real(), Uz[i].imag());
             hw[i] = make_double2(Wz[i].real(), Wz[i].imag());
         }
-        if ((rc = dU.upload(hu)) || (rc = dW.upload(hw)) || (rc = dkx.upload(kx)) || (rc = dky.upload(ky)) ||
-            (rc = drx.upload(rx)) || (rc = dry.upload(ry)))
+        if ((rc = dU.upload(hu, h->st)) || (rc = dW.upload(hw, h->st)) || (rc = dkx.upload(kx, h->st)) ||
+            (rc = dky.upload(ky, h->st)) || (rc = drx.upload(rx, h->st)) || (rc = dry.upload(ry, h->st)))
             return rc;
         k_pw_expand<<<ceil_div((n / 3) * mm, 256), 256, 0, h->st>>>(nx, ny, nz, h->grid.dx, mm, dU.p, dW.p, dkx.p,
                                                                      dky.p, drx.p, dry.p, h->Rn.p, MAXRHS);
@@ -1095,8 +1099,8 @@ int wt3d_rhs_planewave(wt3d_solver *h, const wt3d_layered1d *m, int nsrc, const 
 int wt3d_set_values_c64(wt3d_solver *h, const float _Complex *a)
 {
     if (!h || !a) { set_error("null pointer"); return WT3D_ERR_ARG; }
-    DevVec<float2> tmp;
-    int rc = tmp.alloc(h->nnz);
+    StreamBuf<float2> tmp;   // per-call, in stream order (see StreamBuf)
+    int rc = tmp.alloc(h->nnz, h->st);
     if (rc) return rc;
     WT_CUDA(cudaMemcpyAsync(tmp.p, a, sizeof(float2) * h->nnz, cudaMemcpyHostToDevice, h->st));
     k_c64_to_c128<<<ceil_div(h->nnz, 256), 256, 0, h->st>>>(h->nnz, tmp.p, h->a.p);
@@ -1124,13 +1128,14 @@ static int solve_host(wt3d_solver *h, int nrhs, const double _Complex *B, double
 {
     if (!h || nrhs < 1 || !B || !X) { set_error("wt3d_solve: bad arguments"); return WT3D_ERR_ARG; }
     if (!h->have_factor) { set_error("solve before factor"); return WT3D_ERR_STATE; }
-    DevVec<double2> dB, dX;
+    StreamBuf<double2> dB, dX;   // per-call, in the solve stream's order (see StreamBuf)
     int rc;
-    if ((rc = dB.alloc((size_t)h->n * nrhs)) || (rc = dX.alloc((size_t)h->n * nrhs))) return rc;
+    if ((rc = dB.alloc((size_t)h->n * nrhs, h->sts)) || (rc = dX.alloc((size_t)h->n * nrhs, h->sts))) return rc;
     WT_CUDA(cudaMemcpyAsync(dB.p, B, sizeof(double2) * h->n * nrhs, cudaMemcpyHostToDevice, h->sts));
     rc = solve_dev_cm(h, nrhs, dB.p, dX.p, tol, maxit, relres, iters, adjoint);
     if (rc && rc != WT3D_ERR_NOCONV) return rc;
-    WT_CUDA(cudaMemcpy(X, dX.p, sizeof(double2) * h->n * nrhs, cudaMemcpyDeviceToHost));
+    WT_CUDA(cudaMemcpyAsync(X, dX.p, sizeof(double2) * h->n * nrhs, cudaMemcpyDeviceToHost, h->sts));
+    WT_CUDA(cudaStreamSynchronize(h->sts));
     return rc;
 }
 
@@ -1151,8 +1156,8 @@ int wt3d_apply(wt3d_solver *h, int nrhs, const double _Complex *X, double _Compl
     if (!h || nrhs < 1 || !X || !Y) { set_error("wt3d_apply: bad arguments"); return WT3D_ERR_ARG; }
     if (!h->have_values) { set_error("no operator"); return WT3D_ERR_STATE; }
     const long long n = h->n;
-    DevVec<double2> dX;
-    int rc = dX.alloc((size_t)n * nrhs);
+    StreamBuf<double2> dX;   // per-call, in stream order (see StreamBuf)
+    int rc = dX.alloc((size_t)n * nrhs, h->st);
     if (rc) return rc;
     WT_CUDA(cudaMemcpyAsync(dX.p, X, sizeof(double2) * n * nrhs, cudaMemcpyHostToDevice, h->st));
     for (int c0 = 0; c0 < nrhs; c0 += MAXRHS) {
@@ -1165,9 +1170,9 @@ int wt3d_apply(wt3d_solver *h, int nrhs, const double _Complex *X, double _Compl
                                                h->Rn.p, h->norms.p, h->norms.p + MAXRHS, 0);
         k_rm_to_cm<<<ceil_div(n, 256), 256, 0, h->st>>>(n, m, h->Rn.p, dX.p + (long long)c0 * n);
     }
-    WT_CUDA(cudaStreamSynchronize(h->st));
     std::vector<std::complex<double>> tmp((size_t)n * nrhs);
-    WT_CUDA(cudaMemcpy(tmp.data(), dX.p, sizeof(double2) * n * nrhs, cudaMemcpyDeviceToHost));
+    WT_CUDA(cudaMemcpyAsync(tmp.data(), dX.p, sizeof(double2) * n * nrhs, cudaMemcpyDeviceToHost, h->st));
+    WT_CUDA(cudaStreamSynchronize(h->st));
     std::complex<double> *Yc = reinterpret_cast<std::complex<double> *>(Y);
     for (size_t i = 0; i < tmp.size(); i++) Yc[i] = -tmp[i];
     return WT3D_OK;
