@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
     }
     if (threadIdx.x == TS_WM * 32) {
         for (int s = 0; s < TS_TSTAGES; s++) {
-            mbar_init(&full[s], TS_LOADERS);
+            mbar_init(&full[s], TMA ? TS_LOADERS / 2 : TS_LOADERS);   // the warps that convert a stage
             mbar_init(&empty[s], 1);
         }
         for (int s = 0; s < TS_BSTAGES; s++) {
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
         mbar_init(drain, 1);
         for (int s = 0; s < TS_RAW; s++) {
             mbar_init(&rfull[s], 1);
-            mbar_init(&rempty[s], TS_LOADERS);
+            mbar_init(&rempty[s], TS_LOADERS / 2);
         }
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
@@ -316,14 +316,25 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
         // the loaders read each other's copies, so every stage passes one
         // named barrier of the 512 loader threads; a loader whose wait timed
         // out keeps looping (without converting) so that none is left at it.
+        // TMA variant: warps 0-7 convert the even stages and warps 8-15 the
+        // odd ones, each thread two k parts of its row, so that two stages
+        // are converted at once (one warp's stage is a chain of waits, shared
+        // loads, the split, TMEM stores and their completion).  Copy variant:
+        // all 16 warps every stage (they also copy it), one k part each.
         const int l = threadIdx.x;
-        const int r = 32 * (warp & 3) + lane, kpart = warp >> 2;
+        constexpr int NG = TMA ? 2 : 1, NKP = TMA ? 2 : 1;
+        const int r = 32 * (warp & 3) + lane;
+        const int kpa = TMA ? 2 * ((warp >> 2) & 1) : warp >> 2;   // first k part
         const uint32_t tlane = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
         uint8_t *rawb = smem + TS_RAW_OFF;
         const uint32_t raw0 = smem_u32(rawb);
         TsStage cp, cs;
         ts_stage_at(cs, tasks, ntasks, nunits, blockIdx.x);
         long long g = 0;
+        if (TMA && (warp >> 3) == 1 && cs.valid) {   // the odd stages
+            ts_stage_next(cs, tasks, ntasks, nunits);
+            g = 1;
+        }
         bool ok = true;
         if constexpr (!TMA) {
             ts_stage_at(cp, tasks, ntasks, nunits, blockIdx.x);
@@ -353,7 +364,10 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
             ok = __all_sync(0xffffffffu, ok);   // the tcgen05 stores below are warp-collective
             if (ok) {
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                ts_convert<!TMA>(cs, rawb + slot * TS_RAW_BYTES, tlane, TS_ACC_COLS + 64 * s + 8 * kpart, r, kpart);
+#pragma unroll
+                for (int kk = 0; kk < NKP; kk++)
+                    ts_convert<!TMA>(cs, rawb + slot * TS_RAW_BYTES, tlane, TS_ACC_COLS + 64 * s + 8 * (kpa + kk), r,
+                                     kpa + kk);
                 asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;");
             }
@@ -363,8 +377,12 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
                 if constexpr (TMA) mbar_arrive(&rempty[slot]);
             }
             if (TMA && !ok) break;
-            ts_stage_next(cs, tasks, ntasks, nunits);
-            g++;
+#pragma unroll
+            for (int i = 0; i < NG; i++) {
+                ts_stage_next(cs, tasks, ntasks, nunits);
+                g++;
+                if (!cs.valid) break;
+            }
         }
         if constexpr (!TMA) asm volatile("cp.async.wait_all;" ::: "memory");   // no copy into shared memory outlives the CTA
     } else if (warp == TS_WB && lane == 0) {
