@@ -838,6 +838,20 @@ __host__ __device__ constexpr int sub_step_smem_elems()
     return KB * KB + KB * (MAXRHS + 1) + KB * SUB_RB + SUB_RB * (MAXRHS + 1);
 }
 
+// d += a b and d += conj(a) b as four fused multiply-adds
+template <class T>
+__device__ __forceinline__ void cmac(cx<T> &d, const cx<T> a, const cx<T> b)
+{
+    d.re = fma(a.re, b.re, fma(-a.im, b.im, d.re));
+    d.im = fma(a.re, b.im, fma(a.im, b.re, d.im));
+}
+template <class T>
+__device__ __forceinline__ void cmac_conj(cx<T> &d, const cx<T> a, const cx<T> b)
+{
+    d.re = fma(a.re, b.re, fma(a.im, b.im, d.re));
+    d.im = fma(a.re, b.im, fma(-a.im, b.re, d.im));
+}
+
 // four consecutive complex values from 16-byte-aligned shared memory
 __device__ __forceinline__ void lds4(const cx<float> *p, cx<float> (&a)[4])
 {
@@ -906,28 +920,30 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
         cp_async_cx(herm ? Ms + q : Ms + (q & (KB - 1)) * KB + (q >> 6), Mi + q);
     if (nr) {
         if (mode == 0 || mode == 1) {   // A(r, l) = P[r0 + r][k + l]
-            for (int q = tid; q < nr * kb; q += blockDim.x) {
-                const int r = q / kb, l = q % kb;
-                cp_async_cx(As + l * SUB_RB + r, P + (long long)(t.r0 + r) * nf + k + l);
+            for (int q = tid; q < nr * KB; q += blockDim.x) {   // (row, column) = (q / KB, q % KB)
+                const int r = q >> 6, l = q & (KB - 1);
+                if (l < kb) cp_async_cx(As + l * SUB_RB + r, P + (long long)(t.r0 + r) * nf + k + l);
             }
         } else {                        // A(r, l) = conj(P[k + l][r0 + r])
-            for (int q = tid; q < kb * nr; q += blockDim.x) {
-                const int l = q / nr, r = q % nr;
-                cp_async_cx(As + l * SUB_RB + r, P + (long long)(k + l) * nf + t.r0 + r);
+            for (int q = tid; q < kb * SUB_RB; q += blockDim.x) {   // (column, row) = (q / SUB_RB, q % SUB_RB)
+                const int l = q / SUB_RB, r = q % SUB_RB;
+                if (r < nr) cp_async_cx(As + l * SUB_RB + r, P + (long long)(k + l) * nf + t.r0 + r);
             }
         }
     }
     panel_rows(pord, F.pan + k / KB, kb, mode == 0 || mode == 3, idx);
     // everything below reads or writes rows of X or the slots
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    for (int q = tid; q < kb * m; q += blockDim.x) {
-        const int i = q / m, c = q % m;
-        cp_async_cx(Ys + i * LY + c, Y + (long long)(k + i) * ldx + c);
+    // (row, column) loops run over MAXRHS columns (a power of two) and skip
+    // those at or beyond m: no integer division per element
+    for (int q = tid; q < kb * MAXRHS; q += blockDim.x) {
+        const int i = q / MAXRHS, c = q % MAXRHS;
+        if (c < m) cp_async_cx(Ys + i * LY + c, Y + (long long)(k + i) * ldx + c);
     }
     if (nr) {
-        for (int q = tid; q < nr * m; q += blockDim.x) {
-            const int r = q / m, c = q % m;
-            cp_async_cx(Yr + r * LY + c, Y + (long long)(t.r0 + r) * ldx + c);
+        for (int q = tid; q < nr * MAXRHS; q += blockDim.x) {
+            const int r = q / MAXRHS, c = q % MAXRHS;
+            if (c < m) cp_async_cx(Yr + r * LY + c, Y + (long long)(t.r0 + r) * ldx + c);
         }
     }
     // while the copies fly: the previous panel's solved rows into X (roles
@@ -935,9 +951,9 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
     if (t.role != 1 && t.kprev >= 0) {
         const int kbp = min(KB, F.p - t.kprev);
         #pragma unroll 8   // several loads in flight per thread
-        for (int q = tid; q < kbp * m; q += blockDim.x) {
-            const int i = q / m, c = q % m;
-            Y[(long long)(t.kprev + i) * ldx + c] = slot[i * MAXRHS + c];
+        for (int q = tid; q < kbp * MAXRHS; q += blockDim.x) {
+            const int i = q / MAXRHS, c = q % MAXRHS;
+            if (c < m) Y[(long long)(t.kprev + i) * ldx + c] = slot[i * MAXRHS + c];
         }
     }
     cp_async_wait_all();
@@ -952,12 +968,22 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
 #pragma unroll
     for (int j = 0; j < RPT; j++) acc[j] = cx<T>(0);
     if (c < m) {
-        for (int l = 0; l < kb; l++) {
-            const cx<T> y = Ys[(mode == 0 ? idx[l] : l) * LY + c];
-            cx<T> a[4];
-            lds4(Ms + l * KB + i0, a);
+        if (!herm) {
+            for (int l = 0; l < kb; l++) {
+                const cx<T> y = Ys[(mode == 0 ? idx[l] : l) * LY + c];
+                cx<T> a[4];
+                lds4(Ms + l * KB + i0, a);
 #pragma unroll
-            for (int j = 0; j < RPT; j++) acc[j] = acc[j] + (herm ? conj(a[j]) : a[j]) * y;
+                for (int j = 0; j < RPT; j++) cmac(acc[j], a[j], y);
+            }
+        } else {
+            for (int l = 0; l < kb; l++) {
+                const cx<T> y = Ys[l * LY + c];
+                cx<T> a[4];
+                lds4(Ms + l * KB + i0, a);
+#pragma unroll
+                for (int j = 0; j < RPT; j++) cmac_conj(acc[j], a[j], y);
+            }
         }
     }
     __syncthreads();
@@ -973,8 +999,9 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
     if (t.role == 0 || t.role == 3) {
         // role 3: the front's last panel of the block, which no other CTA of
         // this launch reads: solved rows straight into X
-        for (int q = tid; q < kb * m; q += blockDim.x) {
-            const int i = q / m, cc = q % m;
+        for (int q = tid; q < kb * MAXRHS; q += blockDim.x) {
+            const int i = q / MAXRHS, cc = q % MAXRHS;
+            if (cc >= m) continue;
             if (t.role == 0) slot[i * MAXRHS + cc] = Ys[i * LY + cc];
             else Y[(long long)(k + i) * ldx + cc] = Ys[i * LY + cc];
         }
@@ -986,12 +1013,22 @@ __global__ void __launch_bounds__(SUB_THREADS) k_sub_step(const StepTask *__rest
         cx<T> u[UPT];
 #pragma unroll
         for (int j = 0; j < UPT; j++) u[j] = cx<T>(0);
-        for (int l = 0; l < kb; l++) {
-            const cx<T> z = Ys[l * LY + c];
-            cx<T> a[UPT];
-            lds2(As + l * SUB_RB + u0, a);
+        if (!herm) {
+            for (int l = 0; l < kb; l++) {
+                const cx<T> z = Ys[l * LY + c];
+                cx<T> a[UPT];
+                lds2(As + l * SUB_RB + u0, a);
 #pragma unroll
-            for (int j = 0; j < UPT; j++) u[j] = u[j] + (herm ? conj(a[j]) : a[j]) * z;
+                for (int j = 0; j < UPT; j++) cmac(u[j], a[j], z);
+            }
+        } else {
+            for (int l = 0; l < kb; l++) {
+                const cx<T> z = Ys[l * LY + c];
+                cx<T> a[UPT];
+                lds2(As + l * SUB_RB + u0, a);
+#pragma unroll
+                for (int j = 0; j < UPT; j++) cmac_conj(u[j], a[j], z);
+            }
         }
 #pragma unroll
         for (int j = 0; j < UPT; j++) {
