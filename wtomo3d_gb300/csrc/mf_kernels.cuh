@@ -161,20 +161,6 @@ __device__ __forceinline__ void panel_rows(const int *__restrict__ pord, int pan
     if (tid < KB) idx[tid] = (pivoted && tid < kb) ? pord[(long long)pan * KB + tid] : tid;
 }
 
-// d += a b and d += conj(a) b as four fused multiply-adds
-template <class T>
-__device__ __forceinline__ void cmac(cx<T> &d, const cx<T> a, const cx<T> b)
-{
-    d.re = fma(a.re, b.re, fma(-a.im, b.im, d.re));
-    d.im = fma(a.re, b.im, fma(a.im, b.re, d.im));
-}
-template <class T>
-__device__ __forceinline__ void cmac_conj(cx<T> &d, const cx<T> a, const cx<T> b)
-{
-    d.re = fma(a.re, b.re, fma(a.im, b.im, d.re));
-    d.im = fma(a.re, b.im, fma(-a.im, b.re, d.im));
-}
-
 // ---------------------------------------------------------------------------
 // panel: LU of the KB x KB diagonal tile with partial pivoting inside the tile
 // ---------------------------------------------------------------------------
@@ -281,7 +267,7 @@ __global__ void __launch_bounds__(256) k_panel(const PanelTask *__restrict__ tas
         __syncthreads();
         for (int i = j + 1 + ty; i < kb; i += 16) {
             const cx<T> l = S[i * LD + j];
-            for (int c = j + 1 + tx; c < kb; c += 16) cmac(S[i * LD + c], -l, S[j * LD + c]);
+            for (int c = j + 1 + tx; c < kb; c += 16) S[i * LD + c] = S[i * LD + c] - l * S[j * LD + c];
         }
         __syncthreads();
     }
@@ -850,6 +836,20 @@ constexpr int SUB_RB = 32;   // rows per update CTA
 __host__ __device__ constexpr int sub_step_smem_elems()
 {
     return KB * KB + KB * (MAXRHS + 1) + KB * SUB_RB + SUB_RB * (MAXRHS + 1);
+}
+
+// d += a b and d += conj(a) b as four fused multiply-adds
+template <class T>
+__device__ __forceinline__ void cmac(cx<T> &d, const cx<T> a, const cx<T> b)
+{
+    d.re = fma(a.re, b.re, fma(-a.im, b.im, d.re));
+    d.im = fma(a.re, b.im, fma(a.im, b.re, d.im));
+}
+template <class T>
+__device__ __forceinline__ void cmac_conj(cx<T> &d, const cx<T> a, const cx<T> b)
+{
+    d.re = fma(a.re, b.re, fma(a.im, b.im, d.re));
+    d.im = fma(a.re, b.im, fma(-a.im, b.re, d.im));
 }
 
 // four consecutive complex values from 16-byte-aligned shared memory
