@@ -25,7 +25,7 @@ extern "C" {
 #define WT3D_ERR_CUDA          2   /* CUDA runtime error                      */
 #define WT3D_ERR_NOMEM         3   /* device or host allocation failed        */
 #define WT3D_ERR_STATE         4   /* call out of order (no model, no factor) */
-#define WT3D_ERR_PATTERN       5   /* CSR pattern is not a 27-point grid graph */
+#define WT3D_ERR_PATTERN       5   /* CSR pattern malformed or not symmetric  */
 #define WT3D_ERR_NOCONV        6   /* refinement did not reach the tolerance  */
 #define WT3D_ERR_NOGPU         7   /* no CUDA device                          */
 
@@ -55,9 +55,11 @@ typedef struct wt3d_grid {
  *   job  3 : solve one right-hand side: sol = A^-1 rhs
  *   job -1 : destroy
  * *ierr = 0 on success, 1 on error (with a message on stdout), as the
- * reference.  irptr/jcptr are read, never modified.  The pattern must be the
- * 27-point, 3-dof grid graph built by srel3d + SPARSE_ADJ2CRS; the grid is
- * recovered from it.  Factorisation is complex64 with FP64 iterative
+ * reference.  irptr/jcptr are read, never modified.  The 27-point, 3-dof grid
+ * graph built by srel3d + SPARSE_ADJ2CRS is recognised (the grid is recovered
+ * from it and ordered by plane separators); any other structurally symmetric
+ * pattern is ordered as wt3d_solver_create_csr does.  Factorisation is
+ * complex64 with FP64 iterative
  * refinement; the solution is returned in complex64 as the reference does.
  * Not re-entrant (one global instance, like the reference). */
 void strumpack_serial_finter(int *job, int *nrows, int *nnz,
@@ -121,6 +123,19 @@ typedef struct wt3d_solver wt3d_solver;
 int wt3d_solver_create(wt3d_solver **h, const wt3d_grid *g, int precision);
 int wt3d_solver_destroy(wt3d_solver *h);
 
+/* Analyse any structurally symmetric CSR pattern (n rows, nnz entries,
+ * index base 0 or 1, columns in any order, no duplicates), as STRUMPACK's
+ * reordering does for the job-1 pattern (strumpack_finter.c:42-48): automatic
+ * nested dissection (level-structure separators) on the graph of
+ * supervariables (runs of consecutive rows with equal column sets), then the
+ * same multifrontal symbolic factorisation and device storage as the grid.
+ * The handle takes values with wt3d_set_values_c64 / _c128 in this CSR order
+ * and solves with wt3d_solve*, wt3d_apply*; the entry points that need the
+ * grid (model, sources, receivers, gradient) return WT3D_ERR_STATE.  A
+ * pattern that is not structurally symmetric returns WT3D_ERR_PATTERN. */
+int wt3d_solver_create_csr(wt3d_solver **h, int n, long long nnz, const int *irptr, const int *jcptr, int base,
+                           int precision);
+
 /* Model (host arrays, (nz,nx,ny) floats). */
 int wt3d_set_model(wt3d_solver *h, const float *vp, const float *vs, const float *rho);
 
@@ -139,10 +154,13 @@ int wt3d_set_attenuation(wt3d_solver *h, const float *qp_inv, const float *qs_in
  * elwave.f90:164 (the mass terms keep only REAL(omega^2), pfdfd3d.f:140-142). */
 int wt3d_factor(wt3d_solver *h, double omega_re, double omega_im);
 
-/* Set caller-assembled operator values (complex64, host, CSR order of
- * wt3d_pattern) and factor them; the job-2 path of strumpack_serial_finter
- * (strumpack_finter.c:68-92). */
+/* Set caller-assembled operator values (complex64, host, in the CSR order of
+ * wt3d_pattern, or of the pattern given to wt3d_solver_create_csr);
+ * wt3d_factor_values then factors them.  Together the job-2 path of
+ * strumpack_serial_finter (strumpack_finter.c:68-92). */
 int wt3d_set_values_c64(wt3d_solver *h, const float _Complex *a);
+/* The same with complex128 values (no job-protocol counterpart). */
+int wt3d_set_values_c128(wt3d_solver *h, const double _Complex *a);
 int wt3d_factor_values(wt3d_solver *h);
 
 /* Background model (host floats, (nz,nx,ny)) of the scattered-field sources:
@@ -317,6 +335,14 @@ int wt3d_analyse_info(int nx, int ny, int nz, int leaf_nodes, long long *info, d
  * (new indices) and their positions in the parent front (rel). */
 int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *perm, int *fp, int *fb, int *ffirst,
                         int *fparent, int *flevel, int *border, int *rel);
+/* The same two for a general CSR pattern (as wt3d_solver_create_csr):
+ * leaf_dofs <= 0 selects 192.  info also requires every entry to fall inside
+ * its front (the scatter map). */
+int wt3d_analyse_csr_info(int n, long long nnz, const int *irptr, const int *jcptr, int base, int leaf_dofs,
+                          long long *info, double *flops);
+int wt3d_analyse_csr_export(int n, long long nnz, const int *irptr, const int *jcptr, int base, int leaf_dofs,
+                            int *perm, int *fp, int *fb, int *ffirst, int *fparent, int *flevel, int *border,
+                            int *rel);
 
 /* Select the CUDA device of the calling thread (one process per GPU). */
 int wt3d_set_device(int dev);

@@ -117,7 +117,7 @@ def numpy_multifrontal_solve(A, e, rhs):
         F[:p, :] = sub
         subT = Ap[idx[p:]][:, first:first + p].toarray()
         F[p:, :p] = subT
-        for c in [c for c in range(f) if e["parent"][c] == f]:
+        for c in [c for c in range(f) if e["parent"][c] == f and c in upd]:   # children with a border
             U, crel = upd.pop(c)
             F[np.ix_(crel, crel)] += U
         L11U11 = F[:p, :p].copy()
@@ -162,3 +162,172 @@ def test_numpy_multifrontal_matches_superlu(oracle, dims, leaf):
     e = export(nx, ny, nz, leaf)
     x = numpy_multifrontal_solve(A, e, b)
     assert np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref) < 1e-9
+
+
+# ---------------------------------------------------------------------------
+# general structurally symmetric patterns (wt3d_analyse_csr_*)
+# ---------------------------------------------------------------------------
+def check_structure(e, n):
+    assert np.array_equal(np.sort(e["perm"]), np.arange(n))
+    assert e["first"][0] == 0
+    assert np.all(e["first"][1:] == e["first"][:-1] + e["p"][:-1])
+    assert e["first"][-1] + e["p"][-1] == n
+    assert np.all(e["p"] > 0)
+    roots = np.flatnonzero(e["parent"] == -1)
+    assert list(roots) == [len(e["p"]) - 1] and e["b"][-1] == 0
+    for f, par in enumerate(e["parent"][:-1]):
+        assert par > f and e["level"][par] == e["level"][f] - 1
+    off = np.concatenate([[0], np.cumsum(e["b"])])
+    for f in range(len(e["p"])):
+        bd = e["border"][off[f]:off[f + 1]]
+        assert np.all(np.diff(bd) > 0)
+        assert bd.size == 0 or bd[0] >= e["first"][f] + e["p"][f]
+
+
+def general_case(A, leaf=0, seed=0):
+    """Export the general analysis of A's pattern, check the structure and
+    solve with the numpy multifrontal over it against SuperLU."""
+    A = sp.csr_matrix(A)
+    e = wt.analyse_csr_export(A.indptr, A.indices, 0, leaf)
+    check_structure(e, A.shape[0])
+    rng = np.random.default_rng(seed)
+    b = rng.standard_normal(A.shape[0]) + 1j * rng.standard_normal(A.shape[0])
+    x = numpy_multifrontal_solve(A, e, b)
+    xr = spla.spsolve(A.tocsc(), b)
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-9
+    return e
+
+
+def random_values(P, seed=0, dominant=True):
+    """Complex values on pattern P (csr), diagonally dominant."""
+    rng = np.random.default_rng(seed)
+    A = sp.csr_matrix(P, dtype=complex, copy=True)
+    A.data = rng.standard_normal(A.nnz) + 1j * rng.standard_normal(A.nnz)
+    if dominant:
+        A = A + sp.diags(np.abs(A).sum(axis=1).A1 + 1.0)
+    return sp.csr_matrix(A)
+
+
+def elastic_operator(oracle, nx, ny, nz):
+    g = Grid(nx, ny, nz, 20.0, pmld=2 * 20.0, fst=1)
+    vp, vs, rho = model.layered_random(nx, ny, nz, g.dx, seed=5)
+    ir, jc = oracle.pattern(nx, ny, nz)
+    a, _ = oracle.assemble(g, vp, vs, rho, 2 * np.pi * 1.0, ir)
+    return sp.csr_matrix((a, jc - 1, ir - 1), shape=(g.n, g.n))
+
+
+def test_general_grid_operator_fill_close_to_plane_separators(oracle):
+    """The elastic operator's own pattern through the general analysis: the
+    3 dofs of a node form one supervariable, the solve is exact, and the
+    factorisation costs at most 3x the flops of the plane-separator
+    ordering."""
+    A = elastic_operator(oracle, 8, 7, 6)
+    e = general_case(A, leaf=81)
+    # supervariables of 3 dofs: every front holds whole nodes
+    assert np.all(e["p"] % 3 == 0) and np.all(e["b"] % 3 == 0)
+    eg = export(8, 7, 6, 27)
+    assert e["flops"] <= 3.0 * eg["flops"], (e["flops"], eg["flops"])
+
+
+def test_general_grid_fill_at_20_cubed(oracle):
+    ir, jc = oracle.pattern(20, 20, 20)
+    info, fl = wt.analyse_csr(ir, jc, base=1)
+    eg = export(20, 20, 20, 64)
+    assert fl <= 3.0 * eg["flops"], (fl, eg["flops"])
+
+
+def test_general_node_permuted_operator(oracle):
+    """A symmetric node permutation hides the grid (job 1 no longer
+    recognises it) but keeps the 3-dof supervariables."""
+    A = elastic_operator(oracle, 6, 5, 7)
+    nn = A.shape[0] // 3
+    q = np.random.default_rng(3).permutation(nn)
+    perm = (3 * q[:, None] + np.arange(3)).reshape(-1)
+    general_case(A[perm][:, perm], leaf=30)
+
+
+def test_general_dof_permuted_operator(oracle):
+    """A random dof permutation breaks the supervariables as well."""
+    A = elastic_operator(oracle, 5, 5, 5)
+    perm = np.random.default_rng(4).permutation(A.shape[0])
+    general_case(A[perm][:, perm], leaf=40)
+
+
+def test_general_2d_five_point():
+    n1 = 30
+    T = sp.diags([np.ones(n1 - 1), np.ones(n1), np.ones(n1 - 1)], [-1, 0, 1])
+    P = sp.kron(sp.eye(n1), T) + sp.kron(T, sp.eye(n1))
+    e = general_case(random_values(P, 1), leaf=16)
+    assert len(e["p"]) > 8
+
+
+def test_general_disconnected_and_isolated():
+    """Two separate meshes plus isolated unknowns (a diagonal block)."""
+    n1 = 12
+    T = sp.diags([np.ones(n1 - 1), np.ones(n1), np.ones(n1 - 1)], [-1, 0, 1])
+    P2 = sp.kron(sp.eye(n1), T) + sp.kron(T, sp.eye(n1))
+    P = sp.block_diag([P2, sp.eye(7), sp.kron(T, T)])
+    general_case(random_values(P, 2), leaf=10)
+
+
+def test_general_unsorted_rows_random_pattern():
+    """A random symmetric pattern whose rows list their columns in random order."""
+    rng = np.random.default_rng(7)
+    n = 300
+    R = sp.random(n, n, density=0.01, random_state=8, format="csr")
+    P = ((R + R.T) != 0).astype(float) + sp.eye(n)
+    A = random_values(P, 3)
+    A = sp.csr_matrix(A)
+    # shuffle the entries inside each row
+    ind, dat = A.indices.copy(), A.data.copy()
+    for r in range(n):
+        s0, s1 = A.indptr[r], A.indptr[r + 1]
+        o = rng.permutation(s1 - s0)
+        ind[s0:s1], dat[s0:s1] = ind[s0:s1][o], dat[s0:s1][o]
+    B = sp.csr_matrix((dat, ind, A.indptr.copy()), shape=A.shape)
+    assert not B.has_sorted_indices
+    e = wt.analyse_csr_export(B.indptr, B.indices, 0, 24)
+    check_structure(e, n)
+    b = rng.standard_normal(n) + 0j
+    x = numpy_multifrontal_solve(B, e, b)
+    xr = spla.spsolve(A.tocsc(), b)
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-9
+
+
+def test_general_dense_and_single():
+    general_case(random_values(np.ones((40, 40)), 4), leaf=8)
+    e = wt.analyse_csr_export(np.array([0, 1]), np.array([0]))
+    assert list(e["p"]) == [1] and list(e["b"]) == [0]
+    # one row without its diagonal entry is still a valid pattern
+    e = wt.analyse_csr_export(np.array([0, 0]), np.array([], np.int32))
+    assert list(e["p"]) == [1]
+
+
+def test_general_long_path_is_balanced():
+    """A tridiagonal pattern of 200k unknowns: the level structure of a path
+    splits it in the middle each time, so the tree is ~log2(n / leaf) deep
+    and every front is small."""
+    n = 200_000
+    T = sp.diags([np.ones(n - 1), np.ones(n), np.ones(n - 1)], [-1, 0, 1], format="csr")
+    info, fl = wt.analyse_csr(T.indptr, T.indices, 0, 64)
+    nfronts, levels, maxp, maxb = info[0], info[2], info[3], info[4]
+    assert levels <= 20 and maxp <= 64 and maxb <= 2 * levels
+
+
+def test_general_bad_patterns_are_rejected():
+    # (0,1) without (1,0): not structurally symmetric
+    with pytest.raises(wt.WT3DError) as e:
+        wt.analyse_csr([0, 2, 3], [0, 1, 1])
+    assert e.value.code == wt.WT3D_ERR_PATTERN
+    # duplicate column in a row
+    with pytest.raises(wt.WT3DError) as e:
+        wt.analyse_csr([0, 2, 3], [0, 0, 1])
+    assert e.value.code == wt.WT3D_ERR_PATTERN
+    # column out of range
+    with pytest.raises(wt.WT3DError) as e:
+        wt.analyse_csr([0, 1, 2], [0, 5])
+    assert e.value.code == wt.WT3D_ERR_PATTERN
+    # row pointers that do not start at the base
+    with pytest.raises(wt.WT3DError) as e:
+        wt.analyse_csr([1, 2, 3], [0, 1], base=0)
+    assert e.value.code == wt.WT3D_ERR_PATTERN

@@ -117,6 +117,13 @@ def lib():
         L.wt3d_set_model.argtypes = [vp, vp, vp, vp]
         L.wt3d_factor.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         L.wt3d_set_values_c64.argtypes = [vp, vp]
+        L.wt3d_set_values_c128.argtypes = [vp, vp]
+        L.wt3d_solver_create_csr.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_longlong, vp, vp,
+                                             ctypes.c_int, ctypes.c_int]
+        L.wt3d_analyse_csr_info.argtypes = [ctypes.c_int, ctypes.c_longlong, vp, vp, ctypes.c_int, ctypes.c_int,
+                                            vp, vp]
+        L.wt3d_analyse_csr_export.argtypes = [ctypes.c_int, ctypes.c_longlong, vp, vp, ctypes.c_int, ctypes.c_int]\
+            + [vp] * 8
         L.wt3d_factor_values.argtypes = [vp]
         for f in (L.wt3d_solve, L.wt3d_solve_adjoint):
             f.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_double, ctypes.c_int, vp, vp]
@@ -235,14 +242,64 @@ def solver_bytes(grid, precision=PREC_MIXED):
     return float(out[0]), float(out[1]), float(out[2])
 
 
+def _csr_arrays(indptr, indices):
+    ir = np.ascontiguousarray(indptr, np.int32)
+    jc = np.ascontiguousarray(indices, np.int32)
+    return ir, jc, len(ir) - 1, len(jc)
+
+
+def analyse_csr(indptr, indices, base=0, leaf_dofs=0):
+    """Host analysis of a general structurally symmetric CSR pattern (no GPU):
+    returns (info[8], flops) as wt3d_analyse_csr_info does."""
+    ir, jc, n, nnz = _csr_arrays(indptr, indices)
+    info = np.zeros(8, np.int64)
+    fl = ctypes.c_double()
+    _check(lib().wt3d_analyse_csr_info(n, nnz, _ptr(ir), _ptr(jc), int(base), int(leaf_dofs), _ptr(info),
+                                       ctypes.byref(fl)))
+    return info, fl.value
+
+
+def analyse_csr_export(indptr, indices, base=0, leaf_dofs=0):
+    """Elimination structure of a general pattern: dict of perm, per-front p,
+    b, first, parent, level, and the border dofs with their parent positions."""
+    ir, jc, n, nnz = _csr_arrays(indptr, indices)
+    info, flops = analyse_csr(ir, jc, base, leaf_dofs)
+    nf, nb = int(info[0]), int(info[5])
+    perm = np.zeros(n, np.int32)
+    arrs = [np.zeros(nf, np.int32) for _ in range(5)]
+    border = np.zeros(nb, np.int32)
+    rel = np.zeros(nb, np.int32)
+    _check(lib().wt3d_analyse_csr_export(n, nnz, _ptr(ir), _ptr(jc), int(base), int(leaf_dofs), _ptr(perm),
+                                         *[_ptr(a) for a in arrs], _ptr(border), _ptr(rel)))
+    fp, fb, ffirst, fpar, flev = arrs
+    return dict(perm=perm, p=fp, b=fb, first=ffirst, parent=fpar, level=flev, border=border, rel=rel,
+                info=[int(v) for v in info], flops=flops)
+
+
 class Solver:
     """Handle-based multifrontal solver on one GPU (wt3d_solver_*)."""
 
     def __init__(self, grid, precision=PREC_MIXED):
         self.grid = grid
+        self.n = grid.n
         self.precision = precision
         self._h = ctypes.c_void_p()
         _check(lib().wt3d_solver_create(ctypes.byref(self._h), ctypes.byref(grid), precision))
+
+    @classmethod
+    def from_csr(cls, indptr, indices, precision=PREC_MIXED, base=0):
+        """Handle for any structurally symmetric CSR pattern
+        (wt3d_solver_create_csr); values come from set_values in the same CSR
+        order.  The grid-only calls (model, sources, gradient) raise."""
+        ir, jc, n, nnz = _csr_arrays(indptr, indices)
+        self = cls.__new__(cls)
+        self.grid = None
+        self.n = n
+        self.precision = precision
+        self._h = ctypes.c_void_p()
+        _check(lib().wt3d_solver_create_csr(ctypes.byref(self._h), n, nnz, _ptr(ir), _ptr(jc), int(base),
+                                            precision))
+        return self
 
     def close(self):
         if self._h:
@@ -270,15 +327,21 @@ class Solver:
         om = complex(omega)
         _check(lib().wt3d_factor(self._h, om.real, om.imag))
 
-    def set_values(self, a_c64):
-        a = np.ascontiguousarray(a_c64, dtype=np.complex64)
-        _check(lib().wt3d_set_values_c64(self._h, _ptr(a)))
+    def set_values(self, a, dtype=np.complex64):
+        """Set operator values in CSR order (complex64 as the job protocol
+        takes them, or complex128) and factor."""
+        if np.dtype(dtype) == np.complex128:
+            a = np.ascontiguousarray(a, dtype=np.complex128)
+            _check(lib().wt3d_set_values_c128(self._h, _ptr(a)))
+        else:
+            a = np.ascontiguousarray(a, dtype=np.complex64)
+            _check(lib().wt3d_set_values_c64(self._h, _ptr(a)))
         _check(lib().wt3d_factor_values(self._h))
 
     def _solve(self, fn, B, tol, maxit, allow_noconv):
         B = np.asarray(B, dtype=np.complex128)
         one = B.ndim == 1
-        Bf = np.asfortranarray(B.reshape(self.grid.n, -1))
+        Bf = np.asfortranarray(B.reshape(self.n, -1))
         nrhs = Bf.shape[1]
         X = np.empty_like(Bf, order="F")
         relres = np.zeros(nrhs)
@@ -299,7 +362,7 @@ class Solver:
     def apply(self, X):
         X = np.asarray(X, dtype=np.complex128)
         one = X.ndim == 1
-        Xf = np.asfortranarray(X.reshape(self.grid.n, -1))
+        Xf = np.asfortranarray(X.reshape(self.n, -1))
         Y = np.empty_like(Xf, order="F")
         _check(lib().wt3d_apply(self._h, Xf.shape[1], _ptr(Xf), _ptr(Y)))
         return Y[:, 0] if one else Y

@@ -113,6 +113,53 @@ __global__ void __launch_bounds__(256) k_residual(long long n, int m, const int 
         if (on[h]) { atomicAdd(&nr[lane + 32 * h], sr[h]); atomicAdd(&nb[lane + 32 * h], sb[h]); }
 }
 
+// The same residual for a general pattern: one warp per row, rows of any
+// length and columns in any order.
+__global__ void __launch_bounds__(256) k_residual_rows(long long n, int m, const int *__restrict__ irptr,
+                                                       const int *__restrict__ jcptr, const double2 *__restrict__ a,
+                                                       const int *__restrict__ tpos, const double2 *__restrict__ X,
+                                                       const double2 *__restrict__ B, double2 *__restrict__ R,
+                                                       double *__restrict__ nr, double *__restrict__ nb, int adjoint)
+{
+    const int lane = threadIdx.x & 31;
+    const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    bool on[NH];
+    double sr[NH], sb[NH];
+#pragma unroll
+    for (int h = 0; h < NH; h++) { on[h] = lane + 32 * h < m; sr[h] = sb[h] = 0; }
+    for (long long r = w0; r < n; r += nw) {
+        double2 acc[NH];
+#pragma unroll
+        for (int h = 0; h < NH; h++) acc[h] = make_double2(0, 0);
+        for (int k = irptr[r]; k < irptr[r + 1]; k++) {
+            const double2 *xr = X + (long long)jcptr[k] * MAXRHS + lane;
+            double2 av;
+            if (adjoint) { av = a[tpos[k]]; av.y = -av.y; }
+            else av = a[k];
+#pragma unroll
+            for (int h = 0; h < NH; h++) {
+                const double2 x = on[h] ? xr[32 * h] : make_double2(0, 0);
+                acc[h].x = fma(av.x, x.x, fma(-av.y, x.y, acc[h].x));
+                acc[h].y = fma(av.x, x.y, fma(av.y, x.x, acc[h].y));
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < NH; h++) {
+            if (!on[h]) continue;
+            const int j = lane + 32 * h;
+            const double2 b = B ? B[r * MAXRHS + j] : make_double2(0, 0);
+            const double2 q = B ? make_double2(b.x - acc[h].x, b.y - acc[h].y) : acc[h];
+            R[r * MAXRHS + j] = q;
+            sr[h] += q.x * q.x + q.y * q.y;
+            sb[h] += b.x * b.x + b.y * b.y;
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < NH; h++)
+        if (on[h]) { atomicAdd(&nr[lane + 32 * h], sr[h]); atomicAdd(&nb[lane + 32 * h], sb[h]); }
+}
+
 // ---- batched Krylov kernels over n x MAXRHS row-major FP64 blocks -------
 // Column c of every block is an independent system; reductions go through
 // per-block partial sums and a second pass, so they do not depend on
@@ -329,6 +376,7 @@ struct GridAnalysis {
 struct wt3d_solver {
     wt3d_grid grid{};
     int prec = WT3D_PREC_MIXED;
+    bool general = false;                 // caller's pattern (wt3d_solver_create_csr), not the grid graph
     std::shared_ptr<GridAnalysis> ga;
     long long n = 0, nnz = 0;
     DevVec<int> irptr, jcptr, tpos, perm;
@@ -404,6 +452,20 @@ int have_gpu()
         return WT3D_ERR_NOGPU;
     }
     return WT3D_OK;
+}
+
+// R = B - op(A) X (R = op(A) X when B is null), accumulating the squared
+// column norms of R and B into h->norms: node-blocked rows for the grid
+// pattern, one warp per row for a general pattern.
+void residual(const wt3d_solver *h, cudaStream_t st, int m, const double2 *X, const double2 *B, double2 *R,
+              bool adjoint)
+{
+    if (h->general)
+        k_residual_rows<<<152 * 8, 256, 0, st>>>(h->n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, X, B, R,
+                                                 h->norms.p, h->norms.p + MAXRHS, adjoint ? 1 : 0);
+    else
+        k_residual<<<152 * 8, 256, 0, st>>>(h->n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, X, B, R,
+                                            h->norms.p, h->norms.p + MAXRHS, adjoint ? 1 : 0);
 }
 
 // Restarted flexible GMRES in FP64, right-preconditioned by the factorisation
@@ -496,8 +558,7 @@ int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, d
             k_scatter_add_nat<T><<<nbm, th, 0, st>>>(n, m, h->perm.p, E.scale.p, E.X.p, Zj);
             // w = op(A) z_j
             WT_CUDA(cudaMemsetAsync(h->norms.p, 0, sizeof(double) * 2 * MAXRHS, st));
-            k_residual<<<152 * 8, 256, 0, st>>>(n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, Zj, nullptr, W,
-                                                h->norms.p, h->norms.p + MAXRHS, adjoint ? 1 : 0);
+            residual(h, st, m, Zj, nullptr, W, adjoint);
             h->kernels_solve += sc->kernels() + 11;
             if ((rc = orth(j + 1, W, hb, false)) || (rc = orth(j + 1, W, hb2, true))) return rc;
             it++;
@@ -551,8 +612,7 @@ int fgmres(wt3d_solver *h, Engine<T> &E, Schedule<T> *sc, int m, bool adjoint, d
         // true residual
         std::vector<double> hn2(2 * MAXRHS);
         WT_CUDA(cudaMemsetAsync(h->norms.p, 0, sizeof(double) * 2 * MAXRHS, st));
-        k_residual<<<152 * 8, 256, 0, st>>>(n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, h->Xn.p, h->Bn.p,
-                                            h->Rn.p, h->norms.p, h->norms.p + MAXRHS, adjoint ? 1 : 0);
+        residual(h, st, m, h->Xn.p, h->Bn.p, h->Rn.p, adjoint);
         WT_CUDA(cudaGetLastError());
         WT_CUDA(cudaMemcpyAsync(hn2.data(), h->norms.p, sizeof(double) * 2 * MAXRHS, cudaMemcpyDeviceToHost, st));
         WT_CUDA(cudaStreamSynchronize(st));
@@ -614,8 +674,7 @@ int refine(wt3d_solver *h, Engine<T> &E, int m, bool adjoint, double tol, int ma
         h->kernels_solve += sc->kernels() + 3;   // + gather, scatter-add, residual
         k_scatter_add_nat<T><<<nb, th, 0, st>>>(n, m, h->perm.p, E.scale.p, E.X.p, h->Xn.p);
         WT_CUDA(cudaMemsetAsync(h->norms.p, 0, sizeof(double) * 2 * MAXRHS, st));
-        k_residual<<<152 * 8, 256, 0, st>>>(n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, h->Xn.p, h->Bn.p,
-                                            h->Rn.p, h->norms.p, h->norms.p + MAXRHS, adjoint ? 1 : 0);
+        residual(h, st, m, h->Xn.p, h->Bn.p, h->Rn.p, adjoint);
         WT_CUDA(cudaGetLastError());
         WT_CUDA(cudaMemcpyAsync(hn.data(), h->norms.p, sizeof(double) * 2 * MAXRHS, cudaMemcpyDeviceToHost, st));
         WT_CUDA(cudaStreamSynchronize(st));
@@ -844,23 +903,25 @@ int wt3d_assemble(const wt3d_grid *g, const float *vp, const float *vs, const fl
 }
 
 // -------------------------------------------------------------------------
-int wt3d_solver_create(wt3d_solver **out, const wt3d_grid *g, int precision)
+}  // extern "C"
+
+namespace {
+
+// Leaf fronts of a general pattern hold at most this many dofs (the grid's
+// leaf boxes hold 64 nodes, 192 dofs).
+constexpr long long GENERAL_LEAF_DOFS = 192;
+
+// Entry points that build or use the grid's model, sources and receivers
+// refuse handles of a general pattern.
+int grid_only(const char *fn)
 {
-    if (!out) { set_error("null handle pointer"); return WT3D_ERR_ARG; }
-    *out = nullptr;
-    int rc = check_grid(g);
-    if (rc) return rc;
-    if (precision != WT3D_PREC_MIXED && precision != WT3D_PREC_FP64) { set_error("bad precision"); return WT3D_ERR_ARG; }
-    if ((rc = have_gpu())) return rc;
-    auto t0 = std::chrono::steady_clock::now();
-    std::unique_ptr<wt3d_solver> h(new wt3d_solver());
-    h->grid = *g;
-    h->prec = precision;
-    if ((rc = grid_analysis(g->nx, g->ny, g->nz, h->ga))) return rc;
-    GridAnalysis &ga = *h->ga;
-    const Symbolic &sym = ga.sym;
-    h->n = sym.n;
-    h->nnz = wt3d_pattern_nnz(g->nx, g->ny, g->nz);
+    set_error(std::string(fn) + ": needs a grid handle (wt3d_solver_create), not a general pattern");
+    return WT3D_ERR_STATE;
+}
+
+// Streams and events of a new handle.
+int handle_streams(wt3d_solver *h)
+{
     WT_CUDA(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
     {
         // solves run ahead of other handles' factorisations: their kernels are
@@ -872,29 +933,19 @@ int wt3d_solver_create(wt3d_solver **out, const wt3d_grid *g, int precision)
     WT_CUDA(cudaEventCreate(&h->ev0));
     WT_CUDA(cudaEventCreate(&h->ev1));
     WT_CUDA(cudaEventCreateWithFlags(&h->evl, cudaEventDisableTiming));
-    if ((rc = h->irptr.alloc(h->n + 1)) || (rc = h->jcptr.alloc(h->nnz)) || (rc = h->a.alloc(h->nnz))) return rc;
-    if ((rc = device_pattern(g->nx, g->ny, g->nz, 0, h->irptr.p, h->jcptr.p, h->st))) return rc;
-    std::shared_ptr<FactorWorkspace<float>> w32;
-    std::shared_ptr<FactorWorkspace<double>> w64;
-    {
-        std::lock_guard<std::mutex> lk(ga.mu);
-        if (ga.map.empty()) {
-            std::vector<int> hir(h->n + 1), hjc(h->nnz);
-            WT_CUDA(cudaMemcpyAsync(hir.data(), h->irptr.p, sizeof(int) * (h->n + 1), cudaMemcpyDeviceToHost, h->st));
-            WT_CUDA(cudaMemcpyAsync(hjc.data(), h->jcptr.p, sizeof(int) * h->nnz, cudaMemcpyDeviceToHost, h->st));
-            WT_CUDA(cudaStreamSynchronize(h->st));
-            std::vector<long long> map;
-            if ((rc = scatter_map(sym, hir, hjc, map))) return rc;
-            // transposed positions for the adjoint residual
-            std::vector<int> tp(h->nnz), cur(hir.begin(), hir.end() - 1);
-            for (long long r = 0; r < h->n; r++)
-                for (long long k = hir[r]; k < hir[r + 1]; k++) tp[k] = cur[hjc[k]]++;
-            ga.map.swap(map);
-            ga.tpos.swap(tp);
-        }
-        if (precision == WT3D_PREC_MIXED) w32 = pick_workspace(ga.ws32);
-        else w64 = pick_workspace(ga.ws64);
-    }
+    return WT3D_OK;
+}
+
+// The rest of a new handle once its analysis (h->ga, with the scatter map and
+// transposed positions) and its 0-based pattern on the device are in place:
+// the permutation, the FP64 refinement blocks and the engine of the
+// precision, over the factorisation workspace w32 or w64.
+int handle_engine(wt3d_solver *h, int precision, std::shared_ptr<FactorWorkspace<float>> w32,
+                  std::shared_ptr<FactorWorkspace<double>> w64, std::chrono::steady_clock::time_point t0)
+{
+    int rc;
+    const GridAnalysis &ga = *h->ga;
+    const Symbolic &sym = ga.sym;
     if ((rc = h->tpos.upload(ga.tpos))) return rc;
     if ((rc = h->perm.upload(sym.perm))) return rc;
     if ((rc = h->Bn.alloc((size_t)h->n * MAXRHS)) || (rc = h->Xn.alloc((size_t)h->n * MAXRHS)) ||
@@ -917,8 +968,94 @@ int wt3d_solver_create(wt3d_solver **out, const wt3d_grid *g, int precision)
     h->stats.factor_bytes = (double)sym.fac_total * (precision == WT3D_PREC_MIXED ? 8.0 : 16.0);
     h->stats.levels = (int)sym.levels.size();
     h->stats.t_analyse_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
-    h->stats.device_bytes = own_bytes(h.get());
+    h->stats.device_bytes = own_bytes(h);
     h->stats.workspace_bytes = (double)(h->e32 ? h->e32->workspace_bytes() : h->e64->workspace_bytes());
+    return WT3D_OK;
+}
+
+std::vector<int> to_int(const std::vector<long long> &v)
+{
+    return std::vector<int>(v.begin(), v.end());
+}
+
+}  // namespace
+
+extern "C" {
+
+int wt3d_solver_create(wt3d_solver **out, const wt3d_grid *g, int precision)
+{
+    if (!out) { set_error("null handle pointer"); return WT3D_ERR_ARG; }
+    *out = nullptr;
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (precision != WT3D_PREC_MIXED && precision != WT3D_PREC_FP64) { set_error("bad precision"); return WT3D_ERR_ARG; }
+    if ((rc = have_gpu())) return rc;
+    auto t0 = std::chrono::steady_clock::now();
+    std::unique_ptr<wt3d_solver> h(new wt3d_solver());
+    h->grid = *g;
+    h->prec = precision;
+    if ((rc = grid_analysis(g->nx, g->ny, g->nz, h->ga))) return rc;
+    GridAnalysis &ga = *h->ga;
+    const Symbolic &sym = ga.sym;
+    h->n = sym.n;
+    h->nnz = wt3d_pattern_nnz(g->nx, g->ny, g->nz);
+    if ((rc = handle_streams(h.get()))) return rc;
+    if ((rc = h->irptr.alloc(h->n + 1)) || (rc = h->jcptr.alloc(h->nnz)) || (rc = h->a.alloc(h->nnz))) return rc;
+    if ((rc = device_pattern(g->nx, g->ny, g->nz, 0, h->irptr.p, h->jcptr.p, h->st))) return rc;
+    std::shared_ptr<FactorWorkspace<float>> w32;
+    std::shared_ptr<FactorWorkspace<double>> w64;
+    {
+        std::lock_guard<std::mutex> lk(ga.mu);
+        if (ga.map.empty()) {
+            std::vector<int> hir(h->n + 1), hjc(h->nnz);
+            WT_CUDA(cudaMemcpyAsync(hir.data(), h->irptr.p, sizeof(int) * (h->n + 1), cudaMemcpyDeviceToHost, h->st));
+            WT_CUDA(cudaMemcpyAsync(hjc.data(), h->jcptr.p, sizeof(int) * h->nnz, cudaMemcpyDeviceToHost, h->st));
+            WT_CUDA(cudaStreamSynchronize(h->st));
+            std::vector<long long> map;
+            if ((rc = scatter_map(sym, hir, hjc, map))) return rc;
+            // transposed positions for the adjoint residual
+            std::vector<int> tp = to_int(transpose_positions(h->n, hir.data(), hjc.data()));
+            ga.map.swap(map);
+            ga.tpos.swap(tp);
+        }
+        if (precision == WT3D_PREC_MIXED) w32 = pick_workspace(ga.ws32);
+        else w64 = pick_workspace(ga.ws64);
+    }
+    if ((rc = handle_engine(h.get(), precision, w32, w64, t0))) return rc;
+    *out = h.release();
+    return WT3D_OK;
+}
+
+int wt3d_solver_create_csr(wt3d_solver **out, int n, long long nnz, const int *irptr, const int *jcptr, int base,
+                           int precision)
+{
+    if (!out) { set_error("null handle pointer"); return WT3D_ERR_ARG; }
+    *out = nullptr;
+    if (precision != WT3D_PREC_MIXED && precision != WT3D_PREC_FP64) { set_error("bad precision"); return WT3D_ERR_ARG; }
+    int rc = check_csr(n, nnz, irptr, jcptr, base, true);
+    if (rc) return rc;
+    if ((rc = have_gpu())) return rc;
+    auto t0 = std::chrono::steady_clock::now();
+    std::unique_ptr<wt3d_solver> h(new wt3d_solver());
+    h->general = true;
+    h->prec = precision;
+    h->ga = std::make_shared<GridAnalysis>();
+    GridAnalysis &ga = *h->ga;
+    if ((rc = symbolic_graph(n, irptr, jcptr, base, GENERAL_LEAF_DOFS, ga.sym))) return rc;
+    h->n = n;
+    h->nnz = nnz;
+    std::vector<int> hir(irptr, irptr + n + 1), hjc(jcptr, jcptr + nnz);
+    for (auto &v : hir) v -= base;
+    for (auto &v : hjc) v -= base;
+    if ((rc = scatter_map(ga.sym, hir, hjc, ga.map))) return rc;
+    ga.tpos = to_int(transpose_positions(n, hir.data(), hjc.data()));
+    if ((rc = handle_streams(h.get()))) return rc;
+    if ((rc = h->irptr.upload(hir)) || (rc = h->jcptr.upload(hjc)) || (rc = h->a.alloc(nnz))) return rc;
+    std::shared_ptr<FactorWorkspace<float>> w32;
+    std::shared_ptr<FactorWorkspace<double>> w64;
+    if (precision == WT3D_PREC_MIXED) w32 = pick_workspace(ga.ws32);
+    else w64 = pick_workspace(ga.ws64);
+    if ((rc = handle_engine(h.get(), precision, w32, w64, t0))) return rc;
     *out = h.release();
     return WT3D_OK;
 }
@@ -931,6 +1068,7 @@ int wt3d_solver_destroy(wt3d_solver *h)
 
 int wt3d_set_model(wt3d_solver *h, const float *vp, const float *vs, const float *rho)
 {
+    if (h && h->general) return grid_only("wt3d_set_model");
     if (!h || !vp || !vs || !rho) { set_error("wt3d_set_model: null pointer"); return WT3D_ERR_ARG; }
     long long nn = h->n / 3;
     int rc;
@@ -974,6 +1112,7 @@ static int factor_values(wt3d_solver *h)
 
 int wt3d_factor(wt3d_solver *h, double omega_re, double omega_im)
 {
+    if (h && h->general) return grid_only("wt3d_factor");
     if (!h) { set_error("null handle"); return WT3D_ERR_ARG; }
     if (!h->have_model) { set_error("wt3d_factor: no model set"); return WT3D_ERR_STATE; }
     h->have_factor = false;
@@ -998,6 +1137,7 @@ int wt3d_factor(wt3d_solver *h, double omega_re, double omega_im)
 
 int wt3d_set_attenuation(wt3d_solver *h, const float *qp_inv, const float *qs_inv, double freqbase)
 {
+    if (h && h->general) return grid_only("wt3d_set_attenuation");
     if (!h) { set_error("null handle"); return WT3D_ERR_ARG; }
     if (!qp_inv || !qs_inv) {   // back to an elastic model
         h->qp.free();
@@ -1021,6 +1161,7 @@ int wt3d_set_attenuation(wt3d_solver *h, const float *qp_inv, const float *qs_in
 
 int wt3d_set_background(wt3d_solver *h, const float *vp, const float *vs, const float *rho)
 {
+    if (h && h->general) return grid_only("wt3d_set_background");
     if (!h || !vp || !vs || !rho) { set_error("wt3d_set_background: null pointer"); return WT3D_ERR_ARG; }
     const long long nn = h->n / 3;
     int rc;
@@ -1047,6 +1188,7 @@ int wt3d_haskgrn(const wt3d_layered1d *m, double omega, double ain, int s_wave, 
 int wt3d_rhs_planewave(wt3d_solver *h, const wt3d_layered1d *m, int nsrc, const double *ain, const double *baz,
                        const int *s_wave, void *d_F, void *d_U0)
 {
+    if (h && h->general) return grid_only("wt3d_rhs_planewave");
     if (!h || !m || nsrc < 1 || !ain || !baz || !d_F) { set_error("wt3d_rhs_planewave: bad arguments"); return WT3D_ERR_ARG; }
     if (int rc0 = after_legacy(h, h->st)) return rc0;
     if (!h->have_values || !h->have_bg) { set_error("wt3d_rhs_planewave: needs a factored operator and a background"); return WT3D_ERR_STATE; }
@@ -1110,6 +1252,16 @@ int wt3d_set_values_c64(wt3d_solver *h, const float _Complex *a)
     return WT3D_OK;
 }
 
+int wt3d_set_values_c128(wt3d_solver *h, const double _Complex *a)
+{
+    if (!h || !a) { set_error("null pointer"); return WT3D_ERR_ARG; }
+    WT_CUDA(cudaMemcpyAsync(h->a.p, a, sizeof(double2) * h->nnz, cudaMemcpyHostToDevice, h->st));
+    WT_CUDA(cudaStreamSynchronize(h->st));
+    h->have_values = true;
+    h->have_factor = false;
+    return WT3D_OK;
+}
+
 int wt3d_factor_values(wt3d_solver *h)
 {
     if (!h || !h->have_values) { set_error("no operator values"); return WT3D_ERR_STATE; }
@@ -1166,8 +1318,7 @@ int wt3d_apply(wt3d_solver *h, int nrhs, const double _Complex *X, double _Compl
         WT_CUDA(cudaMemsetAsync(h->Bn.p, 0, sizeof(double2) * n * MAXRHS, h->st));
         WT_CUDA(cudaMemsetAsync(h->norms.p, 0, sizeof(double) * 2 * MAXRHS, h->st));
         // R = 0 - A X
-        k_residual<<<152 * 8, 256, 0, h->st>>>(n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, h->Xn.p, h->Bn.p,
-                                               h->Rn.p, h->norms.p, h->norms.p + MAXRHS, 0);
+        residual(h, h->st, m, h->Xn.p, h->Bn.p, h->Rn.p, false);
         k_rm_to_cm<<<ceil_div(n, 256), 256, 0, h->st>>>(n, m, h->Rn.p, dX.p + (long long)c0 * n);
     }
     std::vector<std::complex<double>> tmp((size_t)n * nrhs);
@@ -1190,8 +1341,7 @@ int wt3d_apply_device(wt3d_solver *h, int nrhs, const void *d_X, void *d_Y)
         WT_CUDA(cudaMemsetAsync(h->Bn.p, 0, sizeof(double2) * n * MAXRHS, h->st));
         WT_CUDA(cudaMemsetAsync(h->norms.p, 0, sizeof(double) * 2 * MAXRHS, h->st));
         // R = 0 - A X, then Y = -R
-        k_residual<<<152 * 8, 256, 0, h->st>>>(n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, h->Xn.p, h->Bn.p,
-                                               h->Rn.p, h->norms.p, h->norms.p + MAXRHS, 0);
+        residual(h, h->st, m, h->Xn.p, h->Bn.p, h->Rn.p, false);
         k_rm_to_cm_neg<<<ceil_div(n, 256), 256, 0, h->st>>>(n, m, h->Rn.p, (double2 *)d_Y + (long long)c0 * n);
     }
     WT_CUDA(cudaGetLastError());
@@ -1201,6 +1351,7 @@ int wt3d_apply_device(wt3d_solver *h, int nrhs, const void *d_X, void *d_Y)
 
 int wt3d_update_operator(wt3d_solver *h)
 {
+    if (h && h->general) return grid_only("wt3d_update_operator");
     if (!h) { set_error("null handle"); return WT3D_ERR_ARG; }
     if (!h->have_model || !h->have_values) { set_error("wt3d_update_operator: needs a model and a factored operator"); return WT3D_ERR_STATE; }
     int rc;
@@ -1215,6 +1366,7 @@ int wt3d_update_operator(wt3d_solver *h)
 
 int wt3d_gradient_contract(wt3d_solver *h, int nrhs, const void *d_U, const void *d_Lam, void *d_grad)
 {
+    if (h && h->general) return grid_only("wt3d_gradient_contract");
     if (!h || nrhs < 1 || !d_U || !d_Lam || !d_grad) { set_error("wt3d_gradient_contract: bad arguments"); return WT3D_ERR_ARG; }
     if (int rc0 = after_legacy(h, h->st)) return rc0;
     if (!h->have_model || !h->have_values) { set_error("wt3d_gradient_contract: needs a model and an assembled operator"); return WT3D_ERR_STATE; }
@@ -1236,6 +1388,7 @@ int wt3d_misfit_gradient(wt3d_solver *h, int nsrc, const void *d_F, const void *
                          const long long *rec_node, const double _Complex *dobs, double tol, int maxit, double *chi,
                          double *grad, double _Complex *dpred)
 {
+    if (h && h->general) return grid_only("wt3d_misfit_gradient");
     if (!h || nsrc < 1 || !d_F || nrec < 1 || !rec_node || !dobs || !chi || !grad) {
         set_error("wt3d_misfit_gradient: bad arguments");
         return WT3D_ERR_ARG;
@@ -1303,6 +1456,7 @@ int wt3d_memcpy(wt3d_solver *h, void *dst, const void *src, long long bytes)
 int wt3d_rhs_sources(wt3d_solver *h, int nsrc, const double *xyz, const int *comp, const double _Complex *sterm,
                      int ireg, double sprd, void *d_F)
 {
+    if (h && h->general) return grid_only("wt3d_rhs_sources");
     if (!h || nsrc < 1 || !xyz || !comp || !d_F) { set_error("wt3d_rhs_sources: bad arguments"); return WT3D_ERR_ARG; }
     if (int rc0 = after_legacy(h, h->st)) return rc0;
     const long long n = h->n;
@@ -1343,6 +1497,7 @@ int wt3d_rhs_sources(wt3d_solver *h, int nsrc, const double *xyz, const int *com
 int wt3d_sample_receivers(wt3d_solver *h, int nrhs, const void *d_U, int nrec, const double *xyz, int ireg,
                           double sprd, double _Complex *out)
 {
+    if (h && h->general) return grid_only("wt3d_sample_receivers");
     if (!h || nrhs < 1 || !d_U || nrec < 1 || !xyz || !out) { set_error("wt3d_sample_receivers: bad arguments"); return WT3D_ERR_ARG; }
     if (int rc0 = after_legacy(h, h->st)) return rc0;
     std::vector<int> start(1, 0);
@@ -1375,6 +1530,7 @@ int wt3d_sample_receivers(wt3d_solver *h, int nrhs, const void *d_U, int nrec, c
 int wt3d_sample_pressure(wt3d_solver *h, int nrhs, const void *d_U, int nrec, const double *xyz, int ireg,
                          double sprd, double _Complex *out)
 {
+    if (h && h->general) return grid_only("wt3d_sample_pressure");
     if (!h || nrhs < 1 || !d_U || nrec < 1 || !xyz || !out) { set_error("wt3d_sample_pressure: bad arguments"); return WT3D_ERR_ARG; }
     if (!h->have_model || !h->have_values) { set_error("wt3d_sample_pressure: needs a model and an assembled operator"); return WT3D_ERR_STATE; }
     const wt3d_grid &g = h->grid;
@@ -1486,15 +1642,22 @@ void strumpack_serial_finter(int *job, int *nrows, int *nnz, int *irptr, int *jc
     *ierr = 0;
     if (*job == 1) {
         if (g_sp) { printf("%s: Error already initialized!\n", fcnm); *ierr = 1; return; }
-        int nx, ny, nz;
-        if (detect_grid(*nrows, *nnz, irptr, jcptr, nx, ny, nz) != WT3D_OK) {
+        // the grid graph of srel3d + SPARSE_ADJ2CRS gets the geometric nested
+        // dissection; any other structurally symmetric pattern the general one
+        int nx, ny, nz, rc;
+        if (!irptr || !jcptr || !nrows || !nnz) {
             printf("%s: Error reordering matrix!\n", fcnm);
-            set_error("CSR pattern is not the 27-point 3-dof grid graph");
+            set_error("null pattern argument");
             *ierr = 1;
             return;
         }
-        wt3d_grid g{nx, ny, nz, 1.0, 0.0, 0.0, 1, 1};
-        if (wt3d_solver_create(&g_sp, &g, WT3D_PREC_MIXED) != WT3D_OK) {
+        if (detect_grid(*nrows, *nnz, irptr, jcptr, nx, ny, nz) == WT3D_OK) {
+            wt3d_grid g{nx, ny, nz, 1.0, 0.0, 0.0, 1, 1};
+            rc = wt3d_solver_create(&g_sp, &g, WT3D_PREC_MIXED);
+        } else {
+            rc = wt3d_solver_create_csr(&g_sp, *nrows, *nnz, irptr, jcptr, 1, WT3D_PREC_MIXED);
+        }
+        if (rc != WT3D_OK) {
             printf("%s: Error reordering matrix! (%s)\n", fcnm, g_err.c_str());
             g_sp = nullptr;
             *ierr = 1;
@@ -1545,11 +1708,8 @@ void strumpack_serial_finter(int *job, int *nrows, int *nnz, int *irptr, int *jc
 // ---------------------------------------------------------------------------
 // host-only inspection of the analysis (no GPU needed)
 // ---------------------------------------------------------------------------
-extern "C" int wt3d_analyse_info(int nx, int ny, int nz, int leaf_nodes, long long *info, double *flops)
+static void analysis_info(const Symbolic &S, long long *info, double *flops)
 {
-    Symbolic S;
-    int rc = symbolic_grid(nx, ny, nz, leaf_nodes > 0 ? leaf_nodes : 64, S);
-    if (rc) return rc;
     if (info) {
         info[0] = (long long)S.fronts.size();
         info[1] = S.fac_total;
@@ -1561,15 +1721,11 @@ extern "C" int wt3d_analyse_info(int nx, int ny, int nz, int leaf_nodes, long lo
         info[7] = S.upd_size[1];
     }
     if (flops) *flops = S.flops;
-    return WT3D_OK;
 }
 
-extern "C" int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *perm, int *fp, int *fb, int *ffirst,
-                                   int *fparent, int *flevel, int *border, int *rel)
+static void analysis_export(const Symbolic &S, int *perm, int *fp, int *fb, int *ffirst, int *fparent, int *flevel,
+                            int *border, int *rel)
 {
-    Symbolic S;
-    int rc = symbolic_grid(nx, ny, nz, leaf_nodes > 0 ? leaf_nodes : 64, S);
-    if (rc) return rc;
     std::copy(S.perm.begin(), S.perm.end(), perm);
     for (size_t f = 0; f < S.fronts.size(); f++) {
         fp[f] = S.fronts[f].p;
@@ -1580,6 +1736,52 @@ extern "C" int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *
     }
     std::copy(S.border.begin(), S.border.end(), border);
     std::copy(S.rel.begin(), S.rel.end(), rel);
+}
+
+extern "C" int wt3d_analyse_info(int nx, int ny, int nz, int leaf_nodes, long long *info, double *flops)
+{
+    Symbolic S;
+    int rc = symbolic_grid(nx, ny, nz, leaf_nodes > 0 ? leaf_nodes : 64, S);
+    if (rc) return rc;
+    analysis_info(S, info, flops);
+    return WT3D_OK;
+}
+
+extern "C" int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *perm, int *fp, int *fb, int *ffirst,
+                                   int *fparent, int *flevel, int *border, int *rel)
+{
+    Symbolic S;
+    int rc = symbolic_grid(nx, ny, nz, leaf_nodes > 0 ? leaf_nodes : 64, S);
+    if (rc) return rc;
+    analysis_export(S, perm, fp, fb, ffirst, fparent, flevel, border, rel);
+    return WT3D_OK;
+}
+
+extern "C" int wt3d_analyse_csr_info(int n, long long nnz, const int *irptr, const int *jcptr, int base,
+                                     int leaf_dofs, long long *info, double *flops)
+{
+    Symbolic S;
+    int rc = check_csr(n, nnz, irptr, jcptr, base, true);
+    if (rc || (rc = symbolic_graph(n, irptr, jcptr, base, leaf_dofs > 0 ? leaf_dofs : GENERAL_LEAF_DOFS, S)))
+        return rc;
+    std::vector<long long> map;
+    std::vector<int> hir(irptr, irptr + n + 1), hjc(jcptr, jcptr + nnz);
+    for (auto &v : hir) v -= base;
+    for (auto &v : hjc) v -= base;
+    if ((rc = scatter_map(S, hir, hjc, map))) return rc;
+    analysis_info(S, info, flops);
+    return WT3D_OK;
+}
+
+extern "C" int wt3d_analyse_csr_export(int n, long long nnz, const int *irptr, const int *jcptr, int base,
+                                       int leaf_dofs, int *perm, int *fp, int *fb, int *ffirst, int *fparent,
+                                       int *flevel, int *border, int *rel)
+{
+    Symbolic S;
+    int rc = check_csr(n, nnz, irptr, jcptr, base, true);
+    if (rc || (rc = symbolic_graph(n, irptr, jcptr, base, leaf_dofs > 0 ? leaf_dofs : GENERAL_LEAF_DOFS, S)))
+        return rc;
+    analysis_export(S, perm, fp, fb, ffirst, fparent, flevel, border, rel);
     return WT3D_OK;
 }
 
@@ -1615,8 +1817,7 @@ extern "C" int wt3d_profile_solve(wt3d_solver *h, int m, double *out)
     }
     if (rc) return rc;
     cudaEventRecord(h->ev0, h->st);
-    k_residual<<<152 * 8, 256, 0, h->st>>>(h->n, m, h->irptr.p, h->jcptr.p, h->a.p, h->tpos.p, h->Xn.p, h->Bn.p,
-                                           h->Rn.p, h->norms.p, h->norms.p + MAXRHS, 0);
+    residual(h, h->st, m, h->Xn.p, h->Bn.p, h->Rn.p, false);
     cudaEventRecord(h->ev1, h->st);
     WT_CUDA(cudaStreamSynchronize(h->st));
     out[11] = ms_between(h->ev0, h->ev1);

@@ -36,8 +36,8 @@ int device_add(long long total, const void *d_a, void *d_y, cudaStream_t st);
 
 // ---- symbolic analysis (symbolic.cpp) -------------------------------------
 // Nested dissection of the nx*ny*nz grid with one-node-thick plane
-// separators, and the multifrontal symbolic factorisation of the 3-dof
-// 27-point graph in that ordering.  Fronts are listed in postorder.
+// separators (or of a general pattern's graph), and the multifrontal
+// symbolic factorisation in that ordering.  Fronts are listed in postorder.
 struct Front {
     int p = 0, b = 0;        // pivot dofs, border (update) dofs
     int first = 0;           // new index of the first pivot dof
@@ -68,6 +68,19 @@ struct Symbolic {
 };
 
 int symbolic_grid(int nx, int ny, int nz, int leaf_nodes, Symbolic &S);
+
+// Any structurally symmetric pattern (rows irptr/jcptr with index base 0 or
+// 1): automatic nested dissection on the supervariable graph, then the same
+// symbolic factorisation; leaf fronts hold at most leaf_dofs dofs.
+int symbolic_graph(long long n, const int *irptr, const int *jcptr, int base, long long leaf_dofs, Symbolic &S);
+
+// Check a CSR pattern: pointers start at the base and grow, columns in range,
+// no duplicates in a row and, if need_symmetric, structural symmetry.
+int check_csr(long long n, long long nnz, const int *irptr, const int *jcptr, int base, bool need_symmetric);
+
+// Position of the transposed entry (c, r) of every entry (r, c) of a
+// structurally symmetric 0-based pattern; columns may be in any order.
+std::vector<long long> transpose_positions(long long n, const int *irptr, const int *jcptr);
 
 // Destination of every CSR entry (0-based CSR, natural ordering) in the factor
 // pool: entry (r,c) belongs to the front holding min(new r, new c).

@@ -88,6 +88,66 @@ struct Builder {
 
 }  // namespace
 
+// Depth levels, storage offsets, flop count and the parent-front position of
+// every border dof, for fronts already listed in postorder with their pivots,
+// borders and permutation.
+static int finalize(Symbolic &S, const char *who)
+{
+    const int nf = (int)S.fronts.size();
+    // ---- levels, storage offsets, flop count ----
+    int maxlev = 0;
+    for (auto &F : S.fronts) maxlev = std::max(maxlev, F.level);
+    S.levels.assign(maxlev + 1, {});
+    for (int f = 0; f < nf; f++) S.levels[S.fronts[f].level].push_back(f);
+    long long fac = 0;
+    for (int f = 0; f < nf; f++) {
+        Front &F = S.fronts[f];
+        fac += fac & 1;   // even offsets: 16-byte-aligned complex64 fronts (TMA-addressable blocks)
+        F.fac_off = fac;
+        fac += (long long)F.p * F.nf() + (long long)F.b * F.p;
+        double p = F.p, b = F.b;
+        S.flops += 8.0 * (p * p * p / 3.0 + p * p * b + p * b * b);
+        S.max_p = std::max(S.max_p, F.p);
+        S.max_b = std::max(S.max_b, F.b);
+    }
+    S.fac_total = fac;
+    for (int l = 0; l <= maxlev; l++) {
+        long long u = 0;
+        for (int f : S.levels[l]) {
+            S.fronts[f].upd_off = u;
+            u += (long long)S.fronts[f].b * S.fronts[f].b;
+        }
+        S.upd_size[l & 1] = std::max(S.upd_size[l & 1], u);
+    }
+
+    // ---- relative positions of each border dof in the parent front ----
+    std::vector<int> pos(S.n, -1);
+    S.rel.assign(S.border.size(), -1);
+    for (int f = 0; f < nf; f++) {
+        const Front &P = S.fronts[f];
+        if (P.nchild == 0) continue;
+        for (int i = 0; i < P.p; i++) pos[P.first + i] = i;
+        for (int j = 0; j < P.b; j++) pos[S.border[P.border_off + j]] = P.p + j;
+        for (int c = 0; c < P.nchild; c++) {
+            Front &C = S.fronts[P.child[c]];
+            C.rel_off = C.border_off;
+            for (int j = 0; j < C.b; j++) {
+                int d = S.border[C.border_off + j];
+                int r = pos[d];
+                if (r < 0) {
+                    set_error(std::string(who) + ": child border entry missing from parent front");
+                    return WT3D_ERR_PATTERN;
+                }
+                S.rel[C.rel_off + j] = r;
+            }
+        }
+        for (int i = 0; i < P.p; i++) pos[P.first + i] = -1;
+        for (int j = 0; j < P.b; j++) pos[S.border[P.border_off + j]] = -1;
+    }
+    return WT3D_OK;
+}
+
+
 int symbolic_grid(int nx, int ny, int nz, int leaf_nodes, Symbolic &S)
 {
     if (nx < 2 || ny < 2 || nz < 2) {
@@ -158,57 +218,386 @@ int symbolic_grid(int nx, int ny, int nz, int leaf_nodes, Symbolic &S)
         }
     }
 
-    // ---- levels, storage offsets, flop count ----
-    int maxlev = 0;
-    for (auto &F : S.fronts) maxlev = std::max(maxlev, F.level);
-    S.levels.assign(maxlev + 1, {});
-    for (int f = 0; f < nf; f++) S.levels[S.fronts[f].level].push_back(f);
-    long long fac = 0;
-    for (int f = 0; f < nf; f++) {
-        Front &F = S.fronts[f];
-        fac += fac & 1;   // even offsets: 16-byte-aligned complex64 fronts (TMA-addressable blocks)
-        F.fac_off = fac;
-        fac += (long long)F.p * F.nf() + (long long)F.b * F.p;
-        double p = F.p, b = F.b;
-        S.flops += 8.0 * (p * p * p / 3.0 + p * p * b + p * b * b);
-        S.max_p = std::max(S.max_p, F.p);
-        S.max_b = std::max(S.max_b, F.b);
-    }
-    S.fac_total = fac;
-    for (int l = 0; l <= maxlev; l++) {
-        long long u = 0;
-        for (int f : S.levels[l]) {
-            S.fronts[f].upd_off = u;
-            u += (long long)S.fronts[f].b * S.fronts[f].b;
-        }
-        S.upd_size[l & 1] = std::max(S.upd_size[l & 1], u);
+    return finalize(S, "symbolic_grid");
+}
+
+// ---------------------------------------------------------------------------
+// General structurally symmetric patterns
+// ---------------------------------------------------------------------------
+// STRUMPACK accepts any CSR pattern (strumpack_finter.c:42-48 hands it to a
+// nested-dissection reordering).  A pattern that is not the grid graph is
+// ordered here by automatic nested dissection (George and Liu, Computer
+// Solution of Large Sparse Positive Definite Systems, 1981, ch. 8): the
+// separator of a connected subgraph is one level of a breadth-first level
+// structure rooted at a pseudo-peripheral vertex, the smallest level that
+// leaves at least a fifth of the weight on either side, thinned to the
+// vertices that touch both sides.  A disconnected subgraph is split between
+// its components, and one vertex of the second group becomes the (trivial)
+// separator.  The graph is first compressed to supervariables, runs of
+// consecutive rows with the same column set (the 3 dofs of an elastic node),
+// so fronts never split a node.
+namespace {
+
+struct GraphND {
+    int nv = 0;                      // supervariables
+    std::vector<long long> xadj;     // quotient graph, no self loops
+    std::vector<int> adj;
+    std::vector<int> wt;             // dofs per supervariable
+    std::vector<int> first_dof;      // first (old) dof of each supervariable
+    long long leaf = 0;              // leaf fronts hold at most this many dofs
+    Symbolic &S;
+    std::vector<int> part;           // subset id of each vertex; -1 once numbered
+    std::vector<int> lev;            // breadth-first level of each vertex
+    std::vector<long long> seen;     // stamp of the last search that reached each vertex
+    long long stamp = 0;
+    int next_part = 1;
+    std::vector<std::vector<int>> snodes;   // per front: supervariables, in numbering order
+    static constexpr int MAXDEPTH = 256;
+
+    explicit GraphND(Symbolic &s) : S(s) {}
+
+    int degree(int v, int pid) const
+    {
+        int d = 0;
+        for (long long k = xadj[v]; k < xadj[v + 1]; k++) d += part[adj[k]] == pid;
+        return d;
     }
 
-    // ---- relative positions of each border dof in the parent front ----
-    std::vector<int> pos(S.n, -1);
-    S.rel.assign(S.border.size(), -1);
-    for (int f = 0; f < nf; f++) {
-        const Front &P = S.fronts[f];
-        if (P.nchild == 0) continue;
-        for (int i = 0; i < P.p; i++) pos[P.first + i] = i;
-        for (int j = 0; j < P.b; j++) pos[S.border[P.border_off + j]] = P.p + j;
-        for (int c = 0; c < P.nchild; c++) {
-            Front &C = S.fronts[P.child[c]];
-            C.rel_off = C.border_off;
-            for (int j = 0; j < C.b; j++) {
-                int d = S.border[C.border_off + j];
-                int r = pos[d];
-                if (r < 0) {
-                    set_error("symbolic_grid: child border entry missing from parent front");
-                    return WT3D_ERR_PATTERN;
+    // Level structure of the component of `root` inside subset pid: fills
+    // `levels` (vertex lists); returns the number of levels.
+    int bfs(int root, int pid, std::vector<std::vector<int>> &levels)
+    {
+        stamp++;
+        levels.assign(1, std::vector<int>{root});
+        seen[root] = stamp;
+        lev[root] = 0;
+        for (int l = 0;; l++) {
+            std::vector<int> nxt;
+            for (int v : levels[l])
+                for (long long k = xadj[v]; k < xadj[v + 1]; k++) {
+                    int u = adj[k];
+                    if (part[u] != pid || seen[u] == stamp) continue;
+                    seen[u] = stamp;
+                    lev[u] = l + 1;
+                    nxt.push_back(u);
                 }
-                S.rel[C.rel_off + j] = r;
-            }
+            if (nxt.empty()) break;
+            levels.push_back(std::move(nxt));
         }
-        for (int i = 0; i < P.p; i++) pos[P.first + i] = -1;
-        for (int j = 0; j < P.b; j++) pos[S.border[P.border_off + j]] = -1;
+        return (int)levels.size();
+    }
+
+    long long weight(const std::vector<int> &vs) const
+    {
+        long long w = 0;
+        for (int v : vs) w += wt[v];
+        return w;
+    }
+
+    int min_degree_vertex(const std::vector<int> &vs, int pid) const
+    {
+        int best = vs[0], bd = degree(vs[0], pid);
+        for (int v : vs) {
+            int d = degree(v, pid);
+            if (d < bd) { bd = d; best = v; }
+        }
+        return best;
+    }
+
+    // Split subset pid (vertices vs, weight W) into sep, s1, s2 with no edge
+    // between s1 and s2; false if no useful split exists.
+    bool split(const std::vector<int> &vs, int pid, long long W, std::vector<int> &sep, std::vector<int> &s1,
+               std::vector<int> &s2)
+    {
+        std::vector<std::vector<int>> L;
+        int root = min_degree_vertex(vs, pid);
+        int nl = bfs(root, pid, L);
+        long long reached = 0;
+        for (auto &l : L) reached += weight(l);
+        if (reached < W) {
+            // disconnected: components, heaviest first, to the lighter group.
+            // Stamps only grow, so seen[v] >= s0 marks the vertices reached
+            // by this split's searches.
+            const long long s0 = stamp;
+            std::vector<std::vector<int>> comps(1);
+            for (auto &l : L) comps[0].insert(comps[0].end(), l.begin(), l.end());
+            for (int v : vs) {
+                if (seen[v] >= s0) continue;
+                std::vector<std::vector<int>> Lc;
+                bfs(v, pid, Lc);
+                std::vector<int> c;
+                for (auto &l : Lc) c.insert(c.end(), l.begin(), l.end());
+                comps.push_back(std::move(c));
+            }
+            std::sort(comps.begin(), comps.end(),
+                      [&](const std::vector<int> &a, const std::vector<int> &b) { return weight(a) > weight(b); });
+            std::vector<int> A, B;
+            long long wa = 0, wb = 0;
+            for (auto &c : comps) {
+                long long w = weight(c);
+                if (wa <= wb) { A.insert(A.end(), c.begin(), c.end()); wa += w; }
+                else { B.insert(B.end(), c.begin(), c.end()); wb += w; }
+            }
+            if (B.size() < 2) std::swap(A, B);
+            if (B.size() < 2) return false;   // two single supervariables heavier than a leaf
+            int v = min_degree_vertex(B, pid);
+            sep.assign(1, v);
+            s1 = std::move(A);
+            for (int u : B)
+                if (u != v) s2.push_back(u);
+            return true;
+        }
+        // pseudo-peripheral root: restart from a minimum-degree vertex of the
+        // last level while the level structure gets deeper
+        for (int it = 0; it < 8; it++) {
+            int u = min_degree_vertex(L.back(), pid);
+            std::vector<std::vector<int>> L2;
+            int nl2 = bfs(u, pid, L2);
+            if (nl2 <= nl) { bfs(root, pid, L); break; }
+            root = u;
+            nl = nl2;
+            L.swap(L2);
+        }
+        if (nl < 3) return false;   // diameter < 2: nothing to separate
+        std::vector<long long> lw(nl), cw(nl + 1, 0);
+        for (int l = 0; l < nl; l++) { lw[l] = weight(L[l]); cw[l + 1] = cw[l] + lw[l]; }
+        int s = -1;
+        long long best_side = -1;
+        for (int l = 1; l < nl - 1; l++) {
+            long long side = std::min(cw[l], W - cw[l + 1]);
+            if (5 * side < W) continue;
+            if (s < 0 || lw[l] < lw[s] || (lw[l] == lw[s] && side > best_side)) { s = l; best_side = side; }
+        }
+        if (s < 0)
+            for (int l = 1; l < nl - 1; l++) {
+                long long side = std::min(cw[l], W - cw[l + 1]);
+                if (side > best_side) { s = l; best_side = side; }
+            }
+        // thin the level: drop the vertices that touch only one side
+        auto touches = [&](int v, bool later) {
+            for (long long k = xadj[v]; k < xadj[v + 1]; k++) {
+                int u = adj[k];
+                if (part[u] == pid && (later ? lev[u] > s : lev[u] < s)) return true;
+            }
+            return false;
+        };
+        std::vector<int> keepA, movA, keepB, movB;
+        for (int v : L[s]) {
+            (touches(v, true) ? keepA : movA).push_back(v);
+            (touches(v, false) ? keepB : movB).push_back(v);
+        }
+        const bool useA = weight(keepA) <= weight(keepB);
+        sep = useA ? keepA : keepB;
+        for (int l = 0; l < s; l++) s1.insert(s1.end(), L[l].begin(), L[l].end());
+        for (int l = s + 1; l < nl; l++) s2.insert(s2.end(), L[l].begin(), L[l].end());
+        if (useA) s1.insert(s1.end(), movA.begin(), movA.end());
+        else s2.insert(s2.end(), movB.begin(), movB.end());
+        return !sep.empty() && !s1.empty() && !s2.empty();
+    }
+
+    int build(std::vector<int> vs, int pid, int depth)
+    {
+        const long long W = weight(vs);
+        Front f;
+        f.level = depth;
+        std::vector<int> nodes, s1, s2;
+        if (W > leaf && depth < MAXDEPTH && split(vs, pid, W, nodes, s1, s2)) {
+            const int p1 = next_part++, p2 = next_part++;
+            for (int v : s1) part[v] = p1;
+            for (int v : s2) part[v] = p2;
+            for (int v : nodes) part[v] = -1;
+            std::vector<int>().swap(vs);
+            f.child[0] = build(std::move(s1), p1, depth + 1);
+            f.child[1] = build(std::move(s2), p2, depth + 1);
+            f.nchild = 2;
+        } else {
+            nodes = std::move(vs);
+            for (int v : nodes) part[v] = -1;
+        }
+        const int id = (int)S.fronts.size();
+        for (int c = 0; c < f.nchild; c++) S.fronts[f.child[c]].parent = id;
+        S.fronts.push_back(f);
+        snodes.push_back(std::move(nodes));
+        return id;
+    }
+};
+
+}  // namespace
+
+int check_csr(long long n, long long nnz, const int *irptr, const int *jcptr, int base, bool need_symmetric)
+{
+    if (n < 1 || n >= (1LL << 31) || nnz < 0 || nnz >= (1LL << 31) || !irptr || (nnz > 0 && !jcptr) ||
+        (base != 0 && base != 1)) {
+        set_error("CSR: bad sizes, pointers or index base");
+        return WT3D_ERR_ARG;
+    }
+    if (irptr[0] != base || (long long)irptr[n] - base != nnz) {
+        set_error("CSR: row pointers do not start at the index base or do not end at nnz");
+        return WT3D_ERR_PATTERN;
+    }
+    std::vector<int> mark(n, -1), cnt(n, 0);
+    for (long long r = 0; r < n; r++) {
+        if (irptr[r + 1] < irptr[r]) { set_error("CSR: row pointers decrease"); return WT3D_ERR_PATTERN; }
+        for (long long k = irptr[r] - base; k < irptr[r + 1] - base; k++) {
+            long long c = (long long)jcptr[k] - base;
+            if (c < 0 || c >= n) { set_error("CSR: column index out of range"); return WT3D_ERR_PATTERN; }
+            if (mark[c] == r) { set_error("CSR: duplicate entry in a row"); return WT3D_ERR_PATTERN; }
+            mark[c] = (int)r;
+            cnt[c]++;
+        }
+    }
+    if (!need_symmetric) return WT3D_OK;
+    // structural symmetry: column c holds as many entries as row c, and every
+    // (r, c) has its (c, r)
+    for (long long r = 0; r < n; r++)
+        if (cnt[r] != irptr[r + 1] - irptr[r]) { set_error("CSR: pattern is not structurally symmetric"); return WT3D_ERR_PATTERN; }
+    std::vector<long long> tptr(n + 1, 0);
+    for (long long r = 0; r < n; r++) tptr[r + 1] = tptr[r] + cnt[r];
+    std::vector<int> trow(nnz);
+    {
+        std::vector<long long> cur(tptr.begin(), tptr.end() - 1);
+        for (long long r = 0; r < n; r++)
+            for (long long k = irptr[r] - base; k < irptr[r + 1] - base; k++) trow[cur[jcptr[k] - base]++] = (int)r;
+    }
+    std::fill(mark.begin(), mark.end(), -1);
+    for (long long r = 0; r < n; r++) {
+        for (long long k = irptr[r] - base; k < irptr[r + 1] - base; k++) mark[jcptr[k] - base] = (int)r;
+        for (long long k = tptr[r]; k < tptr[r + 1]; k++)
+            if (mark[trow[k]] != r) { set_error("CSR: pattern is not structurally symmetric"); return WT3D_ERR_PATTERN; }
     }
     return WT3D_OK;
+}
+
+int symbolic_graph(long long n, const int *irptr, const int *jcptr, int base, long long leaf_dofs, Symbolic &S)
+{
+    if (n < 1 || !irptr) { set_error("symbolic_graph: empty matrix or null row pointers"); return WT3D_ERR_ARG; }
+    int rc = check_csr(n, (long long)irptr[n] - base, irptr, jcptr, base, true);
+    if (rc) return rc;
+    S = Symbolic();
+    S.n = n;
+    S.nnodes = 0;
+    GraphND G(S);
+    G.leaf = std::max(1LL, leaf_dofs);
+    // ---- supervariables: runs of consecutive rows with equal column sets ----
+    std::vector<int> sv_of(n), mark(n, -1);
+    for (long long r = 0; r < n; r++) {
+        bool same = false;
+        if (r > 0) {
+            const long long len = irptr[r + 1] - irptr[r], plen = irptr[r] - irptr[r - 1];
+            if (len == plen) {
+                for (long long k = irptr[r - 1] - base; k < irptr[r] - base; k++) mark[jcptr[k] - base] = (int)r;
+                same = true;
+                for (long long k = irptr[r] - base; k < irptr[r + 1] - base && same; k++)
+                    same = mark[jcptr[k] - base] == (int)r;
+            }
+        }
+        if (same) {
+            sv_of[r] = G.nv - 1;
+            G.wt[G.nv - 1]++;
+        } else {
+            sv_of[r] = G.nv++;
+            G.wt.push_back(1);
+            G.first_dof.push_back((int)r);
+        }
+    }
+    // ---- quotient graph ----
+    G.xadj.assign(G.nv + 1, 0);
+    std::vector<int> smark(G.nv, -1);
+    for (int v = 0; v < G.nv; v++) {
+        const long long r = G.first_dof[v];
+        smark[v] = v;
+        for (long long k = irptr[r] - base; k < irptr[r + 1] - base; k++) {
+            const int u = sv_of[jcptr[k] - base];
+            if (smark[u] == v) continue;
+            smark[u] = v;
+            G.adj.push_back(u);
+        }
+        G.xadj[v + 1] = (long long)G.adj.size();
+    }
+    S.nnodes = G.nv;
+    // ---- nested dissection ----
+    G.part.assign(G.nv, 0);
+    G.lev.assign(G.nv, 0);
+    G.seen.assign(G.nv, 0);
+    std::vector<int> all(G.nv);
+    for (int v = 0; v < G.nv; v++) all[v] = v;
+    G.build(std::move(all), 0, 0);
+    const int nf = (int)S.fronts.size();
+    // ---- numbering: fronts in postorder, supervariables in list order ----
+    std::vector<int> newsv(G.nv), dof0(G.nv);
+    {
+        int q = 0;
+        long long d = 0;
+        for (int f = 0; f < nf; f++) {
+            Front &F = S.fronts[f];
+            F.first = (int)d;
+            for (int v : G.snodes[f]) { newsv[v] = q++; dof0[v] = (int)d; d += G.wt[v]; }
+            F.p = (int)(d - F.first);
+        }
+    }
+    std::vector<int> sv_new(G.nv);   // new supervariable index -> supervariable
+    for (int v = 0; v < G.nv; v++) sv_new[newsv[v]] = v;
+    // ---- borders: struct on supervariables, children before parents ----
+    std::vector<std::vector<int>> sn_struct(nf);
+    std::fill(smark.begin(), smark.end(), -1);
+    for (int f = 0; f < nf; f++) {
+        Front &F = S.fronts[f];
+        const int last_new = newsv[G.snodes[f].back()];
+        std::vector<int> st;
+        auto add = [&](int nw) {
+            if (nw > last_new && smark[nw] != f) { smark[nw] = f; st.push_back(nw); }
+        };
+        for (int v : G.snodes[f])
+            for (long long k = G.xadj[v]; k < G.xadj[v + 1]; k++) add(newsv[G.adj[k]]);
+        for (int c = 0; c < F.nchild; c++) {
+            for (int w : sn_struct[F.child[c]]) add(w);
+            std::vector<int>().swap(sn_struct[F.child[c]]);
+        }
+        std::sort(st.begin(), st.end());
+        F.border_off = (long long)S.border.size();
+        for (int w : st) {
+            const int v = sv_new[w];
+            for (int q = 0; q < G.wt[v]; q++) S.border.push_back(dof0[v] + q);
+        }
+        F.b = (int)((long long)S.border.size() - F.border_off);
+        sn_struct[f] = std::move(st);
+    }
+    // ---- permutation ----
+    S.perm.resize(n);
+    S.iperm.resize(n);
+    for (int v = 0; v < G.nv; v++)
+        for (int q = 0; q < G.wt[v]; q++) {
+            S.perm[dof0[v] + q] = G.first_dof[v] + q;
+            S.iperm[G.first_dof[v] + q] = dof0[v] + q;
+        }
+    return finalize(S, "symbolic_graph");
+}
+
+std::vector<long long> transpose_positions(long long n, const int *irptr, const int *jcptr)
+{
+    // Rows are walked in increasing order, so the t-th entry to reach column c
+    // comes from the t-th smallest row holding c, whose transpose (c, r) is
+    // the t-th entry of row c in column order.
+    const long long nnz = irptr[n];
+    std::vector<int> srt(nnz);   // per row: entry offsets in column order
+    for (long long r = 0; r < n; r++) {
+        const long long k0 = irptr[r], k1 = irptr[r + 1];
+        bool sorted = true;
+        for (long long k = k0; k < k1; k++) {
+            srt[k] = (int)(k - k0);
+            if (k > k0 && jcptr[k] < jcptr[k - 1]) sorted = false;
+        }
+        if (!sorted)
+            std::sort(srt.begin() + k0, srt.begin() + k1,
+                      [&](int x, int y) { return jcptr[k0 + x] < jcptr[k0 + y]; });
+    }
+    std::vector<long long> cur(irptr, irptr + n), tp(nnz);
+    for (long long r = 0; r < n; r++)
+        for (long long k = irptr[r]; k < irptr[r + 1]; k++) {
+            const int c = jcptr[k];
+            tp[k] = irptr[c] + srt[cur[c]++];
+        }
+    return tp;
 }
 
 int scatter_map(const Symbolic &S, const std::vector<int> &irptr, const std::vector<int> &jcptr,
@@ -218,13 +607,7 @@ int scatter_map(const Symbolic &S, const std::vector<int> &irptr, const std::vec
     const long long nnz = irptr[n];
     map.assign(nnz, -1);
     // transposed position of every entry (structurally symmetric pattern)
-    std::vector<long long> tpos(nnz);
-    {
-        std::vector<long long> cur(n);
-        for (long long r = 0; r < n; r++) cur[r] = irptr[r];
-        for (long long r = 0; r < n; r++)
-            for (long long k = irptr[r]; k < irptr[r + 1]; k++) tpos[k] = cur[jcptr[k]]++;
-    }
+    const std::vector<long long> tpos = transpose_positions(n, irptr.data(), jcptr.data());
     std::vector<int> pos(n, -1);
     for (size_t f = 0; f < S.fronts.size(); f++) {
         const Front &F = S.fronts[f];
