@@ -25,7 +25,7 @@ extern "C" {
 #define WT3D_ERR_CUDA          2   /* CUDA runtime error                      */
 #define WT3D_ERR_NOMEM         3   /* device or host allocation failed        */
 #define WT3D_ERR_STATE         4   /* call out of order (no model, no factor) */
-#define WT3D_ERR_PATTERN       5   /* CSR pattern malformed or not symmetric  */
+#define WT3D_ERR_PATTERN       5   /* CSR pattern malformed                   */
 #define WT3D_ERR_NOCONV        6   /* refinement did not reach the tolerance  */
 #define WT3D_ERR_NOGPU         7   /* no CUDA device                          */
 
@@ -57,8 +57,8 @@ typedef struct wt3d_grid {
  * *ierr = 0 on success, 1 on error (with a message on stdout), as the
  * reference.  irptr/jcptr are read, never modified.  The 27-point, 3-dof grid
  * graph built by srel3d + SPARSE_ADJ2CRS is recognised (the grid is recovered
- * from it and ordered by plane separators); any other structurally symmetric
- * pattern is ordered as wt3d_solver_create_csr does.  Factorisation is
+ * from it and ordered by plane separators); any other pattern is ordered as
+ * wt3d_solver_create_csr does.  Factorisation is
  * complex64 with FP64 iterative
  * refinement; the solution is returned in complex64 as the reference does.
  * Not re-entrant (one global instance, like the reference). */
@@ -123,16 +123,17 @@ typedef struct wt3d_solver wt3d_solver;
 int wt3d_solver_create(wt3d_solver **h, const wt3d_grid *g, int precision);
 int wt3d_solver_destroy(wt3d_solver *h);
 
-/* Analyse any structurally symmetric CSR pattern (n rows, nnz entries,
- * index base 0 or 1, columns in any order, no duplicates), as STRUMPACK's
- * reordering does for the job-1 pattern (strumpack_finter.c:42-48): automatic
- * nested dissection (level-structure separators) on the graph of
- * supervariables (runs of consecutive rows with equal column sets), then the
- * same multifrontal symbolic factorisation and device storage as the grid.
- * The handle takes values with wt3d_set_values_c64 / _c128 in this CSR order
- * and solves with wt3d_solve*, wt3d_apply*; the entry points that need the
- * grid (model, sources, receivers, gradient) return WT3D_ERR_STATE.  A
- * pattern that is not structurally symmetric returns WT3D_ERR_PATTERN. */
+/* Analyse any CSR pattern (n rows, nnz >= 1 entries, index base 0 or 1,
+ * columns in any order, no duplicates), as STRUMPACK's reordering does for
+ * the job-1 pattern (strumpack_finter.c:42-48): an unsymmetric pattern is
+ * stored as the pattern of A + A^T (the added entries hold zeros), then
+ * ordered by automatic nested dissection (level-structure separators) on the
+ * graph of supervariables (runs of consecutive rows with equal column sets),
+ * with the same multifrontal symbolic factorisation and device storage as
+ * the grid.  The handle takes values with wt3d_set_values_c64 / _c128 in the
+ * caller's CSR order and solves with wt3d_solve*, wt3d_apply*; the entry
+ * points that need the grid (model, sources, receivers, gradient) return
+ * WT3D_ERR_STATE.  A malformed pattern returns WT3D_ERR_PATTERN. */
 int wt3d_solver_create_csr(wt3d_solver **h, int n, long long nnz, const int *irptr, const int *jcptr, int base,
                            int precision);
 

@@ -64,18 +64,17 @@ def test_job_protocol_order_errors():
     assert wt.strumpack_serial_finter(-1, n, nnz, ir, jc, a, b, x) == 0
 
 
-def test_job1_rejects_unsymmetric_pattern():
-    """Job 1 takes the grid graph or any structurally symmetric pattern; a
-    pattern with (i, i+1) but not (i+1, i) is refused on the host, before
-    any device work."""
+def test_job1_rejects_malformed_pattern():
+    """Job 1 takes the grid graph or any well-formed pattern; a row that lists
+    a column twice is refused on the host, before any device work."""
     n = 24
-    rows = [[j for j in (i, i + 1) if j < n] for i in range(n)]
+    rows = [[j for j in (i, i + 1) if j < n] + [i] for i in range(n)]
     ir = np.cumsum([1] + [len(r) for r in rows]).astype(np.int32)
     jc = (np.concatenate(rows) + 1).astype(np.int32)
     a = np.ones(len(jc), np.complex64)
     b = np.zeros(n, np.complex64)
     assert wt.strumpack_serial_finter(1, n, len(jc), ir, jc, a, b, b.copy()) == 1
-    assert "structurally symmetric" in wt.lib().wt3d_last_error().decode()
+    assert "duplicate" in wt.lib().wt3d_last_error().decode()
 
 
 def test_too_large_grid_is_rejected_before_any_device_work():

@@ -133,8 +133,42 @@ def test_grid_only_calls_refuse_a_general_handle():
                 wt._check(call())
             assert e.value.code == wt.WT3D_ERR_STATE
     with pytest.raises(wt.WT3DError) as e:
-        wt.Solver.from_csr([0, 2, 3], [0, 1, 1])     # not structurally symmetric
+        wt.Solver.from_csr([0, 2, 3], [0, 0, 1])     # duplicate entry
     assert e.value.code == wt.WT3D_ERR_PATTERN
+
+
+def test_unsymmetric_pattern_handle_and_job_protocol():
+    """An unsymmetric pattern (upwinded convection-diffusion) is stored as
+    A + A^T with zeros in the added entries: the handle in both precisions
+    and the job protocol (1-based, complex64) solve it like SuperLU."""
+    from test_symbolic import convection_diffusion
+    A = convection_diffusion(60, seed=3)
+    n = A.shape[0]
+    B0 = rhs(n, 2, 6)
+    Xr = spla.spsolve(A.tocsc(), B0)
+    for prec in (wt.PREC_MIXED, wt.PREC_FP64):
+        with wt.Solver.from_csr(A.indptr, A.indices, prec) as s:
+            s.set_values(A.data, np.complex128)
+            X = s.solve(B0, tol=1e-10)
+            Y = s.apply(X)
+            assert s.stats()["nnz"] == ((A + A.T) != 0).sum()
+        assert np.linalg.norm(X - Xr) / np.linalg.norm(Xr) <= 1e-8
+        np.testing.assert_allclose(Y, A @ X, rtol=0, atol=1e-12 * np.abs(A @ X).max())
+    ir = (A.indptr + 1).astype(np.int32)
+    jc = (A.indices + 1).astype(np.int32)
+    a = A.data.astype(np.complex64)
+    dummy = np.zeros(n, np.complex64)
+    assert wt.strumpack_serial_finter(1, n, A.nnz, ir, jc, a, dummy, dummy.copy()) == 0
+    try:
+        assert wt.strumpack_serial_finter(2, n, A.nnz, ir, jc, a, dummy, dummy.copy()) == 0
+        b = B0[:, 0].astype(np.complex64)
+        sol = np.zeros(n, np.complex64)
+        assert wt.strumpack_serial_finter(3, n, A.nnz, ir, jc, a, b, sol) == 0
+        A64 = A.astype(np.complex64).astype(np.complex128)
+        xr = spla.spsolve(A64.tocsc(), b.astype(np.complex128))
+        assert np.linalg.norm(sol - xr) / np.linalg.norm(xr) <= 1e-6
+    finally:
+        assert wt.strumpack_serial_finter(-1, n, A.nnz, ir, jc, a, dummy, dummy.copy()) == 0
 
 
 def test_job_protocol_with_a_permuted_operator(oracle):

@@ -314,11 +314,33 @@ def test_general_long_path_is_balanced():
     assert levels <= 20 and maxp <= 64 and maxb <= 2 * levels
 
 
+def convection_diffusion(n1, seed=0):
+    """Upwinded 2-D convection-diffusion: each unknown couples to its west
+    and south neighbours and to its east neighbour only on even rows, so the
+    pattern is not structurally symmetric."""
+    rng = np.random.default_rng(seed)
+    rows, cols, vals = [], [], []
+    for j in range(n1):
+        for i in range(n1):
+            r = i + n1 * j
+            rows.append(r); cols.append(r); vals.append(4.0 + rng.random() + 1j * rng.random())
+            if i > 0:
+                rows.append(r); cols.append(r - 1); vals.append(-1.0 - 0.5 * rng.random())
+            if j > 0:
+                rows.append(r); cols.append(r - n1); vals.append(-1.0 - 0.5 * rng.random())
+            if i < n1 - 1 and j % 2 == 0:
+                rows.append(r); cols.append(r + 1); vals.append(-0.3 + 0.1j)
+    return sp.csr_matrix((vals, (rows, cols)), shape=(n1 * n1, n1 * n1))
+
+
+def test_general_unsymmetric_pattern():
+    """An unsymmetric pattern is ordered through A + A^T, as STRUMPACK does."""
+    A = convection_diffusion(24)
+    assert (A != 0).sum() != ((A + A.T) != 0).sum()
+    general_case(A, leaf=20)
+
+
 def test_general_bad_patterns_are_rejected():
-    # (0,1) without (1,0): not structurally symmetric
-    with pytest.raises(wt.WT3DError) as e:
-        wt.analyse_csr([0, 2, 3], [0, 1, 1])
-    assert e.value.code == wt.WT3D_ERR_PATTERN
     # duplicate column in a row
     with pytest.raises(wt.WT3DError) as e:
         wt.analyse_csr([0, 2, 3], [0, 0, 1])

@@ -353,6 +353,22 @@ __global__ void k_c64_to_c128(long long n, const float2 *__restrict__ s, double2
     if (i < n) d[i] = make_double2(s[i].x, s[i].y);
 }
 
+// Values of an unsymmetric caller pattern into the stored A + A^T pattern
+// (its other entries are zero): d[map[i]] = s[i].
+__global__ void k_spread_c64(long long n, const float2 *__restrict__ s, const int *__restrict__ map,
+                             double2 *__restrict__ d)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[map[i]] = make_double2(s[i].x, s[i].y);
+}
+
+__global__ void k_spread_c128(long long n, const double2 *__restrict__ s, const int *__restrict__ map,
+                              double2 *__restrict__ d)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[map[i]] = s[i];
+}
+
 }  // namespace wt3d
 
 using namespace wt3d;
@@ -378,8 +394,10 @@ struct wt3d_solver {
     int prec = WT3D_PREC_MIXED;
     bool general = false;                 // caller's pattern (wt3d_solver_create_csr), not the grid graph
     std::shared_ptr<GridAnalysis> ga;
-    long long n = 0, nnz = 0;
+    long long n = 0, nnz = 0;             // the (symmetrised) pattern the handle stores
+    long long nnz_in = 0;                 // entries of the caller's pattern
     DevVec<int> irptr, jcptr, tpos, perm;
+    DevVec<int> vmap;                     // caller entry -> stored entry (unsymmetric patterns only)
     DevVec<double2> a;
     DevVec<double2> da, mu;
     DevVec<double> ro;
@@ -809,7 +827,7 @@ void handle_bytes(const Symbolic &S, long long nnz, int prec, double *out)
 double own_bytes(const wt3d_solver *h)
 {
     double b = (double)(h->e32 ? h->e32->device_bytes() : h->e64->device_bytes());
-    b += (double)(h->irptr.n + h->jcptr.n + h->tpos.n + h->perm.n) * 4;
+    b += (double)(h->irptr.n + h->jcptr.n + h->tpos.n + h->perm.n + h->vmap.n) * 4;
     b += (double)(h->a.n + h->da.n + h->mu.n + h->Bn.n + h->Xn.n + h->Rn.n + h->T1.n + h->abg.n + h->bgda.n +
                   h->bgmu.n + h->batF.n + h->batX.n) * 16;
     b += (double)(h->ro.n + h->bgro.n + h->norms.n + h->gscr.n) * 8 +
@@ -1032,8 +1050,9 @@ int wt3d_solver_create_csr(wt3d_solver **out, int n, long long nnz, const int *i
     if (!out) { set_error("null handle pointer"); return WT3D_ERR_ARG; }
     *out = nullptr;
     if (precision != WT3D_PREC_MIXED && precision != WT3D_PREC_FP64) { set_error("bad precision"); return WT3D_ERR_ARG; }
-    int rc = check_csr(n, nnz, irptr, jcptr, base, true);
+    int rc = check_csr(n, nnz, irptr, jcptr, base, false);
     if (rc) return rc;
+    if (nnz == 0) { set_error("CSR: the matrix has no entries"); return WT3D_ERR_PATTERN; }
     if ((rc = have_gpu())) return rc;
     auto t0 = std::chrono::steady_clock::now();
     std::unique_ptr<wt3d_solver> h(new wt3d_solver());
@@ -1041,16 +1060,17 @@ int wt3d_solver_create_csr(wt3d_solver **out, int n, long long nnz, const int *i
     h->prec = precision;
     h->ga = std::make_shared<GridAnalysis>();
     GridAnalysis &ga = *h->ga;
-    if ((rc = symbolic_graph(n, irptr, jcptr, base, GENERAL_LEAF_DOFS, ga.sym))) return rc;
+    std::vector<int> hir, hjc, vmap;
+    if ((rc = symmetrize(n, irptr, jcptr, base, hir, hjc, vmap))) return rc;
+    if ((rc = symbolic_graph(n, hir.data(), hjc.data(), 0, GENERAL_LEAF_DOFS, ga.sym))) return rc;
     h->n = n;
-    h->nnz = nnz;
-    std::vector<int> hir(irptr, irptr + n + 1), hjc(jcptr, jcptr + nnz);
-    for (auto &v : hir) v -= base;
-    for (auto &v : hjc) v -= base;
+    h->nnz = (long long)hjc.size();
+    h->nnz_in = nnz;
     if ((rc = scatter_map(ga.sym, hir, hjc, ga.map))) return rc;
     ga.tpos = to_int(transpose_positions(n, hir.data(), hjc.data()));
     if ((rc = handle_streams(h.get()))) return rc;
-    if ((rc = h->irptr.upload(hir)) || (rc = h->jcptr.upload(hjc)) || (rc = h->a.alloc(nnz))) return rc;
+    if ((rc = h->irptr.upload(hir)) || (rc = h->jcptr.upload(hjc)) || (rc = h->a.alloc(h->nnz))) return rc;
+    if (!vmap.empty() && (rc = h->vmap.upload(vmap))) return rc;
     std::shared_ptr<FactorWorkspace<float>> w32;
     std::shared_ptr<FactorWorkspace<double>> w64;
     if (precision == WT3D_PREC_MIXED) w32 = pick_workspace(ga.ws32);
@@ -1241,11 +1261,17 @@ int wt3d_rhs_planewave(wt3d_solver *h, const wt3d_layered1d *m, int nsrc, const 
 int wt3d_set_values_c64(wt3d_solver *h, const float _Complex *a)
 {
     if (!h || !a) { set_error("null pointer"); return WT3D_ERR_ARG; }
+    const long long nin = h->vmap.p ? h->nnz_in : h->nnz;   // caller entries
     StreamBuf<float2> tmp;   // per-call, in stream order (see StreamBuf)
-    int rc = tmp.alloc(h->nnz, h->st);
+    int rc = tmp.alloc(nin, h->st);
     if (rc) return rc;
-    WT_CUDA(cudaMemcpyAsync(tmp.p, a, sizeof(float2) * h->nnz, cudaMemcpyHostToDevice, h->st));
-    k_c64_to_c128<<<ceil_div(h->nnz, 256), 256, 0, h->st>>>(h->nnz, tmp.p, h->a.p);
+    WT_CUDA(cudaMemcpyAsync(tmp.p, a, sizeof(float2) * nin, cudaMemcpyHostToDevice, h->st));
+    if (h->vmap.p) {
+        WT_CUDA(cudaMemsetAsync(h->a.p, 0, sizeof(double2) * h->nnz, h->st));
+        k_spread_c64<<<ceil_div(nin, 256), 256, 0, h->st>>>(nin, tmp.p, h->vmap.p, h->a.p);
+    } else {
+        k_c64_to_c128<<<ceil_div(nin, 256), 256, 0, h->st>>>(nin, tmp.p, h->a.p);
+    }
     WT_CUDA(cudaStreamSynchronize(h->st));
     h->have_values = true;
     h->have_factor = false;
@@ -1255,7 +1281,16 @@ int wt3d_set_values_c64(wt3d_solver *h, const float _Complex *a)
 int wt3d_set_values_c128(wt3d_solver *h, const double _Complex *a)
 {
     if (!h || !a) { set_error("null pointer"); return WT3D_ERR_ARG; }
-    WT_CUDA(cudaMemcpyAsync(h->a.p, a, sizeof(double2) * h->nnz, cudaMemcpyHostToDevice, h->st));
+    if (h->vmap.p) {
+        StreamBuf<double2> tmp;
+        int rc = tmp.alloc(h->nnz_in, h->st);
+        if (rc) return rc;
+        WT_CUDA(cudaMemcpyAsync(tmp.p, a, sizeof(double2) * h->nnz_in, cudaMemcpyHostToDevice, h->st));
+        WT_CUDA(cudaMemsetAsync(h->a.p, 0, sizeof(double2) * h->nnz, h->st));
+        k_spread_c128<<<ceil_div(h->nnz_in, 256), 256, 0, h->st>>>(h->nnz_in, tmp.p, h->vmap.p, h->a.p);
+    } else {
+        WT_CUDA(cudaMemcpyAsync(h->a.p, a, sizeof(double2) * h->nnz, cudaMemcpyHostToDevice, h->st));
+    }
     WT_CUDA(cudaStreamSynchronize(h->st));
     h->have_values = true;
     h->have_factor = false;
@@ -1757,18 +1792,27 @@ extern "C" int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *
     return WT3D_OK;
 }
 
+// Host analysis of a caller pattern as wt3d_solver_create_csr does it:
+// checked, symmetrised, ordered, and every entry mapped into its front.
+static int csr_analysis(int n, long long nnz, const int *irptr, const int *jcptr, int base, int leaf_dofs,
+                        Symbolic &S)
+{
+    int rc = check_csr(n, nnz, irptr, jcptr, base, false);
+    if (rc) return rc;
+    std::vector<int> hir, hjc, vmap;
+    std::vector<long long> map;
+    if ((rc = symmetrize(n, irptr, jcptr, base, hir, hjc, vmap)) ||
+        (rc = symbolic_graph(n, hir.data(), hjc.data(), 0, leaf_dofs > 0 ? leaf_dofs : GENERAL_LEAF_DOFS, S)) ||
+        (rc = scatter_map(S, hir, hjc, map)))
+        return rc;
+    return WT3D_OK;
+}
+
 extern "C" int wt3d_analyse_csr_info(int n, long long nnz, const int *irptr, const int *jcptr, int base,
                                      int leaf_dofs, long long *info, double *flops)
 {
     Symbolic S;
-    int rc = check_csr(n, nnz, irptr, jcptr, base, true);
-    if (rc || (rc = symbolic_graph(n, irptr, jcptr, base, leaf_dofs > 0 ? leaf_dofs : GENERAL_LEAF_DOFS, S)))
-        return rc;
-    std::vector<long long> map;
-    std::vector<int> hir(irptr, irptr + n + 1), hjc(jcptr, jcptr + nnz);
-    for (auto &v : hir) v -= base;
-    for (auto &v : hjc) v -= base;
-    if ((rc = scatter_map(S, hir, hjc, map))) return rc;
+    if (int rc = csr_analysis(n, nnz, irptr, jcptr, base, leaf_dofs, S)) return rc;
     analysis_info(S, info, flops);
     return WT3D_OK;
 }
@@ -1778,9 +1822,7 @@ extern "C" int wt3d_analyse_csr_export(int n, long long nnz, const int *irptr, c
                                        int *flevel, int *border, int *rel)
 {
     Symbolic S;
-    int rc = check_csr(n, nnz, irptr, jcptr, base, true);
-    if (rc || (rc = symbolic_graph(n, irptr, jcptr, base, leaf_dofs > 0 ? leaf_dofs : GENERAL_LEAF_DOFS, S)))
-        return rc;
+    if (int rc = csr_analysis(n, nnz, irptr, jcptr, base, leaf_dofs, S)) return rc;
     analysis_export(S, perm, fp, fb, ffirst, fparent, flevel, border, rel);
     return WT3D_OK;
 }

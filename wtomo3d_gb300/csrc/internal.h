@@ -74,6 +74,13 @@ int symbolic_grid(int nx, int ny, int nz, int leaf_nodes, Symbolic &S);
 // symbolic factorisation; leaf fronts hold at most leaf_dofs dofs.
 int symbolic_graph(long long n, const int *irptr, const int *jcptr, int base, long long leaf_dofs, Symbolic &S);
 
+// 0-based pattern of A + A^T (STRUMPACK orders unsymmetric patterns the same
+// way) from a checked CSR pattern: if A's pattern is already symmetric, sir/sjc
+// are A's own rows in the caller's order and vmap is empty; otherwise rows are
+// sorted and vmap[k] is the position of A's entry k in sjc.
+int symmetrize(long long n, const int *irptr, const int *jcptr, int base, std::vector<int> &sir,
+               std::vector<int> &sjc, std::vector<int> &vmap);
+
 // Check a CSR pattern: pointers start at the base and grow, columns in range,
 // no duplicates in a row and, if need_symmetric, structural symmetry.
 int check_csr(long long n, long long nnz, const int *irptr, const int *jcptr, int base, bool need_symmetric);

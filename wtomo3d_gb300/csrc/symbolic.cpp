@@ -468,6 +468,56 @@ int check_csr(long long n, long long nnz, const int *irptr, const int *jcptr, in
     return WT3D_OK;
 }
 
+int symmetrize(long long n, const int *irptr, const int *jcptr, int base, std::vector<int> &sir,
+               std::vector<int> &sjc, std::vector<int> &vmap)
+{
+    const long long nnz = (long long)irptr[n] - base;
+    // transpose lists: the rows holding each column
+    std::vector<long long> tptr(n + 1, 0);
+    for (long long k = 0; k < nnz; k++) tptr[jcptr[k] - base + 1]++;
+    for (long long r = 0; r < n; r++) tptr[r + 1] += tptr[r];
+    std::vector<int> trow(nnz);
+    {
+        std::vector<long long> cur(tptr.begin(), tptr.end() - 1);
+        for (long long r = 0; r < n; r++)
+            for (long long k = irptr[r] - base; k < irptr[r + 1] - base; k++) trow[cur[jcptr[k] - base]++] = (int)r;
+    }
+    // row r of A + A^T: row r of A, then the transposed entries it lacks
+    std::vector<int> mark(n, -1);
+    sir.assign(n + 1, 0);
+    sjc.clear();
+    sjc.reserve(nnz);
+    bool symmetric = true;
+    for (long long r = 0; r < n; r++) {
+        for (long long k = irptr[r] - base; k < irptr[r + 1] - base; k++) {
+            mark[jcptr[k] - base] = (int)r;
+            sjc.push_back(jcptr[k] - base);
+        }
+        for (long long k = tptr[r]; k < tptr[r + 1]; k++)
+            if (mark[trow[k]] != (int)r) {
+                mark[trow[k]] = (int)r;
+                sjc.push_back(trow[k]);
+                symmetric = false;
+            }
+        if ((long long)sjc.size() >= (1LL << 31)) {
+            set_error("CSR: the symmetrised pattern has 2^31 entries or more");
+            return WT3D_ERR_ARG;
+        }
+        sir[r + 1] = (int)sjc.size();
+    }
+    vmap.clear();
+    if (symmetric) return WT3D_OK;   // the caller's own order, no value map
+    // rows of the union in column order
+    for (long long r = 0; r < n; r++) std::sort(sjc.begin() + sir[r], sjc.begin() + sir[r + 1]);
+    vmap.resize(nnz);
+    for (long long r = 0; r < n; r++) {
+        const auto b = sjc.begin() + sir[r], e = sjc.begin() + sir[r + 1];
+        for (long long k = irptr[r] - base; k < irptr[r + 1] - base; k++)
+            vmap[k] = (int)(std::lower_bound(b, e, jcptr[k] - base) - sjc.begin());
+    }
+    return WT3D_OK;
+}
+
 int symbolic_graph(long long n, const int *irptr, const int *jcptr, int base, long long leaf_dofs, Symbolic &S)
 {
     if (n < 1 || !irptr) { set_error("symbolic_graph: empty matrix or null row pointers"); return WT3D_ERR_ARG; }
