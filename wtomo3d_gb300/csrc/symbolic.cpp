@@ -15,6 +15,8 @@
 #include <array>
 #include <cstring>
 #include <functional>
+#include <limits>
+#include <queue>
 
 namespace wt3d {
 
@@ -228,15 +230,359 @@ int symbolic_grid(int nx, int ny, int nz, int leaf_nodes, Symbolic &S)
 // nested-dissection reordering).  A pattern that is not the grid graph is
 // ordered here by automatic nested dissection (George and Liu, Computer
 // Solution of Large Sparse Positive Definite Systems, 1981, ch. 8): the
-// separator of a connected subgraph is one level of a breadth-first level
-// structure rooted at a pseudo-peripheral vertex, the smallest level that
-// leaves at least a fifth of the weight on either side, thinned to the
-// vertices that touch both sides.  A disconnected subgraph is split between
+// separator of a connected subgraph is the smaller of two candidates: one
+// level of a breadth-first level structure rooted at a pseudo-peripheral
+// vertex (the smallest level that leaves at least a fifth of the weight on
+// either side, thinned to the vertices that touch both sides), and the vertex
+// cover of a multilevel edge bisection (below).  A disconnected subgraph is split between
 // its components, and one vertex of the second group becomes the (trivial)
 // separator.  The graph is first compressed to supervariables, runs of
 // consecutive rows with the same column set (the 3 dofs of an elastic node),
 // so fronts never split a node.
 namespace {
+
+// ---- multilevel bisection (the METIS family of methods) -------------------
+// A connected subgraph is also bisected by the multilevel scheme of Karypis
+// and Kumar (SIAM J. Sci. Comput. 20(1), 1998): coarsen by heavy-edge
+// matching, grow a bisection of the coarsest graph greedily from several
+// seeds, refine the edge cut by Fiduccia-Mattheyses passes while projecting
+// back, and turn the cut into a vertex separator by a minimum vertex cover of
+// the cut edges (Konig's theorem on a maximum matching).  split() keeps the
+// smaller of this separator and the level-structure one.
+struct LGraph {
+    int n = 0;
+    std::vector<long long> xadj;
+    std::vector<int> adj, ew;   // neighbours and edge weights
+    std::vector<long long> vw;  // vertex weights
+};
+
+struct Rng {
+    unsigned long long s;
+    explicit Rng(unsigned long long seed) : s(seed * 0x9E3779B97F4A7C15ULL + 1) {}
+    unsigned next()
+    {
+        s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+        return (unsigned)(s >> 11);
+    }
+};
+
+// Heavy-edge matching; returns the coarse graph and cmap (fine -> coarse).
+LGraph coarsen(const LGraph &g, std::vector<int> &cmap, Rng &rng)
+{
+    std::vector<int> order(g.n), match(g.n, -1);
+    for (int v = 0; v < g.n; v++) order[v] = v;
+    for (int i = g.n - 1; i > 0; i--) std::swap(order[i], order[rng.next() % (unsigned)(i + 1)]);
+    for (int v : order) {
+        if (match[v] >= 0) continue;
+        int best = -1, bw = -1;
+        for (long long k = g.xadj[v]; k < g.xadj[v + 1]; k++) {
+            const int u = g.adj[k];
+            if (match[u] < 0 && u != v && g.ew[k] > bw) { bw = g.ew[k]; best = u; }
+        }
+        if (best >= 0) { match[v] = best; match[best] = v; }
+        else match[v] = v;
+    }
+    cmap.assign(g.n, -1);
+    int nc = 0;
+    for (int v = 0; v < g.n; v++)
+        if (cmap[v] < 0) { cmap[v] = nc; cmap[match[v]] = nc; nc++; }
+    LGraph c;
+    c.n = nc;
+    c.vw.assign(nc, 0);
+    c.xadj.assign(nc + 1, 0);
+    std::vector<int> first(nc, -1);
+    for (int v = 0; v < g.n; v++) {
+        c.vw[cmap[v]] += g.vw[v];
+        if (first[cmap[v]] < 0) first[cmap[v]] = v;
+    }
+    std::vector<int> mark(nc, -1);
+    std::vector<long long> pos(nc, 0);
+    for (int cv = 0; cv < nc; cv++) {
+        const int a = first[cv], b = match[a];
+        const int mem[2] = {a, b};
+        for (int t = 0; t < (b == a ? 1 : 2); t++) {
+            const int m = mem[t];
+            for (long long k = g.xadj[m]; k < g.xadj[m + 1]; k++) {
+                const int cu = cmap[g.adj[k]];
+                if (cu == cv) continue;
+                if (mark[cu] == cv) { c.ew[pos[cu]] += g.ew[k]; continue; }
+                mark[cu] = cv;
+                pos[cu] = (long long)c.adj.size();
+                c.adj.push_back(cu);
+                c.ew.push_back(g.ew[k]);
+            }
+        }
+        c.xadj[cv + 1] = (long long)c.adj.size();
+    }
+    return c;
+}
+
+long long edge_cut(const LGraph &g, const std::vector<char> &side)
+{
+    long long cut = 0;
+    for (int v = 0; v < g.n; v++)
+        for (long long k = g.xadj[v]; k < g.xadj[v + 1]; k++)
+            if (side[g.adj[k]] != side[v]) cut += g.ew[k];
+    return cut / 2;
+}
+
+// Fiduccia-Mattheyses passes on a two-way edge cut; sides stay within maxw
+// (a move out of an overweight side is always allowed).  External degrees
+// are kept up to date across moves, so a pass only touches the boundary.
+void fm_refine(const LGraph &g, std::vector<char> &side, long long maxw, int passes)
+{
+    long long pw[2] = {0, 0};
+    for (int v = 0; v < g.n; v++) pw[(int)side[v]] += g.vw[v];
+    std::vector<long long> ext(g.n, 0), tot(g.n, 0);
+    std::vector<int> bnd, locked(g.n, -1);
+    std::vector<char> inb(g.n, 0);
+    for (int v = 0; v < g.n; v++) {
+        for (long long k = g.xadj[v]; k < g.xadj[v + 1]; k++) {
+            tot[v] += g.ew[k];
+            if (side[g.adj[k]] != side[v]) ext[v] += g.ew[k];
+        }
+        if (ext[v] > 0) { bnd.push_back(v); inb[v] = 1; }
+    }
+    auto flip = [&](int v) {   // move v to the other side, keeping ext[] exact
+        const int to = 1 - side[v];
+        side[v] = (char)to;
+        pw[1 - to] -= g.vw[v];
+        pw[to] += g.vw[v];
+        ext[v] = tot[v] - ext[v];
+        for (long long k = g.xadj[v]; k < g.xadj[v + 1]; k++) {
+            const int u = g.adj[k];
+            ext[u] += side[u] == to ? -g.ew[k] : g.ew[k];
+            if (ext[u] > 0 && !inb[u]) { inb[u] = 1; bnd.push_back(u); }
+        }
+        if (ext[v] > 0 && !inb[v]) { inb[v] = 1; bnd.push_back(v); }
+    };
+    for (int pass = 0; pass < passes; pass++) {
+        // drop vertices that left the boundary
+        size_t w = 0;
+        for (int v : bnd) {
+            if (ext[v] > 0) bnd[w++] = v;
+            else inb[v] = 0;
+        }
+        bnd.resize(w);
+        std::priority_queue<std::pair<long long, int>> pq;
+        for (int v : bnd) pq.push({2 * ext[v] - tot[v], v});
+        std::vector<int> moves;
+        long long cut = 0, best = 0;
+        size_t best_n = 0;
+        long long best_over = std::max(pw[0], pw[1]);
+        while (!pq.empty()) {
+            auto [gv, v] = pq.top();
+            pq.pop();
+            if (locked[v] == pass || gv != 2 * ext[v] - tot[v]) continue;
+            const int from = side[v], to = 1 - from;
+            if (pw[to] + g.vw[v] > maxw && pw[from] <= maxw) continue;
+            locked[v] = pass;
+            flip(v);
+            cut -= gv;
+            moves.push_back(v);
+            for (long long k = g.xadj[v]; k < g.xadj[v + 1]; k++) {
+                const int u = g.adj[k];
+                if (locked[u] != pass) pq.push({2 * ext[u] - tot[u], u});
+            }
+            const long long over = std::max(pw[0], pw[1]);
+            const bool balanced = over <= maxw, best_bal = best_over <= maxw;
+            if ((balanced && !best_bal) || (balanced == best_bal && (cut < best || (cut == best && over < best_over)))) {
+                best = cut;
+                best_n = moves.size();
+                best_over = over;
+            }
+            if (moves.size() - best_n > 256) break;
+        }
+        for (size_t i = moves.size(); i > best_n; i--) flip(moves[i - 1]);
+        if (best_n == 0) break;
+    }
+}
+
+// Greedy graph growing from a seed until half the weight is on side 0: the
+// frontier vertex with the largest cut reduction next (breadth-first order
+// on a coarsest graph too large for the quadratic scan).
+void grow(const LGraph &g, int seed, std::vector<char> &side, long long half)
+{
+    side.assign(g.n, 1);
+    if (g.n > 2000) {
+        std::vector<int> q{seed};
+        std::vector<char> in(g.n, 0);
+        in[seed] = 1;
+        long long w0 = 0;
+        for (size_t qi = 0; w0 < half; qi++) {
+            if (qi == q.size()) {   // next component
+                int u = 0;
+                while (u < g.n && in[u]) u++;
+                if (u == g.n) break;
+                in[u] = 1;
+                q.push_back(u);
+            }
+            const int v = q[qi];
+            side[v] = 0;
+            w0 += g.vw[v];
+            for (long long k = g.xadj[v]; k < g.xadj[v + 1]; k++)
+                if (!in[g.adj[k]]) { in[g.adj[k]] = 1; q.push_back(g.adj[k]); }
+        }
+        return;
+    }
+    std::vector<long long> gain(g.n, 0);
+    std::vector<char> front(g.n, 0);
+    long long w0 = 0;
+    int v = seed;
+    for (;;) {
+        side[v] = 0;
+        w0 += g.vw[v];
+        if (w0 >= half) break;
+        for (long long k = g.xadj[v]; k < g.xadj[v + 1]; k++) {
+            const int u = g.adj[k];
+            if (side[u] == 0) continue;
+            front[u] = 1;
+            gain[u] += 2LL * g.ew[k];
+        }
+        int best = -1;
+        for (int u = 0; u < g.n; u++)
+            if (side[u] == 1 && front[u] && (best < 0 || gain[u] > gain[best])) best = u;
+        if (best < 0)
+            for (int u = 0; u < g.n && best < 0; u++)
+                if (side[u] == 1) best = u;
+        if (best < 0) break;
+        v = best;
+    }
+}
+
+// Minimum vertex cover of the bipartite cut graph (side-0 and side-1
+// endpoints of cut edges): maximum matching by Hopcroft and Karp (SIAM J.
+// Comput. 2(4), 1973), then Konig's construction.
+std::vector<int> cut_cover(const LGraph &g, const std::vector<char> &side)
+{
+    std::vector<int> L, R, id(g.n, -1);
+    for (int v = 0; v < g.n; v++) {
+        bool cut = false;
+        for (long long k = g.xadj[v]; k < g.xadj[v + 1] && !cut; k++) cut = side[g.adj[k]] != side[v];
+        if (!cut) continue;
+        if (side[v] == 0) { id[v] = (int)L.size(); L.push_back(v); }
+        else { id[v] = (int)R.size(); R.push_back(v); }
+    }
+    const int nl = (int)L.size(), nr = (int)R.size();
+    std::vector<long long> bx(nl + 1, 0);   // cut edges from each L vertex to R
+    std::vector<int> bj;
+    for (int l = 0; l < nl; l++) {
+        const int v = L[l];
+        for (long long k = g.xadj[v]; k < g.xadj[v + 1]; k++)
+            if (side[g.adj[k]] == 1) bj.push_back(id[g.adj[k]]);
+        bx[l + 1] = (long long)bj.size();
+    }
+    std::vector<int> mL(nl, -1), mR(nr, -1), dist(nl);
+    std::vector<long long> it(nl);
+    const int INF = std::numeric_limits<int>::max();
+    for (;;) {
+        // breadth-first layers from the free L vertices
+        std::vector<int> q;
+        for (int l = 0; l < nl; l++) {
+            dist[l] = mL[l] < 0 ? 0 : INF;
+            if (mL[l] < 0) q.push_back(l);
+        }
+        bool found = false;
+        for (size_t qi = 0; qi < q.size(); qi++) {
+            const int l = q[qi];
+            for (long long k = bx[l]; k < bx[l + 1]; k++) {
+                const int l2 = mR[bj[k]];
+                if (l2 < 0) found = true;
+                else if (dist[l2] == INF) { dist[l2] = dist[l] + 1; q.push_back(l2); }
+            }
+        }
+        if (!found) break;
+        // vertex-disjoint shortest augmenting paths along the layers
+        for (int l = 0; l < nl; l++) it[l] = bx[l];
+        std::vector<int> stk, path;
+        for (int l0 = 0; l0 < nl; l0++) {
+            if (mL[l0] >= 0 || dist[l0] != 0) continue;
+            stk.assign(1, l0);
+            path.clear();
+            while (!stk.empty()) {
+                const int l = stk.back();
+                if (it[l] == bx[l + 1]) {
+                    dist[l] = INF;
+                    stk.pop_back();
+                    if (!path.empty()) path.pop_back();
+                    continue;
+                }
+                const int r = bj[it[l]++];
+                const int l2 = mR[r];
+                if (l2 < 0) {
+                    path.push_back(r);
+                    for (size_t t = 0; t < stk.size(); t++) { mL[stk[t]] = path[t]; mR[path[t]] = stk[t]; }
+                    break;
+                }
+                if (dist[l2] != INF && dist[l2] == dist[l] + 1) {
+                    path.push_back(r);
+                    stk.push_back(l2);
+                }
+            }
+        }
+    }
+    // Z: reachable from free L vertices by alternating paths
+    std::vector<char> zl(nl, 0), zr(nr, 0);
+    std::vector<int> q;
+    for (int l = 0; l < nl; l++)
+        if (mL[l] < 0) { zl[l] = 1; q.push_back(l); }
+    for (size_t qi = 0; qi < q.size(); qi++) {
+        const int l = q[qi];
+        for (long long k = bx[l]; k < bx[l + 1]; k++) {
+            const int r = bj[k];
+            if (zr[r]) continue;
+            zr[r] = 1;
+            const int l2 = mR[r];
+            if (l2 >= 0 && !zl[l2]) { zl[l2] = 1; q.push_back(l2); }
+        }
+    }
+    std::vector<int> cover;
+    for (int l = 0; l < nl; l++)
+        if (!zl[l]) cover.push_back(L[l]);
+    for (int r = 0; r < nr; r++)
+        if (zr[r]) cover.push_back(R[r]);
+    return cover;
+}
+
+// Two-way multilevel bisection of g: side[v] in {0, 1}.
+void ml_bisect(const LGraph &g0, std::vector<char> &side, unsigned long long seed)
+{
+    Rng rng(seed);
+    std::vector<LGraph> gs;
+    std::vector<std::vector<int>> cmaps;
+    const LGraph *cur = &g0;
+    while (cur->n > 160 && gs.size() < 40) {
+        std::vector<int> cm;
+        LGraph c = coarsen(*cur, cm, rng);
+        if (c.n > (int)(0.92 * cur->n)) break;
+        cmaps.push_back(std::move(cm));
+        gs.push_back(std::move(c));
+        cur = &gs.back();
+    }
+    long long W = 0;
+    for (long long w : cur->vw) W += w;
+    const long long maxw = (long long)(0.55 * (double)W) + 1;
+    std::vector<char> best;
+    long long best_cut = -1;
+    const int trials = cur->n > 1000 ? 3 : 8;
+    for (int t = 0; t < trials; t++) {
+        std::vector<char> s;
+        grow(*cur, (int)(rng.next() % (unsigned)cur->n), s, W / 2);
+        fm_refine(*cur, s, maxw, 4);
+        const long long c = edge_cut(*cur, s);
+        if (best_cut < 0 || c < best_cut) { best_cut = c; best = s; }
+    }
+    side = best;
+    for (int lv = (int)gs.size() - 1; lv >= 0; lv--) {
+        const LGraph &fine = lv > 0 ? gs[lv - 1] : g0;
+        std::vector<char> fs(fine.n);
+        for (int v = 0; v < fine.n; v++) fs[v] = side[cmaps[lv][v]];
+        long long Wf = 0;
+        for (long long w : fine.vw) Wf += w;
+        fm_refine(fine, fs, (long long)(0.55 * (double)Wf) + 1, 10);
+        side.swap(fs);
+    }
+}
 
 struct GraphND {
     int nv = 0;                      // supervariables
@@ -252,6 +598,7 @@ struct GraphND {
     long long stamp = 0;
     int next_part = 1;
     std::vector<std::vector<int>> snodes;   // per front: supervariables, in numbering order
+    std::vector<int> lid;            // local index of each vertex inside the subset being split
     static constexpr int MAXDEPTH = 256;
 
     explicit GraphND(Symbolic &s) : S(s) {}
@@ -349,7 +696,7 @@ struct GraphND {
         }
         // pseudo-peripheral root: restart from a minimum-degree vertex of the
         // last level while the level structure gets deeper
-        for (int it = 0; it < 8; it++) {
+        for (int it = 0; it < 3; it++) {
             int u = min_degree_vertex(L.back(), pid);
             std::vector<std::vector<int>> L2;
             int nl2 = bfs(u, pid, L2);
@@ -392,6 +739,59 @@ struct GraphND {
         for (int l = s + 1; l < nl; l++) s2.insert(s2.end(), L[l].begin(), L[l].end());
         if (useA) s1.insert(s1.end(), movA.begin(), movA.end());
         else s2.insert(s2.end(), movB.begin(), movB.end());
+        // the multilevel separator, if it is smaller
+        std::vector<int> mSep, m1, m2;
+        if (vs.size() >= 32 && multilevel(vs, pid, mSep, m1, m2) &&
+            split_score(mSep, m1, m2, W) < split_score(sep, s1, s2, W)) {
+            sep.swap(mSep);
+            s1.swap(m1);
+            s2.swap(m2);
+        }
+        return !sep.empty() && !s1.empty() && !s2.empty();
+    }
+
+    // Separator weight, or a penalty above any separator when a side holds
+    // less than a fifth of the weight.
+    long long split_score(const std::vector<int> &sep, const std::vector<int> &s1, const std::vector<int> &s2,
+                          long long W) const
+    {
+        if (sep.empty() || s1.empty() || s2.empty()) return std::numeric_limits<long long>::max();
+        const long long small = std::min(weight(s1), weight(s2));
+        return 5 * small >= W ? weight(sep) : W + (W - small);
+    }
+
+    // Multilevel bisection of subset pid turned into a vertex separator.
+    bool multilevel(const std::vector<int> &vs, int pid, std::vector<int> &sep, std::vector<int> &s1,
+                    std::vector<int> &s2)
+    {
+        LGraph g;
+        g.n = (int)vs.size();
+        for (int i = 0; i < g.n; i++) lid[vs[i]] = i;
+        g.xadj.assign(g.n + 1, 0);
+        g.vw.resize(g.n);
+        for (int i = 0; i < g.n; i++) {
+            const int v = vs[i];
+            g.vw[i] = wt[v];
+            for (long long k = xadj[v]; k < xadj[v + 1]; k++)
+                if (part[adj[k]] == pid) { g.adj.push_back(lid[adj[k]]); g.ew.push_back(1); }
+            g.xadj[i + 1] = (long long)g.adj.size();
+        }
+        // large subsets (whose separators dominate the flops) try three seeds
+        std::vector<char> side, best_side;
+        std::vector<int> cover;
+        long long best_w = -1;
+        const int tries = g.n >= 20000 ? 3 : 1;
+        for (int t = 0; t < tries; t++) {
+            ml_bisect(g, side, (unsigned long long)pid * 7919ULL + (unsigned long long)t);
+            std::vector<int> c = cut_cover(g, side);
+            long long w = 0;
+            for (int i : c) w += g.vw[i];
+            if (best_w < 0 || w < best_w) { best_w = w; cover.swap(c); best_side.swap(side); }
+        }
+        side.swap(best_side);
+        std::vector<char> inc(g.n, 0);
+        for (int i : cover) inc[i] = 1;
+        for (int i = 0; i < g.n; i++) (inc[i] ? sep : side[i] == 0 ? s1 : s2).push_back(vs[i]);
         return !sep.empty() && !s1.empty() && !s2.empty();
     }
 
@@ -569,6 +969,7 @@ int symbolic_graph(long long n, const int *irptr, const int *jcptr, int base, lo
     G.part.assign(G.nv, 0);
     G.lev.assign(G.nv, 0);
     G.seen.assign(G.nv, 0);
+    G.lid.assign(G.nv, -1);
     std::vector<int> all(G.nv);
     for (int v = 0; v < G.nv; v++) all[v] = v;
     G.build(std::move(all), 0, 0);
