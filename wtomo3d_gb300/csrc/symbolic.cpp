@@ -15,7 +15,10 @@
 #include <array>
 #include <cstring>
 #include <functional>
+#include <atomic>
 #include <limits>
+#include <memory>
+#include <thread>
 #include <queue>
 
 namespace wt3d {
@@ -592,39 +595,53 @@ struct GraphND {
     std::vector<int> first_dof;      // first (old) dof of each supervariable
     long long leaf = 0;              // leaf fronts hold at most this many dofs
     Symbolic &S;
-    std::vector<int> part;           // subset id of each vertex; -1 once numbered
+    // Subset id of each vertex (-1 once it is in a front).  Disjoint subsets
+    // are dissected by concurrent threads: each writes only its own vertices,
+    // but reads the ids of neighbours in other subsets, hence atomics.
+    std::unique_ptr<std::atomic<int>[]> part;
     std::vector<int> lev;            // breadth-first level of each vertex
     std::vector<long long> seen;     // stamp of the last search that reached each vertex
-    long long stamp = 0;
-    int next_part = 1;
+    std::atomic<long long> stamp{0};
+    std::atomic<int> next_part{1};
     std::vector<std::vector<int>> snodes;   // per front: supervariables, in numbering order
     std::vector<int> lid;            // local index of each vertex inside the subset being split
     static constexpr int MAXDEPTH = 256;
+    static constexpr int PAR_DEPTH = 3;       // subtrees above this depth run on their own threads
+
+    struct Node {                    // dissection tree, numbered in postorder afterwards
+        std::vector<int> nodes;      // separator (or leaf) supervariables
+        std::unique_ptr<Node> child[2];
+        int depth = 0;
+    };
 
     explicit GraphND(Symbolic &s) : S(s) {}
+
+    int pid_of(int v) const { return part[v].load(std::memory_order_relaxed); }
+    void set_pid(int v, int id) { part[v].store(id, std::memory_order_relaxed); }
 
     int degree(int v, int pid) const
     {
         int d = 0;
-        for (long long k = xadj[v]; k < xadj[v + 1]; k++) d += part[adj[k]] == pid;
+        for (long long k = xadj[v]; k < xadj[v + 1]; k++) d += pid_of(adj[k]) == pid;
         return d;
     }
 
     // Level structure of the component of `root` inside subset pid: fills
     // `levels` (vertex lists); returns the number of levels.
-    int bfs(int root, int pid, std::vector<std::vector<int>> &levels)
+    int bfs(int root, int pid, std::vector<std::vector<int>> &levels, long long *used = nullptr)
     {
-        stamp++;
+        const long long st = ++stamp;   // unique, and larger than any earlier search's
+        if (used) *used = st;
         levels.assign(1, std::vector<int>{root});
-        seen[root] = stamp;
+        seen[root] = st;
         lev[root] = 0;
         for (int l = 0;; l++) {
             std::vector<int> nxt;
             for (int v : levels[l])
                 for (long long k = xadj[v]; k < xadj[v + 1]; k++) {
                     int u = adj[k];
-                    if (part[u] != pid || seen[u] == stamp) continue;
-                    seen[u] = stamp;
+                    if (pid_of(u) != pid || seen[u] == st) continue;
+                    seen[u] = st;
                     lev[u] = l + 1;
                     nxt.push_back(u);
                 }
@@ -653,19 +670,17 @@ struct GraphND {
 
     // Split subset pid (vertices vs, weight W) into sep, s1, s2 with no edge
     // between s1 and s2; false if no useful split exists.
-    bool split(const std::vector<int> &vs, int pid, long long W, std::vector<int> &sep, std::vector<int> &s1,
-               std::vector<int> &s2)
+    bool split(const std::vector<int> &vs, int pid, long long W, unsigned long long seed, std::vector<int> &sep,
+               std::vector<int> &s1, std::vector<int> &s2)
     {
         std::vector<std::vector<int>> L;
         int root = min_degree_vertex(vs, pid);
-        int nl = bfs(root, pid, L);
+        long long s0 = 0;   // stamps only grow: seen[v] >= s0 marks this split's searches
+        int nl = bfs(root, pid, L, &s0);
         long long reached = 0;
         for (auto &l : L) reached += weight(l);
         if (reached < W) {
-            // disconnected: components, heaviest first, to the lighter group.
-            // Stamps only grow, so seen[v] >= s0 marks the vertices reached
-            // by this split's searches.
-            const long long s0 = stamp;
+            // disconnected: components, heaviest first, to the lighter group
             std::vector<std::vector<int>> comps(1);
             for (auto &l : L) comps[0].insert(comps[0].end(), l.begin(), l.end());
             for (int v : vs) {
@@ -724,7 +739,7 @@ struct GraphND {
         auto touches = [&](int v, bool later) {
             for (long long k = xadj[v]; k < xadj[v + 1]; k++) {
                 int u = adj[k];
-                if (part[u] == pid && (later ? lev[u] > s : lev[u] < s)) return true;
+                if (pid_of(u) == pid && (later ? lev[u] > s : lev[u] < s)) return true;
             }
             return false;
         };
@@ -741,7 +756,7 @@ struct GraphND {
         else s2.insert(s2.end(), movB.begin(), movB.end());
         // the multilevel separator, if it is smaller
         std::vector<int> mSep, m1, m2;
-        if (vs.size() >= 32 && multilevel(vs, pid, mSep, m1, m2) &&
+        if (vs.size() >= 32 && multilevel(vs, pid, seed, mSep, m1, m2) &&
             split_score(mSep, m1, m2, W) < split_score(sep, s1, s2, W)) {
             sep.swap(mSep);
             s1.swap(m1);
@@ -761,8 +776,8 @@ struct GraphND {
     }
 
     // Multilevel bisection of subset pid turned into a vertex separator.
-    bool multilevel(const std::vector<int> &vs, int pid, std::vector<int> &sep, std::vector<int> &s1,
-                    std::vector<int> &s2)
+    bool multilevel(const std::vector<int> &vs, int pid, unsigned long long seed, std::vector<int> &sep,
+                    std::vector<int> &s1, std::vector<int> &s2)
     {
         LGraph g;
         g.n = (int)vs.size();
@@ -773,7 +788,7 @@ struct GraphND {
             const int v = vs[i];
             g.vw[i] = wt[v];
             for (long long k = xadj[v]; k < xadj[v + 1]; k++)
-                if (part[adj[k]] == pid) { g.adj.push_back(lid[adj[k]]); g.ew.push_back(1); }
+                if (pid_of(adj[k]) == pid) { g.adj.push_back(lid[adj[k]]); g.ew.push_back(1); }
             g.xadj[i + 1] = (long long)g.adj.size();
         }
         // large subsets (whose separators dominate the flops) try three seeds
@@ -782,7 +797,7 @@ struct GraphND {
         long long best_w = -1;
         const int tries = g.n >= 20000 ? 3 : 1;
         for (int t = 0; t < tries; t++) {
-            ml_bisect(g, side, (unsigned long long)pid * 7919ULL + (unsigned long long)t);
+            ml_bisect(g, side, seed * 7919ULL + (unsigned long long)t);
             std::vector<int> c = cut_cover(g, side);
             long long w = 0;
             for (int i : c) w += g.vw[i];
@@ -795,29 +810,46 @@ struct GraphND {
         return !sep.empty() && !s1.empty() && !s2.empty();
     }
 
-    int build(std::vector<int> vs, int pid, int depth)
+    // seed: the random streams of this subtree's bisections, fixed by the
+    // position in the tree so that the ordering does not depend on threads
+    std::unique_ptr<Node> dissect(std::vector<int> vs, int pid, int depth, unsigned long long seed)
     {
+        std::unique_ptr<Node> nd(new Node());
+        nd->depth = depth;
         const long long W = weight(vs);
-        Front f;
-        f.level = depth;
-        std::vector<int> nodes, s1, s2;
-        if (W > leaf && depth < MAXDEPTH && split(vs, pid, W, nodes, s1, s2)) {
+        std::vector<int> s1, s2;
+        if (W > leaf && depth < MAXDEPTH && split(vs, pid, W, seed, nd->nodes, s1, s2)) {
             const int p1 = next_part++, p2 = next_part++;
-            for (int v : s1) part[v] = p1;
-            for (int v : s2) part[v] = p2;
-            for (int v : nodes) part[v] = -1;
+            for (int v : s1) set_pid(v, p1);
+            for (int v : s2) set_pid(v, p2);
+            for (int v : nd->nodes) set_pid(v, -1);
             std::vector<int>().swap(vs);
-            f.child[0] = build(std::move(s1), p1, depth + 1);
-            f.child[1] = build(std::move(s2), p2, depth + 1);
-            f.nchild = 2;
+            if (depth < PAR_DEPTH && s1.size() + s2.size() >= 20000) {
+                std::thread t([&] { nd->child[0] = dissect(std::move(s1), p1, depth + 1, 2 * seed + 1); });
+                nd->child[1] = dissect(std::move(s2), p2, depth + 1, 2 * seed + 2);
+                t.join();
+            } else {
+                nd->child[0] = dissect(std::move(s1), p1, depth + 1, 2 * seed + 1);
+                nd->child[1] = dissect(std::move(s2), p2, depth + 1, 2 * seed + 2);
+            }
         } else {
-            nodes = std::move(vs);
-            for (int v : nodes) part[v] = -1;
+            nd->nodes = std::move(vs);
+            for (int v : nd->nodes) set_pid(v, -1);
         }
+        return nd;
+    }
+
+    // Fronts in postorder: children first, then the separator.
+    int number(Node &nd)
+    {
+        Front f;
+        f.level = nd.depth;
+        for (int c = 0; c < 2; c++)
+            if (nd.child[c]) f.child[f.nchild++] = number(*nd.child[c]);
         const int id = (int)S.fronts.size();
         for (int c = 0; c < f.nchild; c++) S.fronts[f.child[c]].parent = id;
         S.fronts.push_back(f);
-        snodes.push_back(std::move(nodes));
+        snodes.push_back(std::move(nd.nodes));
         return id;
     }
 };
@@ -966,13 +998,16 @@ int symbolic_graph(long long n, const int *irptr, const int *jcptr, int base, lo
     }
     S.nnodes = G.nv;
     // ---- nested dissection ----
-    G.part.assign(G.nv, 0);
+    G.part.reset(new std::atomic<int>[G.nv]);
+    for (int v = 0; v < G.nv; v++) G.set_pid(v, 0);
     G.lev.assign(G.nv, 0);
     G.seen.assign(G.nv, 0);
     G.lid.assign(G.nv, -1);
     std::vector<int> all(G.nv);
     for (int v = 0; v < G.nv; v++) all[v] = v;
-    G.build(std::move(all), 0, 0);
+    std::unique_ptr<GraphND::Node> root = G.dissect(std::move(all), 0, 0, 1);
+    G.number(*root);
+    root.reset();
     const int nf = (int)S.fronts.size();
     // ---- numbering: fronts in postorder, supervariables in list order ----
     std::vector<int> newsv(G.nv), dof0(G.nv);
