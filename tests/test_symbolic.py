@@ -219,21 +219,21 @@ def elastic_operator(oracle, nx, ny, nz):
 def test_general_grid_operator_fill_close_to_plane_separators(oracle):
     """The elastic operator's own pattern through the general analysis: the
     3 dofs of a node form one supervariable, the solve is exact, and the
-    factorisation costs at most 3x the flops of the plane-separator
-    ordering."""
+    factorisation costs at most 1.25x the flops of the plane-separator
+    ordering (1.05x measured)."""
     A = elastic_operator(oracle, 8, 7, 6)
     e = general_case(A, leaf=81)
     # supervariables of 3 dofs: every front holds whole nodes
     assert np.all(e["p"] % 3 == 0) and np.all(e["b"] % 3 == 0)
     eg = export(8, 7, 6, 27)
-    assert e["flops"] <= 3.0 * eg["flops"], (e["flops"], eg["flops"])
+    assert e["flops"] <= 1.25 * eg["flops"], (e["flops"], eg["flops"])
 
 
 def test_general_grid_fill_at_20_cubed(oracle):
     ir, jc = oracle.pattern(20, 20, 20)
     info, fl = wt.analyse_csr(ir, jc, base=1)
     eg = export(20, 20, 20, 64)
-    assert fl <= 3.0 * eg["flops"], (fl, eg["flops"])
+    assert fl <= 1.25 * eg["flops"], (fl, eg["flops"])     # 1.05x measured
 
 
 def test_general_node_permuted_operator(oracle):
@@ -353,3 +353,17 @@ def test_general_bad_patterns_are_rejected():
     with pytest.raises(wt.WT3DError) as e:
         wt.analyse_csr([1, 2, 3], [0, 1], base=0)
     assert e.value.code == wt.WT3D_ERR_PATTERN
+
+
+def test_general_ordering_is_deterministic(oracle):
+    """Subtrees of the general dissection run on several threads; the
+    bisections draw their random streams from the position in the tree, so
+    two analyses of the same pattern agree exactly (40^3: 64,000
+    supervariables, large enough for the threaded levels), and the ordering
+    stays within 1.15x of the plane separators' flops."""
+    ir, jc = oracle.pattern(40, 40, 40)
+    e1 = wt.analyse_csr_export(ir, jc, base=1)
+    e2 = wt.analyse_csr_export(ir, jc, base=1)
+    for k in ("perm", "p", "b", "parent", "border", "rel"):
+        np.testing.assert_array_equal(e1[k], e2[k])
+    assert e1["flops"] <= 1.15 * export(40, 40, 40, 64)["flops"]
