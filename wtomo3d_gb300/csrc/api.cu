@@ -1061,13 +1061,18 @@ int wt3d_solver_create_csr(wt3d_solver **out, int n, long long nnz, const int *i
     h->ga = std::make_shared<GridAnalysis>();
     GridAnalysis &ga = *h->ga;
     std::vector<int> hir, hjc, vmap;
-    if ((rc = symmetrize(n, irptr, jcptr, base, hir, hjc, vmap))) return rc;
-    if ((rc = symbolic_graph(n, hir.data(), hjc.data(), 0, GENERAL_LEAF_DOFS, ga.sym))) return rc;
+    try {   // host analysis: its only failure mode besides a bad pattern is host memory
+        if ((rc = symmetrize(n, irptr, jcptr, base, hir, hjc, vmap))) return rc;
+        if ((rc = symbolic_graph(n, hir.data(), hjc.data(), 0, GENERAL_LEAF_DOFS, ga.sym))) return rc;
+        if ((rc = scatter_map(ga.sym, hir, hjc, ga.map))) return rc;
+        ga.tpos = to_int(transpose_positions(n, hir.data(), hjc.data()));
+    } catch (const std::bad_alloc &) {
+        set_error("wt3d_solver_create_csr: out of host memory");
+        return WT3D_ERR_NOMEM;
+    }
     h->n = n;
     h->nnz = (long long)hjc.size();
     h->nnz_in = nnz;
-    if ((rc = scatter_map(ga.sym, hir, hjc, ga.map))) return rc;
-    ga.tpos = to_int(transpose_positions(n, hir.data(), hjc.data()));
     if ((rc = handle_streams(h.get()))) return rc;
     if ((rc = h->irptr.upload(hir)) || (rc = h->jcptr.upload(hjc)) || (rc = h->a.alloc(h->nnz))) return rc;
     if (!vmap.empty() && (rc = h->vmap.upload(vmap))) return rc;
@@ -1799,12 +1804,17 @@ static int csr_analysis(int n, long long nnz, const int *irptr, const int *jcptr
 {
     int rc = check_csr(n, nnz, irptr, jcptr, base, false);
     if (rc) return rc;
-    std::vector<int> hir, hjc, vmap;
-    std::vector<long long> map;
-    if ((rc = symmetrize(n, irptr, jcptr, base, hir, hjc, vmap)) ||
-        (rc = symbolic_graph(n, hir.data(), hjc.data(), 0, leaf_dofs > 0 ? leaf_dofs : GENERAL_LEAF_DOFS, S)) ||
-        (rc = scatter_map(S, hir, hjc, map)))
-        return rc;
+    try {
+        std::vector<int> hir, hjc, vmap;
+        std::vector<long long> map;
+        if ((rc = symmetrize(n, irptr, jcptr, base, hir, hjc, vmap)) ||
+            (rc = symbolic_graph(n, hir.data(), hjc.data(), 0, leaf_dofs > 0 ? leaf_dofs : GENERAL_LEAF_DOFS, S)) ||
+            (rc = scatter_map(S, hir, hjc, map)))
+            return rc;
+    } catch (const std::bad_alloc &) {
+        set_error("host analysis: out of host memory");
+        return WT3D_ERR_NOMEM;
+    }
     return WT3D_OK;
 }
 

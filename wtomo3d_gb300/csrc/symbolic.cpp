@@ -16,6 +16,9 @@
 #include <cstring>
 #include <functional>
 #include <atomic>
+#include <exception>
+#include <new>
+#include <system_error>
 #include <limits>
 #include <memory>
 #include <thread>
@@ -825,9 +828,26 @@ struct GraphND {
             for (int v : nd->nodes) set_pid(v, -1);
             std::vector<int>().swap(vs);
             if (depth < PAR_DEPTH && s1.size() + s2.size() >= 20000) {
-                std::thread t([&] { nd->child[0] = dissect(std::move(s1), p1, depth + 1, 2 * seed + 1); });
-                nd->child[1] = dissect(std::move(s2), p2, depth + 1, 2 * seed + 2);
-                t.join();
+                // the first subtree on a thread of its own (sequentially if no
+                // thread can be made); errors of either side reach the caller
+                std::exception_ptr e1, e2;
+                std::thread t;
+                try {
+                    t = std::thread([&] {
+                        try { nd->child[0] = dissect(std::move(s1), p1, depth + 1, 2 * seed + 1); }
+                        catch (...) { e1 = std::current_exception(); }
+                    });
+                } catch (const std::system_error &) {
+                }
+                try {
+                    if (!t.joinable()) nd->child[0] = dissect(std::move(s1), p1, depth + 1, 2 * seed + 1);
+                    nd->child[1] = dissect(std::move(s2), p2, depth + 1, 2 * seed + 2);
+                } catch (...) {
+                    e2 = std::current_exception();
+                }
+                if (t.joinable()) t.join();
+                if (e1) std::rethrow_exception(e1);
+                if (e2) std::rethrow_exception(e2);
             } else {
                 nd->child[0] = dissect(std::move(s1), p1, depth + 1, 2 * seed + 1);
                 nd->child[1] = dissect(std::move(s2), p2, depth + 1, 2 * seed + 2);
@@ -950,7 +970,21 @@ int symmetrize(long long n, const int *irptr, const int *jcptr, int base, std::v
     return WT3D_OK;
 }
 
+static int symbolic_graph_impl(long long n, const int *irptr, const int *jcptr, int base, long long leaf_dofs,
+                               Symbolic &S);
+
 int symbolic_graph(long long n, const int *irptr, const int *jcptr, int base, long long leaf_dofs, Symbolic &S)
+{
+    try {
+        return symbolic_graph_impl(n, irptr, jcptr, base, leaf_dofs, S);
+    } catch (const std::bad_alloc &) {
+        set_error("symbolic_graph: out of host memory");
+        return WT3D_ERR_NOMEM;
+    }
+}
+
+static int symbolic_graph_impl(long long n, const int *irptr, const int *jcptr, int base, long long leaf_dofs,
+                               Symbolic &S)
 {
     if (n < 1 || !irptr) { set_error("symbolic_graph: empty matrix or null row pointers"); return WT3D_ERR_ARG; }
     int rc = check_csr(n, (long long)irptr[n] - base, irptr, jcptr, base, true);
