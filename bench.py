@@ -497,6 +497,56 @@ def run_cpu(args, steps, warmup, workload=None):
                "detail": agg}
 
 
+def run_general(dims, nrhs=8, seed=5):
+    """The benchmark's operator (1 Hz, layered random model) through the
+    general-pattern path: the grid handle (plane separators) against a handle
+    of the same matrix under a random node permutation
+    (wt3d_solver_create_csr: multilevel ordering on the host, then the same
+    kernels).  Times are host wall clock around synchronous calls."""
+    import scipy.sparse as sp
+    import wtomo3d_gb300 as wt
+    from wtomo3d_gb300 import Grid, model
+    nx, ny, nz = dims
+    g = Grid(nx, ny, nz, 20.0, pmld=200.0, fst=1)
+    vp, vs, rho = model.layered_random(nx, ny, nz, 20.0, seed=1)
+    om = 2 * np.pi * 1.0
+    ir, jc = wt.pattern(nx, ny, nz, base=0)
+    A = sp.csr_matrix((wt.assemble(g, vp, vs, rho, om), jc, ir), shape=(g.n, g.n))
+    q = np.random.default_rng(seed).permutation(g.nnodes)
+    perm = (3 * q[:, None] + np.arange(3)).reshape(-1)
+    Ap = sp.csr_matrix(A[perm][:, perm])
+    Ap.sort_indices()
+    rng = np.random.default_rng(seed + 1)
+    B = np.zeros((g.n, nrhs), complex)
+    for j in range(nrhs):   # point forces away from the Dirichlet faces
+        node = rng.integers(0, nz - 1) + nz * (rng.integers(1, nx - 1) + nx * rng.integers(1, ny - 1))
+        B[3 * node + rng.integers(0, 3), j] = 1.0
+    out, X = {"workload": "%dx%dx%d, 1 Hz, %d point forces, node-permuted operator" % (nx, ny, nz, nrhs)}, {}
+    for name in ("grid", "general"):
+        t0 = time.perf_counter()
+        s = wt.Solver(g) if name == "grid" else wt.Solver.from_csr(Ap.indptr, Ap.indices)
+        t1 = time.perf_counter()
+        if name == "grid":
+            s.set_model(vp, vs, rho)
+            t2 = time.perf_counter()
+            s.factor(om)
+        else:
+            a = np.ascontiguousarray(Ap.data)
+            wt._check(wt.lib().wt3d_set_values_c128(s._h, wt._ptr(a)))
+            t2 = time.perf_counter()
+            wt._check(wt.lib().wt3d_factor_values(s._h))
+        t3 = time.perf_counter()
+        X[name] = s.solve(B if name == "grid" else B[perm], tol=1e-8)
+        t4 = time.perf_counter()
+        st = s.stats()
+        out[name] = {"analysis_s": t1 - t0, "factor_s": t3 - t2, "solve_s": t4 - t3, "solves_per_s": nrhs / (t4 - t3),
+                     "refinement_steps": s.last_iters, "relres_max": float(s.last_relres.max()),
+                     "factor_entries": st["factor_entries"], "factor_flops": st["factor_flops"]}
+        s.close()
+    out["wavefield_rel_diff"] = float(np.linalg.norm(X["grid"][perm] - X["general"]) / np.linalg.norm(X["grid"]))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -520,7 +570,12 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=0.3)
     ap.add_argument("--serve-reuse-requests", type=int, default=30)
     ap.add_argument("--serve-reuse-rate", type=float, default=0.5)
+    ap.add_argument("--general-pattern", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
+                    help="only time the general-pattern path against the grid path at this size")
     args = ap.parse_args()
+    if args.general_pattern:
+        print(json.dumps({"general_pattern": run_general(tuple(args.general_pattern))}))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
 
