@@ -98,3 +98,18 @@ def test_finter_refinement_setter_rejects_bad_arguments():
     assert L.wt3d_finter_set_refinement(0.0, 5) == wt.WT3D_ERR_ARG
     assert L.wt3d_finter_set_refinement(1e-8, -1) == wt.WT3D_ERR_ARG
     assert L.wt3d_finter_set_refinement(1e-10, 20) == 0
+
+
+def test_general_constructor_checks_pattern_before_device_work():
+    """wt3d_solver_create_csr refuses malformed patterns on the host, with or
+    without a GPU: no entries, duplicates, columns out of range, bad base."""
+    cases = [
+        ([0, 0, 0], [], 0),            # no entries
+        ([0, 2, 3], [0, 0, 1], 0),     # duplicate in row 0
+        ([0, 1, 2], [0, 7], 0),        # column out of range
+        ([1, 2, 3], [1, 2], 2),        # index base 2
+    ]
+    for ir, jc, base in cases:
+        with pytest.raises(wt.WT3DError) as e:
+            wt.Solver.from_csr(np.array(ir), np.array(jc, np.int32), base=base)
+        assert e.value.code in (wt.WT3D_ERR_PATTERN, wt.WT3D_ERR_ARG), (ir, jc, base, e.value.code)
