@@ -21,6 +21,7 @@
 #include <system_error>
 #include <limits>
 #include <memory>
+#include <mutex>
 #include <thread>
 #include <queue>
 
@@ -609,7 +610,7 @@ struct GraphND {
     std::vector<std::vector<int>> snodes;   // per front: supervariables, in numbering order
     std::vector<int> lid;            // local index of each vertex inside the subset being split
     static constexpr int MAXDEPTH = 256;
-    static constexpr int PAR_DEPTH = 3;       // subtrees above this depth run on their own threads
+    int par_depth = 3;               // subtrees above this depth run on their own threads
 
     struct Node {                    // dissection tree, numbered in postorder afterwards
         std::vector<int> nodes;      // separator (or leaf) supervariables
@@ -794,19 +795,49 @@ struct GraphND {
                 if (pid_of(adj[k]) == pid) { g.adj.push_back(lid[adj[k]]); g.ew.push_back(1); }
             g.xadj[i + 1] = (long long)g.adj.size();
         }
-        // large subsets (whose separators dominate the flops) try three seeds
-        std::vector<char> side, best_side;
-        std::vector<int> cover;
-        long long best_w = -1;
+        // large subsets (whose separators dominate the flops) try three
+        // seeds, on threads of their own; the first lightest cover wins, so
+        // the result does not depend on the threads
         const int tries = g.n >= 20000 ? 3 : 1;
-        for (int t = 0; t < tries; t++) {
-            ml_bisect(g, side, seed * 7919ULL + (unsigned long long)t);
-            std::vector<int> c = cut_cover(g, side);
-            long long w = 0;
-            for (int i : c) w += g.vw[i];
-            if (best_w < 0 || w < best_w) { best_w = w; cover.swap(c); best_side.swap(side); }
+        std::vector<std::vector<char>> sides(tries);
+        std::vector<std::vector<int>> covers(tries);
+        auto attempt = [&](int t) {
+            ml_bisect(g, sides[t], seed * 7919ULL + (unsigned long long)t);
+            covers[t] = cut_cover(g, sides[t]);
+        };
+        std::vector<std::thread> pool;
+        std::exception_ptr err;
+        std::mutex err_mu;
+        for (int t = 1; t < tries; t++) {
+            try {
+                pool.emplace_back([&, t] {
+                    try { attempt(t); }
+                    catch (...) { std::lock_guard<std::mutex> lk(err_mu); err = std::current_exception(); }
+                });
+            } catch (const std::system_error &) {
+                break;   // no thread: the remaining tries run below
+            }
         }
-        side.swap(best_side);
+        try {
+            attempt(0);
+            for (int t = (int)pool.size() + 1; t < tries; t++) attempt(t);
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(err_mu);
+            err = std::current_exception();
+        }
+        for (auto &th : pool) th.join();
+        if (err) std::rethrow_exception(err);
+        int bt = 0;
+        long long best_w = -1;
+        for (int t = 0; t < tries; t++) {
+            long long w = 0;
+            for (int i : covers[t]) w += g.vw[i];
+            if (best_w < 0 || w < best_w) { best_w = w; bt = t; }
+        }
+        std::vector<char> side;
+        std::vector<int> cover;
+        side.swap(sides[bt]);
+        cover.swap(covers[bt]);
         std::vector<char> inc(g.n, 0);
         for (int i : cover) inc[i] = 1;
         for (int i = 0; i < g.n; i++) (inc[i] ? sep : side[i] == 0 ? s1 : s2).push_back(vs[i]);
@@ -827,7 +858,7 @@ struct GraphND {
             for (int v : s2) set_pid(v, p2);
             for (int v : nd->nodes) set_pid(v, -1);
             std::vector<int>().swap(vs);
-            if (depth < PAR_DEPTH && s1.size() + s2.size() >= 20000) {
+            if (depth < par_depth && s1.size() + s2.size() >= 20000) {
                 // the first subtree on a thread of its own (sequentially if no
                 // thread can be made); errors of either side reach the caller
                 std::exception_ptr e1, e2;
@@ -1037,6 +1068,13 @@ static int symbolic_graph_impl(long long n, const int *irptr, const int *jcptr, 
     G.lev.assign(G.nv, 0);
     G.seen.assign(G.nv, 0);
     G.lid.assign(G.nv, -1);
+    {
+        // about one thread per hardware thread at the deepest threaded level
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        int d = 0;
+        while ((1u << (d + 1)) <= hw && d < 6) d++;
+        G.par_depth = std::max(1, d);
+    }
     std::vector<int> all(G.nv);
     for (int v = 0; v < G.nv; v++) all[v] = v;
     std::unique_ptr<GraphND::Node> root = G.dissect(std::move(all), 0, 0, 1);
