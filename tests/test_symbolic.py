@@ -367,3 +367,22 @@ def test_general_ordering_is_deterministic(oracle):
     for k in ("perm", "p", "b", "parent", "border", "rel"):
         np.testing.assert_array_equal(e1[k], e2[k])
     assert e1["flops"] <= 1.15 * export(40, 40, 40, 64)["flops"]
+
+
+def test_general_pathological_graphs():
+    """A diagonal matrix (every unknown its own component), a star (one
+    row coupled to all others) and a long cycle: balanced trees, the solve
+    over the exported structure still exact."""
+    n = 20000
+    e = wt.analyse_csr_export(np.arange(n + 1), np.arange(n), 0, 64)
+    check_structure(e, n)
+    assert e["info"][2] <= 20 and max(e["b"]) == 0      # no coupling, no borders
+    m = 400
+    rows = [list(range(m))] + [[0, i] for i in range(1, m)]
+    P = sp.csr_matrix((np.ones(sum(map(len, rows))), np.concatenate(rows),
+                       np.cumsum([0] + [len(r) for r in rows])), shape=(m, m))
+    general_case(random_values(P, 5), leaf=16)
+    c = 3000
+    C = sp.diags([np.ones(c - 1), np.ones(c), np.ones(c - 1)], [-1, 0, 1], format="lil")
+    C[0, c - 1] = C[c - 1, 0] = 1
+    general_case(random_values(sp.csr_matrix(C), 6), leaf=32)
