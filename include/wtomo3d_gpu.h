@@ -339,6 +339,11 @@ int wt3d_analyse_export(int nx, int ny, int nz, int leaf_nodes, int *perm, int *
 /* The same two for a general CSR pattern (as wt3d_solver_create_csr):
  * leaf_dofs <= 0 selects 192.  info also requires every entry to fall inside
  * its front (the scatter map). */
+/* 1 if the library was built with the CUDA toolkit's METIS
+ * (libmetis_static.a): the general ordering then also takes METIS's vertex
+ * separator (METIS_ComputeVertexSeparator) at every split where it is the
+ * smallest; 0 if not. */
+int wt3d_general_ordering_uses_metis(void);
 int wt3d_analyse_csr_info(int n, long long nnz, const int *irptr, const int *jcptr, int base, int leaf_dofs,
                           long long *info, double *flops);
 int wt3d_analyse_csr_export(int n, long long nnz, const int *irptr, const int *jcptr, int base, int leaf_dofs,

@@ -1818,6 +1818,8 @@ static int csr_analysis(int n, long long nnz, const int *irptr, const int *jcptr
     return WT3D_OK;
 }
 
+extern "C" int wt3d_general_ordering_uses_metis(void) { return metis_linked() ? 1 : 0; }
+
 extern "C" int wt3d_analyse_csr_info(int n, long long nnz, const int *irptr, const int *jcptr, int base,
                                      int leaf_dofs, long long *info, double *flops)
 {

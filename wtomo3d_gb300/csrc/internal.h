@@ -81,6 +81,10 @@ int symbolic_graph(long long n, const int *irptr, const int *jcptr, int base, lo
 int symmetrize(long long n, const int *irptr, const int *jcptr, int base, std::vector<int> &sir,
                std::vector<int> &sjc, std::vector<int> &vmap);
 
+// Whether the build linked the CUDA toolkit's METIS (its vertex separator is
+// then a candidate at every split of the general ordering).
+bool metis_linked();
+
 // Check a CSR pattern: pointers start at the base and grow, columns in range,
 // no duplicates in a row and, if need_symmetric, structural symmetry.
 int check_csr(long long n, long long nnz, const int *irptr, const int *jcptr, int base, bool need_symmetric);

@@ -16,6 +16,7 @@
 #include <cstring>
 #include <functional>
 #include <atomic>
+#include <cstdint>
 #include <exception>
 #include <new>
 #include <system_error>
@@ -25,7 +26,25 @@
 #include <thread>
 #include <queue>
 
+#ifdef WT3D_HAVE_METIS
+// METIS as it ships with the CUDA toolkit (libmetis_static.a, no header): the
+// two entry points of its public API used here, with its 64-bit index type
+// (checked by the build's probe program).
+extern "C" int METIS_SetDefaultOptions(int64_t *options);
+extern "C" int METIS_ComputeVertexSeparator(int64_t *nvtxs, int64_t *xadj, int64_t *adjncy, int64_t *vwgt,
+                                            int64_t *options, int64_t *sepsize, int64_t *part);
+#endif
+
 namespace wt3d {
+
+bool metis_linked()
+{
+#ifdef WT3D_HAVE_METIS
+    return true;
+#else
+    return false;
+#endif
+}
 
 namespace {
 
@@ -766,8 +785,57 @@ struct GraphND {
             s1.swap(m1);
             s2.swap(m2);
         }
+#ifdef WT3D_HAVE_METIS
+        // and METIS's vertex separator (the reference's ordering), if smaller still
+        std::vector<int> tSep, t1, t2;
+        if (vs.size() >= 32 && metis_separator(vs, pid, tSep, t1, t2) &&
+            split_score(tSep, t1, t2, W) < split_score(sep, s1, s2, W)) {
+            sep.swap(tSep);
+            s1.swap(t1);
+            s2.swap(t2);
+        }
+#endif
         return !sep.empty() && !s1.empty() && !s2.empty();
     }
+
+#ifdef WT3D_HAVE_METIS
+    // METIS_ComputeVertexSeparator on subset pid (calls serialised: the
+    // library's thread safety is not documented).
+    bool metis_separator(const std::vector<int> &vs, int pid, std::vector<int> &sep, std::vector<int> &s1,
+                         std::vector<int> &s2)
+    {
+        int64_t n = (int64_t)vs.size();
+        for (int64_t i = 0; i < n; i++) lid[vs[i]] = (int)i;
+        std::vector<int64_t> xa(n + 1, 0), ad, vw(n), part(n, -1);
+        for (int64_t i = 0; i < n; i++) {
+            const int v = vs[i];
+            vw[i] = wt[v];
+            for (long long k = xadj[v]; k < xadj[v + 1]; k++)
+                if (pid_of(adj[k]) == pid) ad.push_back(lid[adj[k]]);
+            xa[i + 1] = (int64_t)ad.size();
+        }
+        if (ad.empty()) return false;
+        int64_t opt[64] = {0}, sepsize = 0;
+        int rc;
+        {
+            static std::mutex metis_mu;
+            std::lock_guard<std::mutex> lk(metis_mu);
+            if (METIS_SetDefaultOptions(opt) != 1) return false;
+            rc = METIS_ComputeVertexSeparator(&n, xa.data(), ad.data(), vw.data(), opt, &sepsize, part.data());
+        }
+        if (rc != 1) return false;
+        for (int64_t i = 0; i < n; i++) {
+            if (part[i] < 0 || part[i] > 2) return false;
+            (part[i] == 2 ? sep : part[i] == 0 ? s1 : s2).push_back(vs[i]);
+        }
+        // a vertex separator: no edge between the two sides
+        for (int64_t i = 0; i < n; i++)
+            if (part[i] < 2)
+                for (int64_t k = xa[i]; k < xa[i + 1]; k++)
+                    if (part[ad[k]] == 1 - part[i]) return false;
+        return !sep.empty() && !s1.empty() && !s2.empty();
+    }
+#endif
 
     // Separator weight, or a penalty above any separator when a side holds
     // less than a fifth of the weight.
